@@ -1,0 +1,95 @@
+"""ctypes binding of libfocss_gpu.so (the C ABI in include/focss_gpu.h).
+
+The library is the only compute path: if it is missing or cannot find a GPU,
+calls raise.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfocss_gpu.so")
+
+FOCSS_OK = 0
+STATUS_NAMES = {
+    0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA", 4: "TIMEOUT", 5: "NOT_CONVERGED",
+    6: "UNSUPPORTED", 7: "NO_DEVICE",
+}
+
+D, I, P, U64, SZ = C.c_double, C.c_int, C.c_void_p, C.c_uint64, C.c_size_t
+
+
+class FocssError(RuntimeError):
+    def __init__(self, status, message=""):
+        self.status = status
+        super().__init__("focss status %s (%d): %s" % (STATUS_NAMES.get(status, "?"), status, message))
+
+
+class CDomain(C.Structure):
+    _fields_ = [("modes", I), ("samples", I), ("time_step", D), ("center_frequency", D)]
+
+
+class CFiber(C.Structure):
+    _fields_ = [("alpha", D), ("beta2", D), ("gamma", D), ("length", D), ("wavelength", D), ("kappa", D)]
+
+
+class CSsfmOpts(C.Structure):
+    _fields_ = [("grid", I), ("total_steps", I), ("maximum_phase_shift", D), ("maximum_step_size", D)]
+
+
+# name -> (restype, argtypes); every symbol the header declares is listed here
+# (tests check this table against include/*.h).
+SIGNATURES = {
+    "focss_abi_version": (I, []),
+    "focss_status_string": (C.c_char_p, [I]),
+    "focss_ctx_create": (I, [I, C.POINTER(P)]),
+    "focss_ctx_destroy": (I, [P]),
+    "focss_ctx_sync": (I, [P]),
+    "focss_ctx_stream": (P, [P]),
+    "focss_ctx_last_error": (C.c_char_p, [P]),
+    "focss_field_create": (I, [P, C.POINTER(CDomain), I, C.POINTER(P)]),
+    "focss_field_destroy": (I, [P]),
+    "focss_field_domain": (I, [P, C.POINTER(CDomain), C.POINTER(I)]),
+    "focss_field_upload": (I, [P, P, SZ]),
+    "focss_field_download": (I, [P, P, SZ]),
+    "focss_field_upload_c64": (I, [P, P, SZ]),
+    "focss_field_download_c64": (I, [P, P, SZ]),
+    "focss_field_copy": (I, [P, P]),
+    "focss_field_device_ptr": (P, [P]),
+    "focss_field_scale": (I, [P, D, D]),
+    "focss_field_power": (I, [P, P, P]),
+    "focss_field_fft": (I, [P]),
+    "focss_field_ifft": (I, [P]),
+    "focss_ssfm_run": (I, [P, P, C.POINTER(CFiber), C.POINTER(CSsfmOpts), D, P]),
+    "focss_amplifier_apply": (I, [P, P, D, D, U64, U64, I]),
+    "focss_forward_propagation": (I, [P, P, C.POINTER(CFiber), C.POINTER(CSsfmOpts), D, D, U64, U64, I]),
+    "focss_backward_propagation": (I, [P, P, C.POINTER(CFiber), C.POINTER(CSsfmOpts), D, I]),
+    "focss_cd_compensation": (I, [P, P, C.POINTER(CFiber), I]),
+}
+
+_lib = None
+
+
+def lib():
+    """Load libfocss_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise FocssError(6, "libfocss_gpu.so is not built (run __graft_entry__.build())")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status, ctx=None):
+    if status != FOCSS_OK:
+        msg = ""
+        if ctx:
+            raw = lib().focss_ctx_last_error(ctx)
+            msg = raw.decode() if raw else ""
+        raise FocssError(status, msg)

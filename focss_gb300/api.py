@@ -1,0 +1,300 @@
+"""Python mirror of the focss C++ API over the GB300 C ABI.
+
+Class and method names follow the reference (src/focss/field.h,
+src/focss/module/fiber.h, src/focss/module/amplifier.h,
+src/focss/solver/ssfm.h, src/tasks/systems.h) so that tests read like the
+reference's usage.  Fields live on the GPU (complex64); ``numpy()`` copies
+them back as complex128.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, replace
+
+import numpy as np
+
+from ._lib import CDomain, CFiber, CSsfmOpts, FocssError, check, lib
+
+# src/focss/definitions.h:13-15
+MATH_PI = 3.14159265358979323846264338
+PLANCK = 6.62607004081818181818181e-34
+LIGHT_SPEED = 299792458.0
+
+
+# ---- unit conversions (src/focss/functions.cpp:82-96): plain host arithmetic
+def db_to_linear(db):
+    return 10.0 ** (db / 10.0)
+
+
+def dbm_to_watts(dbm):
+    return 1e-3 * 10.0 ** (dbm / 10.0)
+
+
+def db_to_natural(db):
+    return db * math.log(10) / 10.0
+
+
+def disp_to_beta2(dispersion, wavelength):
+    return -wavelength * wavelength * dispersion / (2 * MATH_PI * LIGHT_SPEED)
+
+
+class Context:
+    """One CUDA stream + plans + scratch (one per host thread)."""
+
+    _default = None
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        check(lib().focss_ctx_create(device, C.byref(h)))
+        self.h = h
+        self.device = device
+
+    @classmethod
+    def default(cls):
+        if cls._default is None:
+            cls._default = Context(0)
+        return cls._default
+
+    def sync(self):
+        check(lib().focss_ctx_sync(self.h), self.h)
+
+    @property
+    def stream(self):
+        return lib().focss_ctx_stream(self.h)
+
+    def close(self):
+        if self.h:
+            lib().focss_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass(frozen=True)
+class Domain:
+    """src/focss/field.h:39-61"""
+
+    modes: int
+    samples: int
+    time_step: float
+    center_frequency: float = 0.0
+
+    def size(self):
+        return self.modes * self.samples
+
+
+@dataclass(frozen=True)
+class Fiber:
+    """src/focss/module/fiber.h:5-21 and fiber.cpp:4-45"""
+
+    alpha: float
+    beta2: float
+    gamma: float
+    length: float
+    wavelength: float = 1.55e-6
+    kappa: float = 1.0
+
+    def linear(self):
+        return replace(self, gamma=0.0)
+
+    def nonlinear(self):
+        return replace(self, alpha=0.0, beta2=0.0)
+
+    def dispersive(self):
+        return replace(self, alpha=0.0, gamma=0.0)
+
+    def __neg__(self):
+        return replace(self, alpha=-self.alpha, beta2=-self.beta2, gamma=-self.gamma)
+
+    def __mul__(self, f):
+        if f >= 0:
+            return replace(self, length=self.length * f)
+        return replace(self, alpha=-self.alpha, beta2=-self.beta2, gamma=-self.gamma,
+                       length=self.length * -f)
+
+    def c(self):
+        return CFiber(self.alpha, self.beta2, self.gamma, self.length, self.wavelength, self.kappa)
+
+
+class Field:
+    """Device field: `batch` realizations of one Domain (src/focss/field.h:63-181)."""
+
+    def __init__(self, domain: Domain, data=None, batch: int = 1, ctx: Context | None = None):
+        self.ctx = ctx or Context.default()
+        self.domain = domain
+        self.batch = batch
+        h = C.c_void_p()
+        d = CDomain(domain.modes, domain.samples, domain.time_step, domain.center_frequency)
+        check(lib().focss_field_create(self.ctx.h, C.byref(d), batch, C.byref(h)), self.ctx.h)
+        self.h = h
+        if data is not None:
+            self.upload(data)
+
+    @property
+    def shape(self):
+        return (self.batch, self.domain.modes, self.domain.samples)
+
+    def size(self):
+        return self.batch * self.domain.modes * self.domain.samples
+
+    def upload(self, data):
+        a = np.ascontiguousarray(np.asarray(data).reshape(self.shape))
+        if a.dtype == np.complex64:
+            check(lib().focss_field_upload_c64(self.h, a.ctypes.data_as(C.c_void_p), a.size), self.ctx.h)
+        else:
+            a = np.ascontiguousarray(a, dtype=np.complex128)
+            check(lib().focss_field_upload(self.h, a.ctypes.data_as(C.c_void_p), a.size), self.ctx.h)
+        return self
+
+    def numpy(self, dtype=np.complex128):
+        if dtype == np.complex64:
+            out = np.empty(self.shape, np.complex64)
+            check(lib().focss_field_download_c64(self.h, out.ctypes.data_as(C.c_void_p), out.size), self.ctx.h)
+        else:
+            out = np.empty(self.shape, np.complex128)
+            check(lib().focss_field_download(self.h, out.ctypes.data_as(C.c_void_p), out.size), self.ctx.h)
+        return out
+
+    def copy(self):
+        f = Field(self.domain, batch=self.batch, ctx=self.ctx)
+        check(lib().focss_field_copy(f.h, self.h), self.ctx.h)
+        return f
+
+    def assign(self, other: "Field"):
+        check(lib().focss_field_copy(self.h, other.h), self.ctx.h)
+        return self
+
+    def device_ptr(self):
+        return lib().focss_field_device_ptr(self.h)
+
+    # src/focss/field.cpp:381-391
+    def __imul__(self, s):
+        s = complex(s)
+        check(lib().focss_field_scale(self.h, s.real, s.imag), self.ctx.h)
+        return self
+
+    def power_stats(self):
+        avg = np.zeros(self.batch)
+        pk = np.zeros(self.batch)
+        check(lib().focss_field_power(self.h, avg.ctypes.data_as(C.c_void_p), pk.ctypes.data_as(C.c_void_p)),
+              self.ctx.h)
+        return avg, pk
+
+    def average_power(self):
+        return self.power_stats()[0]
+
+    def peak_power(self):
+        return self.power_stats()[1]
+
+    def fft_inplace(self):
+        check(lib().focss_field_fft(self.h), self.ctx.h)
+        return self
+
+    def ifft_inplace(self):
+        check(lib().focss_field_ifft(self.h), self.ctx.h)
+        return self
+
+    def dt(self):
+        return self.domain.time_step
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().focss_field_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class SSFM:
+    """src/focss/solver/ssfm.h:8-54"""
+
+    UNIFORM, LOGARITHMIC, ADAPTIVE = 0, 1, 2
+    FORWARD, BACKWARD = 1.0, -1.0
+
+    def __init__(self, fiber: Fiber | None = None, total_steps: int | None = None):
+        self.fiber = fiber
+        self.grid = SSFM.UNIFORM if total_steps is not None else None
+        self.total_steps = total_steps or 0
+        self.maximum_phase_shift = 0.0
+        self.maximum_step_size = 0.0
+
+    def set_fiber(self, fiber):
+        self.fiber = fiber
+
+    def set_grid(self, grid):
+        self.grid = grid
+
+    def set_total_steps(self, n):
+        self.total_steps = n
+
+    def set_maximum_phase_shift(self, x):
+        self.maximum_phase_shift = x
+
+    def set_maximum_step_size(self, x):
+        self.maximum_step_size = x
+
+    def opts(self):
+        if self.grid is None:
+            raise FocssError(1, "SSFM grid not set (the reference leaves it uninitialized)")
+        return CSsfmOpts(self.grid, self.total_steps, self.maximum_phase_shift, self.maximum_step_size)
+
+    def run(self, field: Field, direction: float = FORWARD):
+        steps = np.zeros(field.batch, np.int32)
+        fb, op = self.fiber.c(), self.opts()
+        check(lib().focss_ssfm_run(field.ctx.h, field.h, C.byref(fb), C.byref(op), direction,
+                                   steps.ctypes.data_as(C.c_void_p)), field.ctx.h)
+        return steps
+
+
+class Amplifier:
+    """src/focss/module/amplifier.h:7-22 (ASE from a seeded counter-based stream)."""
+
+    AMPLIFY, ADD_NOISE, GIVE_POWER, DROP_POWER = 0, 1, 2, 3
+
+    def __init__(self, gain: float = 1.0, noise_factor: float = 0.0, seed: int = 0):
+        self.gain = gain
+        self.noise_factor = noise_factor
+        self.seed = seed
+
+    def _apply(self, field, op, counter):
+        check(lib().focss_amplifier_apply(field.ctx.h, field.h, self.gain, self.noise_factor, self.seed,
+                                          counter, op), field.ctx.h)
+
+    def amplify(self, field, counter=0):
+        self._apply(field, Amplifier.AMPLIFY, counter)
+
+    def add_noise(self, field, counter=0):
+        self._apply(field, Amplifier.ADD_NOISE, counter)
+
+    def give_power(self, field):
+        self._apply(field, Amplifier.GIVE_POWER, 0)
+
+    def drop_power(self, field):
+        self._apply(field, Amplifier.DROP_POWER, 0)
+
+
+# ---- span drivers (src/tasks/systems.cpp:26-91)
+def forward_propagation(field: Field, fiber: Fiber, ssfm: SSFM, amplifier: Amplifier, spans: int, counter0=0):
+    fb, op = fiber.c(), ssfm.opts()
+    check(lib().focss_forward_propagation(field.ctx.h, field.h, C.byref(fb), C.byref(op), amplifier.gain,
+                                          amplifier.noise_factor, amplifier.seed, counter0, spans), field.ctx.h)
+
+
+def backward_propagation(field: Field, fiber: Fiber, ssfm: SSFM, gain: float, spans: int):
+    fb, op = fiber.c(), ssfm.opts()
+    check(lib().focss_backward_propagation(field.ctx.h, field.h, C.byref(fb), C.byref(op), gain, spans),
+          field.ctx.h)
+
+
+def cd_compensation(field: Field, fiber: Fiber, spans: int):
+    fb = fiber.c()
+    check(lib().focss_cd_compensation(field.ctx.h, field.h, C.byref(fb), spans), field.ctx.h)

@@ -1,0 +1,391 @@
+// capi.cu -- the extern "C" boundary (include/focss_gpu.h) over the kernels.
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+using fg::Ctx;
+using fg::Field;
+
+struct focss_ctx : Ctx {};
+struct focss_field : Field {};
+
+namespace fg {
+
+focss_status set_error(Ctx* ctx, focss_status st, const std::string& msg) {
+    if (ctx) ctx->last_error = msg;
+    return st;
+}
+
+focss_status cuda_check(Ctx* ctx, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return FOCSS_OK;
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return set_error(ctx, FOCSS_ERR_OOM, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+    return set_error(ctx, FOCSS_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+focss_status get_plan(Ctx* ctx, int N, const Plan** out) {
+    auto it = ctx->plans.find(N);
+    if (it != ctx->plans.end()) {
+        *out = &it->second;
+        return FOCSS_OK;
+    }
+    if (!fft_size_supported(N))
+        return set_error(ctx, FOCSS_ERR_UNSUPPORTED,
+                         "field length " + std::to_string(N) + " is not a power of two in [2^8, 2^20]");
+    Plan p;
+    int lg = 0;
+    while ((1 << lg) < N) ++lg;
+    p.N = N;
+    p.log2N1 = lg / 2;
+    p.log2N2 = lg - lg / 2;
+    p.N1 = 1 << p.log2N1;
+    p.N2 = 1 << p.log2N2;
+    // Twiddle tables from FP64, correctly rounded to FP32: [W_N1^e][W_N2^e][W_N^e (e < N2)].
+    std::vector<float2> h(p.N1 + 2 * (size_t)p.N2);
+    const double two_pi = 2.0 * 3.14159265358979323846;
+    for (int e = 0; e < p.N1; ++e)
+        h[e] = make_float2((float)std::cos(two_pi * e / p.N1), (float)-std::sin(two_pi * e / p.N1));
+    for (int e = 0; e < p.N2; ++e)
+        h[p.N1 + e] = make_float2((float)std::cos(two_pi * e / p.N2), (float)-std::sin(two_pi * e / p.N2));
+    for (int e = 0; e < p.N2; ++e)
+        h[p.N1 + p.N2 + e] = make_float2((float)std::cos(two_pi * e / N), (float)-std::sin(two_pi * e / N));
+    cudaError_t e = cudaMalloc(&p.tw, sizeof(float2) * h.size());
+    if (e != cudaSuccess) return cuda_check(ctx, e, "twiddle alloc");
+    e = cudaMemcpy(p.tw, h.data(), sizeof(float2) * h.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(p.tw);
+        return cuda_check(ctx, e, "twiddle upload");
+    }
+    auto res = ctx->plans.emplace(N, p);
+    *out = &res.first->second;
+    return FOCSS_OK;
+}
+
+focss_status ensure_state(Ctx* ctx, int batch) {
+    if (batch <= ctx->state_cap) return FOCSS_OK;
+    if (ctx->d_state) cudaFree(ctx->d_state);
+    ctx->d_state = nullptr;
+    ctx->state_cap = 0;
+    cudaError_t e = cudaMalloc(&ctx->d_state, sizeof(SsfmState) * (size_t)batch);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "state alloc");
+    ctx->state_cap = batch;
+    return FOCSS_OK;
+}
+
+focss_status ensure_red(Ctx* ctx, size_t doubles) {
+    if (doubles <= ctx->red_cap) return FOCSS_OK;
+    if (ctx->d_red) cudaFree(ctx->d_red);
+    ctx->d_red = nullptr;
+    ctx->red_cap = 0;
+    cudaError_t e = cudaMalloc(&ctx->d_red, sizeof(double) * doubles);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "reduction alloc");
+    ctx->red_cap = doubles;
+    return FOCSS_OK;
+}
+
+void* scratch_buffer(Ctx* ctx, int slot, size_t bytes) {
+    if ((int)ctx->scratch.size() <= slot) {
+        ctx->scratch.resize(slot + 1, nullptr);
+        ctx->scratch_cap.resize(slot + 1, 0);
+    }
+    if (ctx->scratch_cap[slot] >= bytes) return ctx->scratch[slot];
+    if (ctx->scratch[slot]) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(ctx->scratch[slot]);
+    }
+    ctx->scratch[slot] = nullptr;
+    ctx->scratch_cap[slot] = 0;
+    if (cudaMalloc(&ctx->scratch[slot], bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    ctx->scratch_cap[slot] = bytes;
+    return ctx->scratch[slot];
+}
+
+}  // namespace fg
+
+namespace {
+const double kPlanck = 6.62607004081818181818181e-34;  // src/focss/definitions.h:14
+
+bool same_shape(const Field* a, const Field* b) {
+    return a->modes == b->modes && a->samples == b->samples && a->batch == b->batch;
+}
+}  // namespace
+
+extern "C" {
+
+FOCSS_API int focss_abi_version(void) { return 1; }
+
+FOCSS_API const char* focss_status_string(int s) {
+    switch (s) {
+        case FOCSS_OK: return "ok";
+        case FOCSS_ERR_INVALID_ARG: return "invalid argument";
+        case FOCSS_ERR_OOM: return "out of memory";
+        case FOCSS_ERR_CUDA: return "CUDA error";
+        case FOCSS_ERR_TIMEOUT: return "timeout";
+        case FOCSS_ERR_NOT_CONVERGED: return "not converged";
+        case FOCSS_ERR_UNSUPPORTED: return "unsupported";
+        case FOCSS_ERR_NO_DEVICE: return "no CUDA device";
+        default: return "unknown status";
+    }
+}
+
+FOCSS_API focss_status focss_ctx_create(int device, focss_ctx** out) {
+    if (!out) return FOCSS_ERR_INVALID_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return FOCSS_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= n) return FOCSS_ERR_INVALID_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return FOCSS_ERR_CUDA;
+    focss_ctx* c = new (std::nothrow) focss_ctx();
+    if (!c) return FOCSS_ERR_OOM;
+    c->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_counters, sizeof(int) * 16);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_pinned, sizeof(int) * 16);
+    if (e != cudaSuccess) {
+        focss_ctx_destroy(c);
+        return e == cudaErrorMemoryAllocation ? FOCSS_ERR_OOM : FOCSS_ERR_CUDA;
+    }
+    *out = c;
+    return FOCSS_OK;
+}
+
+FOCSS_API focss_status focss_ctx_destroy(focss_ctx* c) {
+    if (!c) return FOCSS_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& kv : c->plans) cudaFree(kv.second.tw);
+    for (void* p : c->scratch) cudaFree(p);
+    cudaFree(c->d_state);
+    cudaFree(c->d_counters);
+    cudaFree(c->d_red);
+    if (c->h_pinned) cudaFreeHost(c->h_pinned);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return FOCSS_OK;
+}
+
+FOCSS_API focss_status focss_ctx_sync(focss_ctx* c) {
+    if (!c) return FOCSS_ERR_INVALID_ARG;
+    return fg::cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
+}
+
+FOCSS_API void* focss_ctx_stream(focss_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+FOCSS_API const char* focss_ctx_last_error(const focss_ctx* c) { return c ? c->last_error.c_str() : ""; }
+
+FOCSS_API focss_status focss_field_create(focss_ctx* c, const focss_domain* d, int batch, focss_field** out) {
+    if (!c || !d || !out) return FOCSS_ERR_INVALID_ARG;
+    *out = nullptr;
+    // src/focss/field.cpp:25 asserts modes > 0, samples > 0, time_step > 0.
+    if (d->modes <= 0 || d->samples <= 0 || !(d->time_step > 0) || batch <= 0)
+        return fg::set_error(c, FOCSS_ERR_INVALID_ARG, "field_create: modes, samples, time_step, batch must be > 0");
+    focss_field* f = new (std::nothrow) focss_field();
+    if (!f) return FOCSS_ERR_OOM;
+    f->ctx = c;
+    f->modes = d->modes;
+    f->samples = d->samples;
+    f->dt = d->time_step;
+    f->f0 = d->center_frequency;
+    f->batch = batch;
+    cudaError_t e = cudaMalloc(&f->d, sizeof(float2) * f->n());
+    if (e == cudaSuccess) e = cudaMemsetAsync(f->d, 0, sizeof(float2) * f->n(), c->stream);
+    if (e != cudaSuccess) {
+        cudaFree(f->d);
+        delete f;
+        return fg::cuda_check(c, e, "field alloc");
+    }
+    *out = f;
+    return FOCSS_OK;
+}
+
+FOCSS_API focss_status focss_field_destroy(focss_field* f) {
+    if (!f) return FOCSS_OK;
+    if (f->ctx) cudaStreamSynchronize(f->ctx->stream);
+    cudaFree(f->d);
+    delete f;
+    return FOCSS_OK;
+}
+
+FOCSS_API focss_status focss_field_domain(const focss_field* f, focss_domain* d, int* batch) {
+    if (!f) return FOCSS_ERR_INVALID_ARG;
+    if (d) *d = focss_domain{f->modes, f->samples, f->dt, f->f0};
+    if (batch) *batch = f->batch;
+    return FOCSS_OK;
+}
+
+FOCSS_API void* focss_field_device_ptr(focss_field* f) { return f ? (void*)f->d : nullptr; }
+
+FOCSS_API focss_status focss_field_upload_c64(focss_field* f, const float* h, size_t n) {
+    if (!f || !h) return FOCSS_ERR_INVALID_ARG;
+    if (n != f->n()) return fg::set_error(f->ctx, FOCSS_ERR_INVALID_ARG, "upload: size mismatch");
+    return fg::cuda_check(f->ctx,
+                          cudaMemcpyAsync(f->d, h, sizeof(float2) * n, cudaMemcpyHostToDevice, f->ctx->stream),
+                          "upload");
+}
+
+FOCSS_API focss_status focss_field_download_c64(focss_field* f, float* h, size_t n) {
+    if (!f || !h) return FOCSS_ERR_INVALID_ARG;
+    if (n != f->n()) return fg::set_error(f->ctx, FOCSS_ERR_INVALID_ARG, "download: size mismatch");
+    cudaError_t e = cudaMemcpyAsync(h, f->d, sizeof(float2) * n, cudaMemcpyDeviceToHost, f->ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(f->ctx->stream);
+    return fg::cuda_check(f->ctx, e, "download");
+}
+
+FOCSS_API focss_status focss_field_upload(focss_field* f, const double* h, size_t n) {
+    if (!f || !h) return FOCSS_ERR_INVALID_ARG;
+    if (n != f->n()) return fg::set_error(f->ctx, FOCSS_ERR_INVALID_ARG, "upload: size mismatch");
+    std::vector<float> tmp(2 * n);
+    for (size_t i = 0; i < 2 * n; ++i) tmp[i] = (float)h[i];
+    cudaError_t e = cudaMemcpyAsync(f->d, tmp.data(), sizeof(float2) * n, cudaMemcpyHostToDevice, f->ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(f->ctx->stream);
+    return fg::cuda_check(f->ctx, e, "upload");
+}
+
+FOCSS_API focss_status focss_field_download(focss_field* f, double* h, size_t n) {
+    if (!f || !h) return FOCSS_ERR_INVALID_ARG;
+    if (n != f->n()) return fg::set_error(f->ctx, FOCSS_ERR_INVALID_ARG, "download: size mismatch");
+    std::vector<float> tmp(2 * n);
+    cudaError_t e = cudaMemcpyAsync(tmp.data(), f->d, sizeof(float2) * n, cudaMemcpyDeviceToHost, f->ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(f->ctx->stream);
+    if (e != cudaSuccess) return fg::cuda_check(f->ctx, e, "download");
+    for (size_t i = 0; i < 2 * n; ++i) h[i] = (double)tmp[i];
+    return FOCSS_OK;
+}
+
+FOCSS_API focss_status focss_field_copy(focss_field* dst, const focss_field* src) {
+    if (!dst || !src) return FOCSS_ERR_INVALID_ARG;
+    if (!same_shape(dst, src)) return fg::set_error(dst->ctx, FOCSS_ERR_INVALID_ARG, "copy: shape mismatch");
+    return fg::cuda_check(dst->ctx,
+                          cudaMemcpyAsync(dst->d, src->d, sizeof(float2) * dst->n(), cudaMemcpyDeviceToDevice,
+                                          dst->ctx->stream),
+                          "copy");
+}
+
+FOCSS_API focss_status focss_field_scale(focss_field* f, double re, double im) {
+    if (!f) return FOCSS_ERR_INVALID_ARG;
+    return fg::cuda_check(f->ctx, fg::launch_scale(f->d, f->n(), make_float2((float)re, (float)im), f->ctx->stream),
+                          "scale");
+}
+
+FOCSS_API focss_status focss_field_power(focss_field* f, double* average, double* peak) {
+    if (!f) return FOCSS_ERR_INVALID_ARG;
+    Ctx* c = f->ctx;
+    focss_status st = fg::ensure_red(c, 2 * (size_t)f->batch);
+    if (st != FOCSS_OK) return st;
+    double* avg = c->d_red;
+    unsigned* pk = (unsigned*)(c->d_red + f->batch);
+    cudaError_t e = cudaMemsetAsync(c->d_red, 0, sizeof(double) * 2 * f->batch, c->stream);
+    if (e == cudaSuccess) e = fg::launch_power(f->d, f->modes, f->samples, f->batch, avg, pk, c->stream);
+    std::vector<double> ha(f->batch);
+    std::vector<unsigned> hp(f->batch);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ha.data(), avg, sizeof(double) * f->batch, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hp.data(), pk, sizeof(unsigned) * f->batch, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return fg::cuda_check(c, e, "power");
+    for (int b = 0; b < f->batch; ++b) {
+        if (average) average[b] = ha[b];
+        if (peak) {
+            float v;
+            std::memcpy(&v, &hp[b], sizeof(v));
+            peak[b] = v;
+        }
+    }
+    return FOCSS_OK;
+}
+
+FOCSS_API focss_status focss_field_fft(focss_field* f) {
+    if (!f) return FOCSS_ERR_INVALID_ARG;
+    return fg::fft_forward(f->ctx, f->d, f->samples, f->batch * f->modes);
+}
+
+FOCSS_API focss_status focss_field_ifft(focss_field* f) {
+    if (!f) return FOCSS_ERR_INVALID_ARG;
+    return fg::fft_inverse(f->ctx, f->d, f->samples, f->batch * f->modes);
+}
+
+FOCSS_API focss_status focss_ssfm_run(focss_ctx* c, focss_field* f, const focss_fiber* fiber,
+                                      const focss_ssfm_opts* opts, double direction, int* steps_out) {
+    if (!c || !f || !fiber || !opts) return FOCSS_ERR_INVALID_ARG;
+    if (f->ctx != c) return fg::set_error(c, FOCSS_ERR_INVALID_ARG, "field belongs to another context");
+    if (direction != 1.0 && direction != -1.0)
+        return fg::set_error(c, FOCSS_ERR_INVALID_ARG, "direction must be FOCSS_FORWARD or FOCSS_BACKWARD");
+    return fg::ssfm_run(c, f, *fiber, *opts, direction, steps_out);
+}
+
+FOCSS_API focss_status focss_amplifier_apply(focss_ctx* c, focss_field* f, double gain, double noise_factor,
+                                             uint64_t seed, uint64_t counter, int op) {
+    if (!c || !f) return FOCSS_ERR_INVALID_ARG;
+    if (!(gain > 0)) return fg::set_error(c, FOCSS_ERR_INVALID_ARG, "amplifier: gain must be > 0");
+    double scale = 1.0;
+    bool noise = false;
+    switch (op) {
+        case FOCSS_AMP_AMPLIFY: scale = std::sqrt(gain); noise = noise_factor != 0; break;     // :15-18
+        case FOCSS_AMP_ADD_NOISE: scale = 1.0; noise = true; break;                            // :20-28
+        case FOCSS_AMP_GIVE_POWER: scale = gain > 1 ? std::sqrt(gain) : std::sqrt(1 / gain); break;  // :30-35
+        case FOCSS_AMP_DROP_POWER: scale = gain < 1 ? std::sqrt(gain) : std::sqrt(1 / gain); break;  // :37-42
+        default: return fg::set_error(c, FOCSS_ERR_INVALID_ARG, "amplifier: unknown op");
+    }
+    double sigma = 0.0;
+    if (noise) {
+        // amplifier.cpp:21-27: variance = h f0 NF (G-1)/2 * (1/dt); sigma per quadrature = sqrt(var/2)
+        double variance = kPlanck * f->f0;
+        variance *= noise_factor * (gain - 1) / 2;
+        variance *= 1.0 / f->dt;
+        sigma = std::sqrt(variance / 2);
+    }
+    return fg::cuda_check(c,
+                          fg::launch_amplifier(f->d, f->modes, f->samples, f->batch, (float)scale, (float)sigma,
+                                               seed, counter, c->stream),
+                          "amplifier");
+}
+
+FOCSS_API focss_status focss_forward_propagation(focss_ctx* c, focss_field* f, const focss_fiber* fiber,
+                                                 const focss_ssfm_opts* opts, double gain, double noise_factor,
+                                                 uint64_t seed, uint64_t counter0, int spans) {
+    if (!c || !f || !fiber || !opts || spans < 0) return FOCSS_ERR_INVALID_ARG;
+    for (int i = 0; i < spans; ++i) {
+        focss_status st = focss_ssfm_run(c, f, fiber, opts, FOCSS_FORWARD, nullptr);
+        if (st != FOCSS_OK) return st;
+        st = focss_amplifier_apply(c, f, gain, noise_factor, seed, counter0 + (uint64_t)i, FOCSS_AMP_AMPLIFY);
+        if (st != FOCSS_OK) return st;
+    }
+    return FOCSS_OK;
+}
+
+FOCSS_API focss_status focss_backward_propagation(focss_ctx* c, focss_field* f, const focss_fiber* fiber,
+                                                  const focss_ssfm_opts* opts, double gain, int spans) {
+    if (!c || !f || !fiber || !opts || spans < 0) return FOCSS_ERR_INVALID_ARG;
+    for (int i = 0; i < spans; ++i) {
+        focss_status st = focss_amplifier_apply(c, f, gain, 0.0, 0, 0, FOCSS_AMP_DROP_POWER);
+        if (st != FOCSS_OK) return st;
+        st = focss_ssfm_run(c, f, fiber, opts, FOCSS_BACKWARD, nullptr);
+        if (st != FOCSS_OK) return st;
+    }
+    return FOCSS_OK;
+}
+
+FOCSS_API focss_status focss_cd_compensation(focss_ctx* c, focss_field* f, const focss_fiber* fiber, int spans) {
+    if (!c || !f || !fiber || spans < 0) return FOCSS_ERR_INVALID_ARG;
+    // fiber.dispersive() * spans (src/focss/module/fiber.cpp:17-22, 32-45), then UNIFORM 1 step BACKWARD.
+    focss_fiber d = *fiber;
+    d.alpha = 0;
+    d.gamma = 0;
+    d.length *= spans;
+    if (spans == 0) return FOCSS_OK;
+    focss_ssfm_opts o{FOCSS_UNIFORM, 1, 0.0, 0.0};
+    return focss_ssfm_run(c, f, &d, &o, FOCSS_BACKWARD, nullptr);
+}
+
+}  // extern "C"

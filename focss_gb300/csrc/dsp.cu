@@ -1,0 +1,126 @@
+// dsp.cu -- elementwise and reduction kernels around the SSFM passes:
+// amplifier gain + ASE noise, scaling, power statistics, layout transposes.
+#include "common.cuh"
+#include "internal.h"
+
+namespace fg {
+
+namespace {
+inline int grid_for(size_t n, int threads) {
+    size_t g = (n + threads - 1) / threads;
+    if (g > (size_t)152 * 32) g = (size_t)152 * 32;
+    return (int)(g ? g : 1);
+}
+}  // namespace
+
+__global__ void scale_kernel(float2* __restrict__ d, size_t n, float2 s) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        d[i] = cmul(d[i], s);
+}
+
+cudaError_t launch_scale(float2* d, size_t n, float2 s, cudaStream_t st) {
+    scale_kernel<<<grid_for(n, 256), 256, 0, st>>>(d, n, s);
+    return cudaGetLastError();
+}
+
+// Amplifier::amplify / add_noise (src/focss/module/amplifier.cpp:15-28):
+// A <- scale*A + sigma*(z0 + i z1), (z0, z1) Box-Muller on Philox4x32-10 with
+// counter {sample, mode + modes*realization, counter_lo, counter_hi}.
+__global__ void amplifier_kernel(float2* __restrict__ d, int modes, int samples, size_t n, float scale,
+                                 float sigma, uint2 key, uint32_t c_lo, uint32_t c_hi) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        float2 a = d[i];
+        a.x *= scale;
+        a.y *= scale;
+        if (sigma != 0.0f) {
+            const uint32_t sample = (uint32_t)(i % (size_t)samples);
+            const uint32_t stream = (uint32_t)(i / (size_t)samples);  // mode + modes*b
+            const uint4 r = philox4x32_10(make_uint4(sample, stream, c_lo, c_hi), key);
+            const float2 z = gaussian_pair(r.x, r.y);
+            a.x = fmaf(sigma, z.x, a.x);
+            a.y = fmaf(sigma, z.y, a.y);
+        }
+        d[i] = a;
+    }
+    (void)modes;
+}
+
+cudaError_t launch_amplifier(float2* d, int modes, int samples, int batch, float scale, float sigma,
+                             uint64_t seed, uint64_t counter, cudaStream_t st) {
+    const size_t n = (size_t)batch * modes * samples;
+    amplifier_kernel<<<grid_for(n, 256), 256, 0, st>>>(d, modes, samples, n, scale, sigma,
+                                                        make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)),
+                                                        (uint32_t)counter, (uint32_t)(counter >> 32));
+    return cudaGetLastError();
+}
+
+// Field::average_power / peak_power (src/focss/field.cpp:164-187) per
+// realization: avg[b] = sum_{modes,samples}|A|^2 / samples, peak_bits[b] = bits of
+// max_sample sum_modes |A|^2 (non-negative floats order like their bit patterns).
+// One block per (realization, chunk); FP64 accumulation of per-thread FP32 partials.
+__global__ void power_kernel(const float2* __restrict__ d, int modes, int samples, double* avg,
+                             unsigned int* peak_bits) {
+    const int b = blockIdx.y;
+    const float2* base = d + (size_t)b * modes * samples;
+    double s = 0.0;
+    float pk = 0.0f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < samples; i += gridDim.x * blockDim.x) {
+        float p = 0.0f;
+        for (int m = 0; m < modes; ++m) p += cnorm(base[i + (size_t)m * samples]);
+        s += (double)p;
+        pk = fmaxf(pk, p);
+    }
+    __shared__ double sd[32];
+    __shared__ float sf[64];
+    double tot = block_sum_d(s, sd);
+    float dummy = 0.0f;
+    block_max_sum(pk, dummy, sf);
+    if (threadIdx.x == 0) {
+        atomicAdd(avg + b, tot / samples);
+        atomicMax(peak_bits + b, __float_as_uint(pk));
+    }
+}
+
+cudaError_t launch_power(const float2* d, int modes, int samples, int batch, double* avg,
+                         unsigned int* peak_bits, cudaStream_t st) {
+    // avg and peak_bits must be zeroed.
+    int gx = (samples + 1023) / 1024;
+    if (gx > 64) gx = 64;
+    power_kernel<<<dim3(gx, batch), 256, 0, st>>>(d, modes, samples, avg, peak_bits);
+    return cudaGetLastError();
+}
+
+// Transposed spectrum layout (k1*N2 + k2 holds bin k1 + N1*k2) <-> natural.
+// Tiled 32x32 transpose through shared memory; batch on grid.z.
+__global__ void transpose_kernel(const float2* __restrict__ src, float2* __restrict__ dst, int rows, int cols) {
+    __shared__ float2 tile[32][33];
+    const size_t off = (size_t)blockIdx.z * rows * cols;
+    const int x = blockIdx.x * 32 + threadIdx.x;
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int y = blockIdx.y * 32 + k;
+        if (x < cols && y < rows) tile[k][threadIdx.x] = src[off + (size_t)y * cols + x];
+    }
+    __syncthreads();
+    const int x2 = blockIdx.y * 32 + threadIdx.x;
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int y2 = blockIdx.x * 32 + k;
+        if (x2 < rows && y2 < cols) dst[off + (size_t)y2 * rows + x2] = tile[threadIdx.x][k];
+    }
+}
+
+cudaError_t launch_transpose_to_natural(const float2* src, float2* dst, int N1, int N2, int batch,
+                                        cudaStream_t st) {
+    // src is N1 rows x N2 cols; natural index k1 + N1*k2 = dst row k2, col k1.
+    dim3 grid((N2 + 31) / 32, (N1 + 31) / 32, batch);
+    transpose_kernel<<<grid, dim3(32, 8), 0, st>>>(src, dst, N1, N2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_transpose_from_natural(const float2* src, float2* dst, int N1, int N2, int batch,
+                                          cudaStream_t st) {
+    dim3 grid((N1 + 31) / 32, (N2 + 31) / 32, batch);
+    transpose_kernel<<<grid, dim3(32, 8), 0, st>>>(src, dst, N2, N1);
+    return cudaGetLastError();
+}
+
+}  // namespace fg

@@ -1,0 +1,123 @@
+// internal.h -- host-side objects behind the C ABI (not installed).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/focss_gpu.h"
+
+namespace fg {
+
+// Per-realization SSFM state machine, device resident.  The last CTA of each
+// column pass advances it (no CTA ever waits on another).
+struct SsfmState {
+    double distance;               // |z| travelled (ADAPTIVE)
+    double h;                      // signed size of the next nonlinear step
+    double hl;                     // signed linear step of the next row pass
+    double sum;                    // sum |A|^2 accumulator (LOGARITHMIC estimate)
+    unsigned long long disp_fix;   // beta2/2*hl*dw^2/(2pi) as a 64-bit turn fraction
+    float lin_gain;                // exp(-alpha*hl/2)/N for the next row pass
+    int action;                    // next column-pass operation (ColOp)
+    int row_active;                // 1: data is spectral, next row pass applies hl
+    int final_step;                // current nonlinear step is the last of the span
+    int index;                     // step index (UNIFORM/LOGARITHMIC)
+    int n_steps;                   // step count (UNIFORM/LOGARITHMIC)
+    int steps;                     // steps done (ADAPTIVE, reference counting)
+    unsigned int peak_bits;        // atomicMax accumulator of the peak power (float bits)
+    unsigned int blocks_done;      // last-block ticket
+    int pad_;
+};
+
+enum ColOp : int { COL_FWD = 0, COL_KERR = 1, COL_INV = 2, COL_IDLE = 3 };
+enum RowOp : int { ROW_SSFM = 0, ROW_TABLE = 1, ROW_SCALE = 2, ROW_FWD = 3, ROW_INV = 4, ROW_BANDPASS = 5 };
+
+struct SsfmParams {
+    double alpha, beta2, gamma, kappa, length;
+    double direction;
+    double max_phase, max_step;
+    double dw;
+    int grid, total_steps;
+    int samples;
+    int* n_done;
+};
+
+struct PassArgs {
+    float2* data;           // batch x N complex64
+    const float2* tw;       // [W_N1^e, e<N1][W_N2^e, e<N2][W_N^e, e<N2]
+    const float2* table;    // ROW_TABLE multiplier, transposed layout (k1*N2 + k2), length N
+    SsfmState* state;       // null: plain transform driven by `op`
+    SsfmParams prm;
+    int N, N1, N2, log2N2;
+    int op;
+    float scale;
+    int bp_cut;
+};
+
+struct Plan {
+    int N = 0, N1 = 0, N2 = 0, log2N1 = 0, log2N2 = 0;
+    float2* tw = nullptr;   // device tables
+};
+
+struct Ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::map<int, Plan> plans;
+    std::string last_error;
+    SsfmState* d_state = nullptr;
+    int state_cap = 0;
+    int* d_counters = nullptr;       // small device scratch (n_done etc)
+    int* h_pinned = nullptr;         // pinned polling buffer
+    double* d_red = nullptr;         // reduction scratch
+    size_t red_cap = 0;
+    std::vector<void*> scratch;      // generic device scratch buffers
+    std::vector<size_t> scratch_cap;
+};
+
+struct Field {
+    Ctx* ctx = nullptr;
+    int modes = 0, samples = 0, batch = 0;
+    double dt = 0, f0 = 0;
+    float2* d = nullptr;
+    size_t n() const { return (size_t)batch * modes * samples; }
+};
+
+// ---- helpers implemented in capi.cu
+focss_status set_error(Ctx* ctx, focss_status st, const std::string& msg);
+focss_status cuda_check(Ctx* ctx, cudaError_t e, const char* what);
+focss_status get_plan(Ctx* ctx, int N, const Plan** out);
+focss_status ensure_state(Ctx* ctx, int batch);
+focss_status ensure_red(Ctx* ctx, size_t doubles);
+void* scratch_buffer(Ctx* ctx, int slot, size_t bytes);
+
+// ---- ssfm.cu
+bool fft_size_supported(int N);
+cudaError_t launch_col(const Plan& p, PassArgs a, int batch, cudaStream_t s);
+cudaError_t launch_row(const Plan& p, PassArgs a, int batch, cudaStream_t s);
+focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ssfm_opts& o, double dir,
+                      int* steps_out);
+// Plain transforms on a field buffer of `batch` x N (modes folded into batch).
+focss_status fft_forward(Ctx* ctx, float2* data, int N, int batch);   // natural order, x 1/N
+focss_status fft_inverse(Ctx* ctx, float2* data, int N, int batch);   // natural order, unnormalized
+// Forward then pointwise op then inverse, spectrum never leaves the two-pass layout.
+focss_status spectral_apply(Ctx* ctx, float2* data, int N, int batch, int row_op, const float2* table,
+                            float scale, int bp_cut);
+// Transposed-layout spectrum (k1*N2 + k2 holds bin k1 + N1*k2), x scale.
+focss_status fft_forward_transposed(Ctx* ctx, float2* data, int N, int batch, float scale);
+focss_status fft_inverse_transposed(Ctx* ctx, float2* data, int N, int batch);
+
+// ---- dsp.cu
+cudaError_t launch_scale(float2* d, size_t n, float2 s, cudaStream_t st);
+cudaError_t launch_amplifier(float2* d, int modes, int samples, int batch, float scale, float sigma,
+                             uint64_t seed, uint64_t counter, cudaStream_t st);
+cudaError_t launch_power(const float2* d, int modes, int samples, int batch, double* avg,
+                         unsigned int* peak_bits, cudaStream_t st);
+cudaError_t launch_transpose_to_natural(const float2* src, float2* dst, int N1, int N2, int batch,
+                                        cudaStream_t st);
+cudaError_t launch_transpose_from_natural(const float2* src, float2* dst, int N1, int N2, int batch,
+                                          cudaStream_t st);
+
+}  // namespace fg

@@ -1,0 +1,316 @@
+// ssfm.cu -- two-pass (six-step) split-step Fourier kernels for sm_103a.
+//
+// A field of N = N1*N2 complex64 samples is viewed as an N1 x N2 row-major
+// matrix (sample n = N2*n1 + n2).  One split step costs exactly two passes over
+// HBM, each one read and one write of the field (16 B per sample per pass):
+//
+//   column pass  [inverse six-step twiddle, inverse length-N1 FFT over n1]
+//                -> time domain: Kerr phase exp(i*kappa*gamma*h*|A|^2),
+//                   peak-power reduction (adaptive step estimate)
+//                -> [forward length-N1 FFT, forward six-step twiddle]
+//   row pass     [forward length-N2 FFT] -> exp(-alpha*hl/2)/N *
+//                exp(i*beta2/2*hl*w_k^2) -> [inverse length-N2 FFT]
+//
+// The spectrum never leaves the transposed layout (row k1, column k2 holds
+// bin k = k1 + N1*k2), so no transposes are needed.  The merged half steps of
+// the reference's Strang splitting (src/focss/solver/ssfm.cpp:62-118) appear
+// as one row pass with hl = (h_i + h_{i+1})/2.
+//
+// The dispersion phase is formed from an FP64 per-step scalar
+// a = beta2/2*hl*dw^2/(2*pi) (turns per k'^2) held as a 64-bit fixed-point
+// turn fraction; a*k'^2 mod 1 is then an exact wrapping 64-bit integer
+// product, so the FP32 sincospi argument is already range-reduced to [-1, 1).
+#include <cmath>
+
+#include "ssfm_kernels.cuh"
+
+namespace fg {
+
+// ---------------------------------------------------------------- dispatch
+namespace {
+int ilog2i(int n) {
+    int l = 0;
+    while ((1 << l) < n) ++l;
+    return (1 << l) == n ? l : -1;
+}
+}  // namespace
+
+Launch col_launch_4();
+Launch col_launch_5();
+Launch col_launch_6();
+Launch col_launch_7();
+Launch col_launch_8();
+Launch col_launch_9();
+Launch col_launch_10();
+Launch row_launch_4();
+Launch row_launch_5();
+Launch row_launch_6();
+Launch row_launch_7();
+Launch row_launch_8();
+Launch row_launch_9();
+Launch row_launch_10();
+
+Launch col_launch_for(int lg) {
+    switch (lg) {
+        case 4: return col_launch_4();
+        case 5: return col_launch_5();
+        case 6: return col_launch_6();
+        case 7: return col_launch_7();
+        case 8: return col_launch_8();
+        case 9: return col_launch_9();
+        case 10: return col_launch_10();
+        default: return Launch{};
+    }
+}
+
+Launch row_launch_for(int lg) {
+    switch (lg) {
+        case 4: return row_launch_4();
+        case 5: return row_launch_5();
+        case 6: return row_launch_6();
+        case 7: return row_launch_7();
+        case 8: return row_launch_8();
+        case 9: return row_launch_9();
+        case 10: return row_launch_10();
+        default: return Launch{};
+    }
+}
+
+bool fft_size_supported(int N) {
+    const int lg = ilog2i(N);
+    return lg >= 8 && lg <= 20;
+}
+
+cudaError_t launch_col(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
+    static Launch cache[16];
+    Launch& l = cache[p.log2N1];
+    if (!l.fn) l = col_launch_for(p.log2N1);
+    if (!l.fn) return cudaErrorInvalidValue;
+    const size_t smem = sizeof(float2) * ((size_t)p.N1 * l.per_block + p.N1 + p.N2);
+    if (!l.attr_set || smem > l.smem) {
+        cudaError_t e = cudaFuncSetAttribute((const void*)l.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        l.attr_set = true;
+        l.smem = smem;
+    }
+    a.N = p.N;
+    a.N1 = p.N1;
+    a.N2 = p.N2;
+    a.log2N2 = p.log2N2;
+    a.tw = p.tw;
+    dim3 grid(p.N2 / l.per_block, batch);
+    l.fn<<<grid, l.threads, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_row(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
+    static Launch cache[16];
+    Launch& l = cache[p.log2N2];
+    if (!l.fn) l = row_launch_for(p.log2N2);
+    if (!l.fn) return cudaErrorInvalidValue;
+    const int P = l.threads / l.per_block;
+    const int Q = p.N2 / P;
+    int R = l.per_block;
+    const size_t smem = sizeof(float2) * ((size_t)R * Q * (P + 1) + p.N2);
+    if (!l.attr_set || smem > l.smem) {
+        cudaError_t e = cudaFuncSetAttribute((const void*)l.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        l.attr_set = true;
+        l.smem = smem;
+    }
+    a.N = p.N;
+    a.N1 = p.N1;
+    a.N2 = p.N2;
+    a.log2N2 = p.log2N2;
+    a.tw = p.tw;
+    if (p.N1 % R != 0) return cudaErrorInvalidValue;
+    dim3 grid(p.N1 / R, batch);
+    l.fn<<<grid, l.threads, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- SSFM driver
+focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ssfm_opts& o, double dir,
+                      int* steps_out) {
+    if (f->modes != 1)
+        return set_error(ctx, FOCSS_ERR_UNSUPPORTED, "ssfm_run: only single-mode fields are implemented");
+    const int N = f->samples;
+    const Plan* p = nullptr;
+    focss_status st = get_plan(ctx, N, &p);
+    if (st != FOCSS_OK) return st;
+    if (o.grid == FOCSS_UNIFORM && o.total_steps <= 0)
+        return set_error(ctx, FOCSS_ERR_INVALID_ARG, "ssfm_run: total_steps must be > 0 for UNIFORM");
+    if (o.grid != FOCSS_UNIFORM && (!(o.maximum_step_size > 0) || !(o.maximum_phase_shift > 0)))
+        return set_error(ctx, FOCSS_ERR_INVALID_ARG,
+                         "ssfm_run: maximum_step_size and maximum_phase_shift must be > 0");
+    if (o.grid == FOCSS_LOGARITHMIC && !(fib.alpha != 0))
+        return set_error(ctx, FOCSS_ERR_INVALID_ARG, "ssfm_run: LOGARITHMIC grid needs alpha != 0");
+    if (!(fib.length > 0)) return set_error(ctx, FOCSS_ERR_INVALID_ARG, "ssfm_run: fiber length must be > 0");
+    if (o.grid < 0 || o.grid > 2) return set_error(ctx, FOCSS_ERR_INVALID_ARG, "ssfm_run: unknown grid");
+    st = ensure_state(ctx, f->batch);
+    if (st != FOCSS_OK) return st;
+    cudaStream_t s = ctx->stream;
+    st = cuda_check(ctx, cudaMemsetAsync(ctx->d_state, 0, sizeof(SsfmState) * f->batch, s), "memset state");
+    if (st != FOCSS_OK) return st;
+    st = cuda_check(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(int) * 4, s), "memset counters");
+    if (st != FOCSS_OK) return st;
+
+    PassArgs a{};
+    a.data = f->d;
+    a.state = ctx->d_state;
+    a.prm.alpha = fib.alpha;
+    a.prm.beta2 = fib.beta2;
+    a.prm.gamma = fib.gamma;
+    a.prm.kappa = fib.kappa;
+    a.prm.length = fib.length;
+    a.prm.direction = dir;
+    a.prm.max_phase = o.maximum_phase_shift;
+    a.prm.max_step = o.maximum_step_size;
+    a.prm.dw = 2.0 * 3.14159265358979323846 / (f->dt * N);  // Field::dw (field.cpp:220)
+    a.prm.grid = o.grid;
+    a.prm.total_steps = o.total_steps;
+    a.prm.samples = N;
+    a.prm.n_done = ctx->d_counters;
+
+    // Upper bound on column passes: UNIFORM is exact; the others are polled.
+    long long cap;
+    if (o.grid == FOCSS_UNIFORM) {
+        cap = (long long)o.total_steps + 2;
+    } else {
+        cap = 1ll << 20;
+    }
+    const int chunk = 16;
+    long long launched = 0;
+    bool done = false;
+    cudaEvent_t ev = nullptr;
+    if (o.grid != FOCSS_UNIFORM) {
+        st = cuda_check(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
+        if (st != FOCSS_OK) return st;
+    }
+    bool pending = false;
+    while (!done) {
+        const long long n = (o.grid == FOCSS_UNIFORM) ? cap : chunk;
+        for (long long i = 0; i < n; ++i) {
+            cudaError_t e = launch_col(*p, a, f->batch, s);
+            if (e == cudaSuccess) e = launch_row(*p, a, f->batch, s);
+            if (e != cudaSuccess) {
+                if (ev) cudaEventDestroy(ev);
+                return cuda_check(ctx, e, "ssfm pass launch");
+            }
+        }
+        launched += n;
+        if (o.grid == FOCSS_UNIFORM) break;
+        // Double-buffered poll: queue the next chunk before waiting on this one.
+        if (pending) {
+            cudaError_t e = cudaEventSynchronize(ev);
+            if (e != cudaSuccess) {
+                cudaEventDestroy(ev);
+                return cuda_check(ctx, e, "ssfm poll");
+            }
+            if (*(volatile int*)ctx->h_pinned >= f->batch) done = true;
+        }
+        if (!done) {
+            cudaMemcpyAsync(ctx->h_pinned, ctx->d_counters, sizeof(int), cudaMemcpyDeviceToHost, s);
+            cudaEventRecord(ev, s);
+            pending = true;
+        }
+        if (launched > cap) {
+            cudaEventDestroy(ev);
+            return set_error(ctx, FOCSS_ERR_NOT_CONVERGED, "ssfm_run: step cap reached");
+        }
+    }
+    if (ev) cudaEventDestroy(ev);
+    std::vector<SsfmState> hs(f->batch);
+    st = cuda_check(ctx,
+                    cudaMemcpyAsync(hs.data(), ctx->d_state, sizeof(SsfmState) * f->batch,
+                                    cudaMemcpyDeviceToHost, s),
+                    "state readback");
+    if (st != FOCSS_OK) return st;
+    st = cuda_check(ctx, cudaStreamSynchronize(s), "ssfm sync");
+    if (st != FOCSS_OK) return st;
+    for (int b = 0; b < f->batch; ++b) {
+        if (hs[b].action != COL_IDLE)
+            return set_error(ctx, FOCSS_ERR_TIMEOUT, "ssfm_run: a realization did not finish");
+        if (steps_out) steps_out[b] = (o.grid == FOCSS_ADAPTIVE) ? hs[b].steps : hs[b].n_steps;
+    }
+    return FOCSS_OK;
+}
+
+// ---------------------------------------------------------------- plain FFTs
+focss_status fft_forward_transposed(Ctx* ctx, float2* data, int N, int batch, float scale) {
+    const Plan* p = nullptr;
+    focss_status st = get_plan(ctx, N, &p);
+    if (st != FOCSS_OK) return st;
+    PassArgs a{};
+    a.data = data;
+    a.op = COL_FWD;
+    cudaError_t e = launch_col(*p, a, batch, ctx->stream);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "fft col");
+    a.op = ROW_FWD;
+    a.scale = scale;
+    return cuda_check(ctx, launch_row(*p, a, batch, ctx->stream), "fft row");
+}
+
+focss_status fft_inverse_transposed(Ctx* ctx, float2* data, int N, int batch) {
+    const Plan* p = nullptr;
+    focss_status st = get_plan(ctx, N, &p);
+    if (st != FOCSS_OK) return st;
+    PassArgs a{};
+    a.data = data;
+    a.op = ROW_INV;
+    cudaError_t e = launch_row(*p, a, batch, ctx->stream);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "ifft row");
+    a.op = COL_INV;
+    return cuda_check(ctx, launch_col(*p, a, batch, ctx->stream), "ifft col");
+}
+
+focss_status spectral_apply(Ctx* ctx, float2* data, int N, int batch, int row_op, const float2* table,
+                            float scale, int bp_cut) {
+    const Plan* p = nullptr;
+    focss_status st = get_plan(ctx, N, &p);
+    if (st != FOCSS_OK) return st;
+    PassArgs a{};
+    a.data = data;
+    a.op = COL_FWD;
+    cudaError_t e = launch_col(*p, a, batch, ctx->stream);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "spectral col");
+    a.op = row_op;
+    a.table = table;
+    a.scale = scale;
+    a.bp_cut = bp_cut;
+    e = launch_row(*p, a, batch, ctx->stream);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "spectral row");
+    a.op = COL_INV;
+    return cuda_check(ctx, launch_col(*p, a, batch, ctx->stream), "spectral col inv");
+}
+
+focss_status fft_forward(Ctx* ctx, float2* data, int N, int batch) {
+    const Plan* p = nullptr;
+    focss_status st = get_plan(ctx, N, &p);
+    if (st != FOCSS_OK) return st;
+    st = fft_forward_transposed(ctx, data, N, batch, 1.0f / (float)N);
+    if (st != FOCSS_OK) return st;
+    float2* tmp = (float2*)scratch_buffer(ctx, 0, sizeof(float2) * (size_t)N * batch);
+    if (!tmp) return set_error(ctx, FOCSS_ERR_OOM, "fft scratch");
+    cudaError_t e = launch_transpose_to_natural(data, tmp, p->N1, p->N2, batch, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(data, tmp, sizeof(float2) * (size_t)N * batch, cudaMemcpyDeviceToDevice, ctx->stream);
+    return cuda_check(ctx, e, "fft transpose");
+}
+
+focss_status fft_inverse(Ctx* ctx, float2* data, int N, int batch) {
+    const Plan* p = nullptr;
+    focss_status st = get_plan(ctx, N, &p);
+    if (st != FOCSS_OK) return st;
+    float2* tmp = (float2*)scratch_buffer(ctx, 0, sizeof(float2) * (size_t)N * batch);
+    if (!tmp) return set_error(ctx, FOCSS_ERR_OOM, "ifft scratch");
+    cudaError_t e = launch_transpose_from_natural(data, tmp, p->N1, p->N2, batch, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(data, tmp, sizeof(float2) * (size_t)N * batch, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "ifft transpose");
+    return fft_inverse_transposed(ctx, data, N, batch);
+}
+
+}  // namespace fg

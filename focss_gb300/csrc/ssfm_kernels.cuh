@@ -1,0 +1,316 @@
+// ssfm_kernels.cuh -- device code of the two-pass split-step kernels (see ssfm.cu
+// for the algorithm).  Each FFT length is instantiated in its own translation
+// unit (ssfm_len_*.cu) so the build compiles them in parallel.
+#pragma once
+#include <cmath>
+
+#include "fft.cuh"
+#include "internal.h"
+
+namespace fg {
+
+// ---------------------------------------------------------------- state update
+__device__ __forceinline__ double adaptive_estimate(const SsfmParams& p, float peak) {
+    // src/focss/solver/ssfm.cpp:136-140
+    const double argument = fabs(p.kappa * p.gamma);
+    const double phase_shift = argument * (double)peak;
+    const double h = p.max_phase / phase_shift;
+    return p.max_step < h ? p.max_step : h;
+}
+
+__device__ __forceinline__ double log_step(const SsfmParams& p, int K, int i) {
+    // src/focss/solver/ssfm.cpp:76-84
+    const double inv_alpha = -1.0 / p.alpha * p.direction;
+    double inv_gain = exp(-p.alpha * p.length) - 1;
+    inv_gain /= K;
+    return inv_alpha * log(1 + inv_gain / (1 + inv_gain * i));
+}
+
+__device__ __forceinline__ unsigned long long turns_fix64(double a) {
+    const double ab = fabs(a);
+    const double fr = ab - floor(ab);
+    const double sc = ldexp(fr, 64);
+    unsigned long long A = sc >= 18446744073709551615.0 ? 0ull : (unsigned long long)sc;
+    return a < 0 ? (0ull - A) : A;
+}
+
+__device__ __noinline__ static void ssfm_advance(SsfmState& s, const SsfmParams& p, int op_done, float peak,
+                                                double sum) {
+    if (op_done == COL_INV) {
+        s.action = COL_IDLE;
+        s.row_active = 0;
+        atomicAdd(p.n_done, 1);
+        return;
+    }
+    double hl;
+    if (op_done == COL_FWD) {
+        s.distance = 0;
+        s.index = 0;
+        s.steps = 1;
+        if (p.grid == FOCSS_UNIFORM) {
+            s.n_steps = p.total_steps;
+            s.h = p.direction * (p.length / p.total_steps);
+            s.final_step = p.total_steps == 1;
+        } else if (p.grid == FOCSS_LOGARITHMIC) {
+            // src/focss/solver/ssfm.cpp:120-134
+            const double avg = sum / p.samples;
+            const double L_nl = 1.0 / p.gamma / avg;
+            const double CL = p.max_phase * L_nl / p.kappa;
+            const double L_eff = (1.0 - exp(-p.alpha * p.length)) / p.alpha;
+            const double L_nl_eff = (1.0 - exp(-p.alpha * CL)) / p.alpha;
+            const int est = (int)(L_eff / L_nl_eff);
+            const int mn = (int)(p.length / p.max_step);
+            const int K = mn > est ? mn : est;
+            s.n_steps = K;
+            s.h = log_step(p, K, 0);
+            s.final_step = K == 1;
+        } else {
+            const double h0 = adaptive_estimate(p, peak);
+            if (h0 < p.length) {
+                s.h = p.direction * h0;
+                s.final_step = 0;
+            } else {
+                s.h = p.direction * p.length;
+                s.final_step = 1;
+            }
+        }
+        hl = 0.5 * s.h;
+        s.action = COL_KERR;
+    } else {  // COL_KERR finished with step s.h
+        if (s.final_step) {
+            hl = 0.5 * s.h;
+            s.action = COL_INV;
+        } else {
+            double next;
+            int fin;
+            if (p.grid == FOCSS_UNIFORM) {
+                const int i = ++s.index;
+                next = s.h;
+                fin = (i == s.n_steps - 1);
+            } else if (p.grid == FOCSS_LOGARITHMIC) {
+                const int i = ++s.index;
+                next = log_step(p, s.n_steps, i);
+                fin = (i == s.n_steps - 1);
+            } else {
+                s.distance += fabs(s.h);
+                s.steps++;
+                const double nm = adaptive_estimate(p, peak);
+                if (s.distance + nm < p.length) {
+                    next = p.direction * nm;
+                    fin = 0;
+                } else {
+                    next = p.direction * (p.length - s.distance);
+                    fin = 1;
+                }
+            }
+            hl = 0.5 * (s.h + next);
+            s.h = next;
+            s.final_step = fin;
+        }
+    }
+    s.hl = hl;
+    const double a = 0.5 * p.beta2 * hl * p.dw * p.dw / (2.0 * 3.14159265358979323846);
+    s.disp_fix = turns_fix64(a);
+    s.lin_gain = (float)(exp(-0.5 * p.alpha * hl) / (double)p.samples);
+    s.row_active = 1;
+}
+
+// ---------------------------------------------------------------- column pass
+template <int N1, int C>
+__global__ void __launch_bounds__(C* PQ<N1>::P, 2) col_kernel(const PassArgs a) {
+    constexpr int P = PQ<N1>::P, Q = PQ<N1>::Q;
+    extern __shared__ float2 smem[];
+    float2* sx = smem;            // N1*C exchange
+    float2* s_tc = sx + N1 * C;   // W_N1^e
+    float2* s_tl = s_tc + N1;     // W_N^e, e < N2
+    __shared__ float red[64];
+
+    const int b = blockIdx.y;
+    SsfmState* st = a.state ? a.state + b : nullptr;
+    int op = a.op;
+    if (st) {
+        op = *(volatile int*)&st->action;
+        if (op == COL_IDLE) return;
+    }
+    const int N2 = a.N2;
+    for (int i = threadIdx.x; i < N1; i += blockDim.x) s_tc[i] = a.tw[i];
+    for (int i = threadIdx.x; i < N2; i += blockDim.x) s_tl[i] = a.tw[N1 + N2 + i];
+
+    const int c = threadIdx.x % C, t = threadIdx.x / C;
+    const int n2 = blockIdx.x * C + c;
+    float2* base = a.data + (size_t)b * a.N + n2;
+    float2 v[Q];
+#pragma unroll
+    for (int j = 0; j < Q; ++j) v[j] = base[(size_t)(t + P * j) * N2];
+    __syncthreads();
+
+    const ColLayout<P, C> lay{c};
+    const int mask = N2 - 1, sh = a.log2N2;
+    float pk = 0.0f, sm = 0.0f;
+    if (op != COL_FWD) {
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+            const int e = n2 * (t + P * j);
+            v[j] = cmulc(v[j], cmul(s_tc[e >> sh], s_tl[e & mask]));
+        }
+        fft_pq<P, Q, true, true>(v, sx, lay, t, s_tc);
+    }
+    if (op == COL_KERR) {
+        const float coef = (float)(a.prm.kappa * a.prm.gamma * st->h);
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+            float s, cs;
+            sincosf(coef * cnorm(v[j]), &s, &cs);
+            v[j] = cmul(v[j], make_float2(cs, s));
+            pk = fmaxf(pk, cnorm(v[j]));
+        }
+    } else if (op == COL_FWD && st) {
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+            const float p = cnorm(v[j]);
+            pk = fmaxf(pk, p);
+            sm += p;
+        }
+    }
+    if (op == COL_FWD || op == COL_KERR) {
+        fft_pq<P, Q, false, true>(v, sx, lay, t, s_tc);
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+            const int e = n2 * (t + P * j);
+            v[j] = cmul(v[j], cmul(s_tc[e >> sh], s_tl[e & mask]));
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < Q; ++j) base[(size_t)(t + P * j) * N2] = v[j];
+
+    if (st) {
+        block_max_sum(pk, sm, red);
+        if (threadIdx.x == 0) {
+            if (op != COL_INV) {
+                atomicMax(&st->peak_bits, __float_as_uint(pk));
+                atomicAdd(&st->sum, (double)sm);
+            }
+            __threadfence();
+            const unsigned prev = atomicAdd(&st->blocks_done, 1u);
+            if (prev == gridDim.x - 1) {
+                __threadfence();
+                const float peak = __uint_as_float(atomicOr(&st->peak_bits, 0u));
+                const double sum = atomicAdd(&st->sum, 0.0);
+                ssfm_advance(*st, a.prm, op, peak, sum);
+                st->peak_bits = 0u;
+                st->sum = 0.0;
+                st->blocks_done = 0u;
+                __threadfence();
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- row pass
+template <int N2, int R>
+__global__ void __launch_bounds__(R* PQ<N2>::P, 2) row_kernel(const PassArgs a) {
+    constexpr int P = PQ<N2>::P, Q = PQ<N2>::Q;
+    extern __shared__ float2 smem[];
+    float2* sx = smem;                     // R * Q * (P+1)
+    float2* s_tw = sx + R * Q * (P + 1);   // W_N2^e
+
+    const int b = blockIdx.y;
+    const SsfmState* st = a.state ? a.state + b : nullptr;
+    unsigned long long fix = 0ull;
+    float g = a.scale;
+    if (st) {
+        if (!*(volatile const int*)&st->row_active) return;
+        fix = st->disp_fix;
+        g = st->lin_gain;
+    }
+    for (int i = threadIdx.x; i < N2; i += blockDim.x) s_tw[i] = a.tw[a.N1 + i];
+    const int rl = threadIdx.x / P, t = threadIdx.x % P;
+    const int k1 = blockIdx.x * R + rl;
+    float2* base = a.data + (size_t)b * a.N + (size_t)k1 * N2 + t;
+    float2 v[Q];
+#pragma unroll
+    for (int j = 0; j < Q; ++j) v[j] = base[P * j];
+    __syncthreads();
+    const RowLayout<P> lay{rl * Q * (P + 1)};
+    const int op = st ? (int)ROW_SSFM : a.op;
+    if (op != ROW_INV) fft_pq<P, Q, false, false>(v, sx, lay, t, s_tw);
+    const int N = a.N, N1 = a.N1;
+    if (op == ROW_SSFM) {
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+            const int k = k1 + N1 * (t + P * j);
+            const unsigned kp = (unsigned)(k <= (N >> 1) ? k : N - k);
+            const unsigned long long prod = fix * ((unsigned long long)kp * kp);
+            const float x = (float)(long long)prod * 1.0842021724855044e-19f;  // 2^-63
+            float s, cs;
+            sincospif(x, &s, &cs);
+            v[j] = cmul(v[j], make_float2(cs * g, s * g));
+        }
+    } else if (op == ROW_TABLE) {
+        const float2* tb = a.table + (size_t)k1 * N2 + t;
+#pragma unroll
+        for (int j = 0; j < Q; ++j) v[j] = cscale(cmul(v[j], tb[P * j]), g);
+    } else if (op == ROW_BANDPASS) {
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+            const int k = k1 + N1 * (t + P * j);
+            v[j] = (k >= a.bp_cut && k <= N - a.bp_cut) ? make_float2(0.f, 0.f) : cscale(v[j], g);
+        }
+    } else if (op != ROW_INV) {  // ROW_SCALE, ROW_FWD
+#pragma unroll
+        for (int j = 0; j < Q; ++j) v[j] = cscale(v[j], g);
+    }
+    if (op != ROW_FWD) fft_pq<P, Q, true, false>(v, sx, lay, t, s_tw);
+#pragma unroll
+    for (int j = 0; j < Q; ++j) base[P * j] = v[j];
+}
+
+
+typedef void (*PassFn)(PassArgs);
+struct Launch {
+    PassFn fn = nullptr;
+    int threads = 0, per_block = 0;
+    size_t smem = 0;
+    bool attr_set = false;
+};
+
+// Column-pass tile width: 16 columns (128-byte rows) up to N1 = 512, 8 above
+// (keeps 256 threads and the per-thread register budget at N1 = 1024).
+template <int N1>
+struct ColShape {
+    static constexpr int C = N1 >= 1024 ? 8 : 16;
+};
+// Row-pass rows per block: must divide N1 (N1 >= max(16, N2/2) for every plan).
+template <int N2>
+struct RowShape {
+    static constexpr int P = PQ<N2>::P;
+    static constexpr int R0 = 256 / P;
+    static constexpr int RH = (N2 / 2 > 16 ? N2 / 2 : 16);
+    static constexpr int R = R0 < RH ? R0 : RH;
+};
+
+Launch col_launch_for(int log2N1);
+Launch row_launch_for(int log2N2);
+
+}  // namespace fg
+
+#define FG_INSTANTIATE_COL(L, LG)                                              \
+    namespace fg {                                                             \
+    Launch col_launch_##LG() {                                                 \
+        Launch l;                                                              \
+        l.fn = col_kernel<L, ColShape<L>::C>;                                  \
+        l.threads = ColShape<L>::C * PQ<L>::P;                                 \
+        l.per_block = ColShape<L>::C;                                          \
+        return l;                                                              \
+    }                                                                          \
+    }
+#define FG_INSTANTIATE_ROW(L, LG)                                              \
+    namespace fg {                                                             \
+    Launch row_launch_##LG() {                                                 \
+        Launch l;                                                              \
+        l.fn = row_kernel<L, RowShape<L>::R>;                                  \
+        l.threads = RowShape<L>::R * PQ<L>::P;                                 \
+        l.per_block = RowShape<L>::R;                                          \
+        return l;                                                              \
+    }                                                                          \
+    }

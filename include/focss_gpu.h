@@ -1,0 +1,173 @@
+/*
+ * focss_gpu.h -- C ABI of the GB300 (sm_103a) implementation of the focss
+ * split-step Fourier / digital back-propagation / perturbation-equalizer path.
+ *
+ * The reference (focss) is a C++ class library with no FFI of its own; every
+ * entry point below replaces one reference member or free function, named in
+ * its comment (paths relative to the focss source tree).  Conventions:
+ *
+ *  - Plain C types only: opaque handles, pointers and sizes.
+ *  - Every call returns focss_status; nothing throws across the ABI.
+ *    focss_ctx_last_error() gives a human-readable reason for the last failure.
+ *  - A focss_field is device-resident (complex64, FP32) and holds `batch`
+ *    independent realizations of one Domain, each stored mode-major exactly
+ *    like focss::Field (data[sample + mode*samples], src/focss/field.cpp:140-155).
+ *    Host buffers passed to upload/download are interleaved (re, im).
+ *  - Calls on one context are ordered on the context's CUDA stream.  Calls
+ *    that return host values (reductions, step counts) synchronize the stream.
+ *  - One context per host thread; a context is not thread-safe.
+ *  - The library owns device memory; the caller owns host memory.
+ *  - There is no CPU fallback: without a usable GPU, focss_ctx_create fails.
+ */
+#ifndef FOCSS_GPU_H_
+#define FOCSS_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define FOCSS_API __attribute__((visibility("default")))
+#else
+#define FOCSS_API
+#endif
+
+typedef enum focss_status {
+    FOCSS_OK = 0,
+    FOCSS_ERR_INVALID_ARG = 1,  /* bad size, null pointer, mismatched domains   */
+    FOCSS_ERR_OOM = 2,          /* device or pinned allocation failed           */
+    FOCSS_ERR_CUDA = 3,         /* CUDA runtime error (see last_error)          */
+    FOCSS_ERR_TIMEOUT = 4,      /* a bounded device/host loop hit its cap       */
+    FOCSS_ERR_NOT_CONVERGED = 5,/* adaptive step loop exceeded its step cap     */
+    FOCSS_ERR_UNSUPPORTED = 6,  /* shape outside the implemented range          */
+    FOCSS_ERR_NO_DEVICE = 7     /* no CUDA device                                */
+} focss_status;
+
+typedef struct focss_ctx focss_ctx;
+typedef struct focss_field focss_field;
+
+/* focss::Domain (src/focss/field.h:39-61) */
+typedef struct focss_domain {
+    int modes;
+    int samples;
+    double time_step;
+    double center_frequency;
+} focss_domain;
+
+/* focss::Fiber (src/focss/module/fiber.h:5-12), SI units. */
+typedef struct focss_fiber {
+    double alpha;
+    double beta2;
+    double gamma;
+    double length;
+    double wavelength;
+    double kappa;
+} focss_fiber;
+
+/* SSFM grids and directions (src/focss/solver/ssfm.cpp:6-11). */
+#define FOCSS_UNIFORM 0
+#define FOCSS_LOGARITHMIC 1
+#define FOCSS_ADAPTIVE 2
+#define FOCSS_FORWARD 1.0
+#define FOCSS_BACKWARD (-1.0)
+
+/* SSFM configuration: the setters of focss::SSFM (src/focss/solver/ssfm.h:25-29). */
+typedef struct focss_ssfm_opts {
+    int grid;                    /* FOCSS_UNIFORM / _LOGARITHMIC / _ADAPTIVE      */
+    int total_steps;             /* set_total_steps (UNIFORM)                     */
+    double maximum_phase_shift;  /* set_maximum_phase_shift (ADAPTIVE, LOG)       */
+    double maximum_step_size;    /* set_maximum_step_size (ADAPTIVE, LOG)         */
+} focss_ssfm_opts;
+
+/* Amplifier operations (src/focss/module/amplifier.cpp:15-42). */
+#define FOCSS_AMP_AMPLIFY 0
+#define FOCSS_AMP_ADD_NOISE 1
+#define FOCSS_AMP_GIVE_POWER 2
+#define FOCSS_AMP_DROP_POWER 3
+
+/* ---------------------------------------------------------------- context */
+/* No reference counterpart (the reference is single-threaded host code);
+ * owns a CUDA stream, FFT twiddle tables and scratch. */
+FOCSS_API focss_status focss_ctx_create(int device, focss_ctx** out);
+FOCSS_API focss_status focss_ctx_destroy(focss_ctx* ctx);
+FOCSS_API focss_status focss_ctx_sync(focss_ctx* ctx);
+FOCSS_API void* focss_ctx_stream(focss_ctx* ctx); /* cudaStream_t */
+FOCSS_API const char* focss_ctx_last_error(const focss_ctx* ctx);
+FOCSS_API const char* focss_status_string(int status);
+FOCSS_API int focss_abi_version(void);
+
+/* ------------------------------------------------------------------ field */
+/* focss::Field(const Domain&) (src/focss/field.cpp:24-38): zero-filled.      */
+FOCSS_API focss_status focss_field_create(focss_ctx* ctx, const focss_domain* domain, int batch,
+                                          focss_field** out);
+/* ~Field (src/focss/field.cpp:130, 543-547) */
+FOCSS_API focss_status focss_field_destroy(focss_field* field);
+/* Field::domain() (src/focss/field.cpp:232-234) plus the batch count. */
+FOCSS_API focss_status focss_field_domain(const focss_field* field, focss_domain* domain, int* batch);
+/* Field(const Domain&, const ComplexVector&) (src/focss/field.cpp:40-54) and
+ * element reads Field::operator[] (:135-155): FP64 host <-> FP32 device.
+ * n_complex must equal batch*modes*samples. */
+FOCSS_API focss_status focss_field_upload(focss_field* field, const double* interleaved, size_t n_complex);
+FOCSS_API focss_status focss_field_download(focss_field* field, double* interleaved, size_t n_complex);
+/* Same, FP32 host buffers (no conversion; pinned buffers give full PCIe/C2C rate). */
+FOCSS_API focss_status focss_field_upload_c64(focss_field* field, const float* interleaved, size_t n_complex);
+FOCSS_API focss_status focss_field_download_c64(focss_field* field, float* interleaved, size_t n_complex);
+/* Field::operator=(const Field&) (src/focss/field.cpp:87-105); same shape. */
+FOCSS_API focss_status focss_field_copy(focss_field* dst, const focss_field* src);
+/* Device pointer to the complex64 data (for interop); valid until destroy. */
+FOCSS_API void* focss_field_device_ptr(focss_field* field);
+/* Field::operator*=(const complex_t&) (src/focss/field.cpp:387-391). */
+FOCSS_API focss_status focss_field_scale(focss_field* field, double re, double im);
+/* Field::average_power / peak_power (src/focss/field.cpp:173-187), per
+ * realization, FP64 accumulation.  Either output may be NULL. */
+FOCSS_API focss_status focss_field_power(focss_field* field, double* average, double* peak);
+/* Field::fft_inplace / ifft_inplace (src/focss/field.cpp:343-352): forward
+ * normalized by 1/N, inverse unnormalized, natural bin order. */
+FOCSS_API focss_status focss_field_fft(focss_field* field);
+FOCSS_API focss_status focss_field_ifft(focss_field* field);
+
+/* ------------------------------------------------------------------- SSFM */
+/* SSFM::run(Field&, Direction) (src/focss/solver/ssfm.cpp:39-60) for every
+ * realization of `field`: UNIFORM (:62-72), LOGARITHMIC (:74-90) or ADAPTIVE
+ * (:92-118).  steps_out (length batch, may be NULL) receives the step counts
+ * (UNIFORM: total_steps; LOGARITHMIC: the estimated count; ADAPTIVE: the
+ * reference's steps_done). */
+FOCSS_API focss_status focss_ssfm_run(focss_ctx* ctx, focss_field* field, const focss_fiber* fiber,
+                                      const focss_ssfm_opts* opts, double direction, int* steps_out);
+
+/* ------------------------------------------------------------- amplifier */
+/* Amplifier::amplify / add_noise / give_power / drop_power
+ * (src/focss/module/amplifier.cpp:15-42).  `gain` and `noise_factor` are the
+ * linear values the Amplifier constructor takes.  ASE noise comes from the
+ * counter-based Philox4x32-10 stream keyed by `seed`; `counter` selects an
+ * independent draw (e.g. the span index); realization b of the field uses an
+ * independent substream. */
+FOCSS_API focss_status focss_amplifier_apply(focss_ctx* ctx, focss_field* field, double gain,
+                                             double noise_factor, uint64_t seed, uint64_t counter,
+                                             int op);
+
+/* ----------------------------------------------------------- span loops */
+/* forward_propagation (src/tasks/systems.cpp:26-61): for each span, SSFM
+ * FORWARD with `opts`, then Amplifier(gain, noise_factor).amplify with noise
+ * counter = counter0 + span. */
+FOCSS_API focss_status focss_forward_propagation(focss_ctx* ctx, focss_field* field,
+                                                 const focss_fiber* fiber, const focss_ssfm_opts* opts,
+                                                 double gain, double noise_factor, uint64_t seed,
+                                                 uint64_t counter0, int spans);
+/* backward_propagation (src/tasks/systems.cpp:73-91): for each span,
+ * Amplifier(gain).drop_power then SSFM BACKWARD with `opts` (DBP). */
+FOCSS_API focss_status focss_backward_propagation(focss_ctx* ctx, focss_field* field,
+                                                  const focss_fiber* fiber, const focss_ssfm_opts* opts,
+                                                  double gain, int spans);
+/* cd_compensation (src/tasks/systems.cpp:63-71):
+ * SSFM(fiber.dispersive() * spans, 1).run(BACKWARD). */
+FOCSS_API focss_status focss_cd_compensation(focss_ctx* ctx, focss_field* field,
+                                             const focss_fiber* fiber, int spans);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FOCSS_GPU_H_ */
