@@ -69,6 +69,18 @@ SIGNATURES = {
 }
 
 _lib = None
+_shutting_down = False
+
+
+def _mark_shutdown():
+    global _shutting_down
+    _shutting_down = True
+
+
+def alive() -> bool:
+    """False once interpreter shutdown began: device objects are then left to
+    process teardown instead of being freed after the CUDA runtime is gone."""
+    return not _shutting_down
 
 
 def lib():
@@ -83,6 +95,8 @@ def lib():
             f.restype = res
             f.argtypes = args
         _lib = L
+        import atexit
+        atexit.register(_mark_shutdown)
     return _lib
 
 

@@ -14,7 +14,7 @@ from dataclasses import dataclass, replace
 
 import numpy as np
 
-from ._lib import CDomain, CFiber, CSsfmOpts, FocssError, check, lib
+from ._lib import CDomain, CFiber, CSsfmOpts, FocssError, alive, check, lib
 
 # src/focss/definitions.h:13-15
 MATH_PI = 3.14159265358979323846264338
@@ -64,9 +64,9 @@ class Context:
         return lib().focss_ctx_stream(self.h)
 
     def close(self):
-        if self.h:
+        if self.h and alive():
             lib().focss_ctx_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -203,9 +203,9 @@ class Field:
         return self.domain.time_step
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and alive():
             lib().focss_field_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:

@@ -46,18 +46,23 @@ focss_status get_plan(Ctx* ctx, int N, const Plan** out) {
     p.log2N2 = lg - lg / 2;
     p.N1 = 1 << p.log2N1;
     p.N2 = 1 << p.log2N2;
-    // Twiddle tables from FP64, correctly rounded to FP32: [W_N1^e][W_N2^e][W_N^e (e < N2)].
-    std::vector<float2> h(p.N1 + 2 * (size_t)p.N2);
+    // Twiddle tables from FP64 as double-float pairs {re_hi, im_hi, re_lo, im_lo}:
+    // [W_N1^e][W_N2^e][W_N^e (e < N2)][exp(+2 pi i j / 512)].
+    std::vector<float4> h(p.N1 + 2 * (size_t)p.N2 + 512);
     const double two_pi = 2.0 * 3.14159265358979323846;
-    for (int e = 0; e < p.N1; ++e)
-        h[e] = make_float2((float)std::cos(two_pi * e / p.N1), (float)-std::sin(two_pi * e / p.N1));
-    for (int e = 0; e < p.N2; ++e)
-        h[p.N1 + e] = make_float2((float)std::cos(two_pi * e / p.N2), (float)-std::sin(two_pi * e / p.N2));
-    for (int e = 0; e < p.N2; ++e)
-        h[p.N1 + p.N2 + e] = make_float2((float)std::cos(two_pi * e / N), (float)-std::sin(two_pi * e / N));
-    cudaError_t e = cudaMalloc(&p.tw, sizeof(float2) * h.size());
+    auto df = [](double re, double im) {
+        const float rh = (float)re, ih = (float)im;
+        return make_float4(rh, ih, (float)(re - (double)rh), (float)(im - (double)ih));
+    };
+    // cos/sin of 2 pi e / L evaluated on an exactly reduced argument (e mod L).
+    auto w = [&](long long e, long long L) { return df(std::cos(two_pi * e / L), -std::sin(two_pi * e / L)); };
+    for (int e = 0; e < p.N1; ++e) h[e] = w(e, p.N1);
+    for (int e = 0; e < p.N2; ++e) h[p.N1 + e] = w(e, p.N2);
+    for (int e = 0; e < p.N2; ++e) h[p.N1 + p.N2 + e] = w(e, N);
+    for (int j = 0; j < 512; ++j) h[p.N1 + 2 * p.N2 + j] = df(std::cos(two_pi * j / 512), std::sin(two_pi * j / 512));
+    cudaError_t e = cudaMalloc(&p.tw, sizeof(float4) * h.size());
     if (e != cudaSuccess) return cuda_check(ctx, e, "twiddle alloc");
-    e = cudaMemcpy(p.tw, h.data(), sizeof(float2) * h.size(), cudaMemcpyHostToDevice);
+    e = cudaMemcpy(p.tw, h.data(), sizeof(float4) * h.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         cudaFree(p.tw);
         return cuda_check(ctx, e, "twiddle upload");

@@ -11,41 +11,67 @@
 //   3. write (u, t), read (u = t + P*i, s)      (caller-chosen conflict-free layout)
 //   4. P-point DFT in registers over s.
 // Sign convention: forward = exp(-2 pi i nk/L), unnormalized (FFTW_FORWARD).
+//
+// Precision.  The split-step loop applies the same transforms thousands of
+// times, so a rounding error that depends only on a constant (a twiddle
+// factor) repeats identically every step and grows linearly with the step
+// count, while roundings that depend on the data decorrelate and grow like
+// sqrt(steps).  Every twiddle is therefore held as an unevaluated sum
+// hi + lo of two floats (about 48 significant bits) and applied with a
+// compensated product: the only roundings left are data-dependent.
 #pragma once
 
 #include "common.cuh"
 
 namespace fg {
 
-// cos(pi*j/32), j = 0..16
-__host__ __device__ __forceinline__ constexpr float cos_pi32(int j) {
-    constexpr float t[17] = {
-        1.0f,
-        0.99518472667219688624f,
-        0.98078528040323044913f,
-        0.95694033573220886494f,
-        0.92387953251128675613f,
-        0.88192126434835502971f,
-        0.83146961230254523708f,
-        0.77301045336273696081f,
-        0.7071067811865475244f,
-        0.63439328416364549822f,
-        0.55557023301960222474f,
-        0.47139673682599764856f,
-        0.38268343236508977173f,
-        0.29028467725446236764f,
-        0.19509032201612826785f,
-        0.098017140329560601994f,
-        0.0f};
+// (hi, lo) with hi + lo = cos(pi*j/32) to ~2^-48, j = 0..16
+__host__ __device__ __forceinline__ constexpr float2 cos_pi32_df(int j) {
+    constexpr float2 t[17] = {
+        {1.0f, 0.0f},
+        {0.9951847195625305f, 7.109666189109021e-09f},
+        {0.9807852506637573f, 2.9739473106360492e-08f},
+        {0.9569403529167175f, -1.7184508038781132e-08f},
+        {0.9238795042037964f, 2.830748968563057e-08f},
+        {0.8819212913513184f, -2.7002963420841297e-08f},
+        {0.8314695954322815f, 1.687026340846387e-08f},
+        {0.7730104327201843f, 2.0642552556182636e-08f},
+        {0.7071067690849304f, 1.2101617485882343e-08f},
+        {0.6343932747840881f, 9.37955757507325e-09f},
+        {0.5555702447891235f, -1.1769521357507529e-08f},
+        {0.4713967442512512f, -7.425253745196869e-09f},
+        {0.3826834261417389f, 6.2233507236442165e-09f},
+        {0.290284663438797f, 1.3815665056426951e-08f},
+        {0.19509032368659973f, -1.670471427850373e-09f},
+        {0.0980171412229538f, -8.933931927579408e-10f},
+        {0.0f, 0.0f}};
     return t[j];
 }
 
-// (cos, sin) of pi*idx/32 for idx in [0, 64)
-__host__ __device__ __forceinline__ constexpr float2 cs64(int idx) {
-    return idx <= 16   ? float2{cos_pi32(idx), cos_pi32(16 - idx)}
-           : idx <= 32 ? float2{-cos_pi32(32 - idx), cos_pi32(idx - 16)}
-           : idx <= 48 ? float2{-cos_pi32(idx - 32), -cos_pi32(48 - idx)}
-                       : float2{cos_pi32(64 - idx), -cos_pi32(idx - 48)};
+// (cos, sin) of pi*idx/32 for idx in [0, 64) as double-float: {c_hi, c_lo, s_hi, s_lo}
+__host__ __device__ __forceinline__ constexpr float4 cs64_df(int idx) {
+    return idx <= 16   ? float4{cos_pi32_df(idx).x, cos_pi32_df(idx).y, cos_pi32_df(16 - idx).x,
+                              cos_pi32_df(16 - idx).y}
+           : idx <= 32 ? float4{-cos_pi32_df(32 - idx).x, -cos_pi32_df(32 - idx).y, cos_pi32_df(idx - 16).x,
+                                cos_pi32_df(idx - 16).y}
+           : idx <= 48 ? float4{-cos_pi32_df(idx - 32).x, -cos_pi32_df(idx - 32).y, -cos_pi32_df(48 - idx).x,
+                                -cos_pi32_df(48 - idx).y}
+                       : float4{cos_pi32_df(64 - idx).x, cos_pi32_df(64 - idx).y, -cos_pi32_df(idx - 48).x,
+                                -cos_pi32_df(idx - 48).y};
+}
+
+// a * (w_hi + w_lo) with w = {re_hi, im_hi, re_lo, im_lo}: compensated complex
+// product; the representation error of w drops out, data roundings remain.
+__device__ __forceinline__ float2 cmul_df(float2 a, float4 w) {
+    const float re = fmaf(a.x, w.x, fmaf(-a.y, w.y, fmaf(a.x, w.z, -a.y * w.w)));
+    const float im = fmaf(a.x, w.y, fmaf(a.y, w.x, fmaf(a.x, w.w, a.y * w.z)));
+    return make_float2(re, im);
+}
+// a * conj(w_hi + w_lo)
+__device__ __forceinline__ float2 cmulc_df(float2 a, float4 w) {
+    const float re = fmaf(a.x, w.x, fmaf(a.y, w.y, fmaf(a.x, w.z, a.y * w.w)));
+    const float im = fmaf(a.y, w.x, fmaf(-a.x, w.y, fmaf(a.y, w.z, -a.x * w.w)));
+    return make_float2(re, im);
 }
 
 // a * exp(-+ i*pi*idx/32): forward uses the minus sign.
@@ -56,9 +82,9 @@ __device__ __forceinline__ float2 twmul64(float2 a, int idx) {
     if (idx == 32) return make_float2(-a.x, -a.y);
     if (idx == 16) return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
     if (idx == 48) return INV ? make_float2(a.y, -a.x) : make_float2(-a.y, a.x);
-    const float2 w = cs64(idx);
-    const float s = INV ? w.y : -w.y;
-    return make_float2(fmaf(a.x, w.x, -a.y * s), fmaf(a.x, s, a.y * w.x));
+    const float4 w = cs64_df(idx);  // (c_hi, c_lo, s_hi, s_lo)
+    // forward multiplies by (c - i s), inverse by (c + i s)
+    return INV ? cmul_df(a, make_float4(w.x, w.z, w.y, w.w)) : cmul_df(a, make_float4(w.x, -w.z, w.y, -w.w));
 }
 
 __host__ __device__ __forceinline__ constexpr int bitrev(int i, int bits) {
@@ -106,7 +132,6 @@ template <> struct PQ<128> { static constexpr int P = 8, Q = 16; };
 template <> struct PQ<256> { static constexpr int P = 16, Q = 16; };
 template <> struct PQ<512> { static constexpr int P = 16, Q = 32; };
 template <> struct PQ<1024> { static constexpr int P = 32, Q = 32; };
-template <> struct PQ<2048> { static constexpr int P = 32, Q = 64; };
 
 // Shared-memory layouts for the exchange (element (u, s), u < Q, s < P).
 // Row kernels: one group per row, padded rows of P+1 (conflict-free reads).
@@ -122,20 +147,17 @@ struct ColLayout {
     __device__ __forceinline__ int operator()(int u, int s) const { return (u * P + s) * C + c; }
 };
 
-// Group-wide sub-FFT (see file comment).  twL[e] = exp(-2 pi i e / L), e < L.
+// Group-wide sub-FFT (see file comment).  twL[e] = exp(-2 pi i e / L) as
+// double-float {re_hi, im_hi, re_lo, im_lo}, e < L.
 // BLOCK_SYNC selects __syncthreads (group spans warps) or __syncwarp.
 template <int P, int Q, bool INV, bool BLOCK_SYNC, class Lay>
 __device__ __forceinline__ void fft_pq(float2 (&v)[Q], float2* __restrict__ sm, const Lay lay, int t,
-                                       const float2* __restrict__ twL) {
+                                       const float4* __restrict__ twL) {
     static_assert(Q % P == 0, "Q must be a multiple of P");
     constexpr int M = Q / P;
     dft<Q, INV>(v);
 #pragma unroll
-    for (int u = 1; u < Q; ++u) {
-        float2 w = twL[t * u];
-        if (INV) w.y = -w.y;
-        v[u] = cmul(v[u], w);
-    }
+    for (int u = 1; u < Q; ++u) v[u] = INV ? cmulc_df(v[u], twL[t * u]) : cmul_df(v[u], twL[t * u]);
 #pragma unroll
     for (int u = 0; u < Q; ++u) sm[lay(u, t)] = v[u];
     if (BLOCK_SYNC) __syncthreads(); else __syncwarp();
@@ -150,6 +172,45 @@ __device__ __forceinline__ void fft_pq(float2 (&v)[Q], float2* __restrict__ sm, 
         for (int s = 0; s < P; ++s) v[i + M * s] = w[s];
     }
     if (BLOCK_SYNC) __syncthreads(); else __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
+// exp(2 pi i x) for a 64-bit fixed-point turn fraction x = X / 2^64, returned
+// as a double-float rotation {re_hi, im_hi, re_lo, im_lo} accurate to ~1e-12.
+// x = j/512 + r with |r| <= 1/1024: T[j] = exp(2 pi i j/512) from a
+// double-float table, exp(i theta) (theta = 2 pi r, |theta| <= pi/512) from
+// its Taylor series, combined with error-free products and sums
+// (Dekker / Knuth two-product and two-sum).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bv = s - a;
+    e = (a - (s - bv)) + (b - bv);
+}
+
+__device__ __forceinline__ float4 turns_rotation_df(unsigned long long X, const float4* __restrict__ T512) {
+    const unsigned long long jr = (X + (1ull << 54)) >> 55;      // nearest j/512
+    const int j = (int)(jr & 511ull);
+    const long long r = (long long)(X - (jr << 55));              // |r| <= 2^54
+    const float r_hi = __ll2float_rn(r);
+    const float r_lo = __ll2float_rn(r - __float2ll_rn(r_hi));
+    const float c_hi = 3.4061216748705226e-19f, c_lo = -9.478396428567739e-27f;  // 2 pi / 2^64
+    const float th = r_hi * c_hi;
+    const float tl = fmaf(r_hi, c_hi, -th) + fmaf(r_hi, c_lo, r_lo * c_hi);
+    const float th2 = th * th;
+    // sin(theta) = th + (tl - th^3/6),  cos(theta) - 1 = -th^2/2 - th*tl + th^4/24
+    const float s_hi = th;
+    const float s_lo = fmaf(-th2 * th, 1.0f / 6.0f, tl);
+    const float cm1 = fmaf(th2 * th2, 1.0f / 24.0f, fmaf(-0.5f, th2, -th * tl));
+    const float4 t = T512[j];  // {c_hi, s_hi, c_lo, s_lo}
+    // re = Tc (1 + cm1) - Ts s ;  im = Ts (1 + cm1) + Tc s
+    const float p = t.y * s_hi, pe = fmaf(t.y, s_hi, -p);
+    const float q = t.x * s_hi, qe = fmaf(t.x, s_hi, -q);
+    float re_hi, re_e, im_hi, im_e;
+    two_sum(t.x, -p, re_hi, re_e);
+    two_sum(t.y, q, im_hi, im_e);
+    const float re_lo = re_e + t.z + fmaf(t.x, cm1, -pe) - fmaf(t.y, s_lo, t.w * s_hi);
+    const float im_lo = im_e + t.w + fmaf(t.y, cm1, qe) + fmaf(t.x, s_lo, t.z * s_hi);
+    return make_float4(re_hi, im_hi, re_lo, im_lo);
 }
 
 }  // namespace fg

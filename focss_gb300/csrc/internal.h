@@ -19,8 +19,10 @@ struct SsfmState {
     double h;                      // signed size of the next nonlinear step
     double hl;                     // signed linear step of the next row pass
     double sum;                    // sum |A|^2 accumulator (LOGARITHMIC estimate)
-    unsigned long long disp_fix;   // beta2/2*hl*dw^2/(2pi) as a 64-bit turn fraction
-    float lin_gain;                // exp(-alpha*hl/2)/N for the next row pass
+    double gain_ratio;             // prod(exact gains) / prod(applied FP32 gains) (error feedback)
+    unsigned long long disp_hi;    // beta2/2*hl*dw^2/(2pi) turns per k'^2 as a 96-bit
+    unsigned long long disp_lo;    //   fraction: disp_hi * 2^-64 + disp_lo * 2^-96
+    float lin_gain;                // exp(-alpha*hl/2)/N for the next row pass (FP32, fed back)
     int action;                    // next column-pass operation (ColOp)
     int row_active;                // 1: data is spectral, next row pass applies hl
     int final_step;                // current nonlinear step is the last of the span
@@ -45,9 +47,11 @@ struct SsfmParams {
     int* n_done;
 };
 
+// Twiddle tables, double-float {re_hi, im_hi, re_lo, im_lo}, packed in one
+// device buffer: [W_N1^e, e<N1][W_N2^e, e<N2][W_N^e, e<N2][exp(2 pi i j/512), j<512].
 struct PassArgs {
     float2* data;           // batch x N complex64
-    const float2* tw;       // [W_N1^e, e<N1][W_N2^e, e<N2][W_N^e, e<N2]
+    const float4* tw;
     const float2* table;    // ROW_TABLE multiplier, transposed layout (k1*N2 + k2), length N
     SsfmState* state;       // null: plain transform driven by `op`
     SsfmParams prm;
@@ -59,7 +63,7 @@ struct PassArgs {
 
 struct Plan {
     int N = 0, N1 = 0, N2 = 0, log2N1 = 0, log2N2 = 0;
-    float2* tw = nullptr;   // device tables
+    float4* tw = nullptr;   // device tables (layout above)
 };
 
 struct Ctx {

@@ -26,12 +26,22 @@ __device__ __forceinline__ double log_step(const SsfmParams& p, int K, int i) {
     return inv_alpha * log(1 + inv_gain / (1 + inv_gain * i));
 }
 
-__device__ __forceinline__ unsigned long long turns_fix64(double a) {
+// a (turns, any sign) -> 96-bit two's-complement turn fraction hi*2^-64 + lo*2^-96.
+__device__ __forceinline__ void turns_fix96(double a, unsigned long long& hi, unsigned long long& lo) {
     const double ab = fabs(a);
-    const double fr = ab - floor(ab);
-    const double sc = ldexp(fr, 64);
-    unsigned long long A = sc >= 18446744073709551615.0 ? 0ull : (unsigned long long)sc;
-    return a < 0 ? (0ull - A) : A;
+    const double fr = ab - floor(ab);             // exact
+    const double s64 = ldexp(fr, 64);             // exact, < 2^64
+    const double h = floor(s64);
+    hi = __double2ull_rz(h);
+    lo = __double2ull_rz(ldexp(s64 - h, 32));     // < 2^32
+    if (a < 0) {
+        if (lo == 0) {
+            hi = 0ull - hi;
+        } else {
+            lo = (1ull << 32) - lo;
+            hi = ~hi;
+        }
+    }
 }
 
 __device__ __noinline__ static void ssfm_advance(SsfmState& s, const SsfmParams& p, int op_done, float peak,
@@ -47,6 +57,7 @@ __device__ __noinline__ static void ssfm_advance(SsfmState& s, const SsfmParams&
         s.distance = 0;
         s.index = 0;
         s.steps = 1;
+        s.gain_ratio = 1.0;
         if (p.grid == FOCSS_UNIFORM) {
             s.n_steps = p.total_steps;
             s.h = p.direction * (p.length / p.total_steps);
@@ -110,8 +121,13 @@ __device__ __noinline__ static void ssfm_advance(SsfmState& s, const SsfmParams&
     }
     s.hl = hl;
     const double a = 0.5 * p.beta2 * hl * p.dw * p.dw / (2.0 * 3.14159265358979323846);
-    s.disp_fix = turns_fix64(a);
-    s.lin_gain = (float)(exp(-0.5 * p.alpha * hl) / (double)p.samples);
+    turns_fix96(a, s.disp_hi, s.disp_lo);
+    // FP32 gain with error feedback: the running product of applied gains
+    // tracks the exact FP64 product to one rounding instead of drifting.
+    const double g = exp(-0.5 * p.alpha * hl) / (double)p.samples;
+    const float g32 = (float)(g * s.gain_ratio);
+    s.gain_ratio = s.gain_ratio * g / (double)g32;
+    s.lin_gain = g32;
     s.row_active = 1;
 }
 
@@ -119,10 +135,10 @@ __device__ __noinline__ static void ssfm_advance(SsfmState& s, const SsfmParams&
 template <int N1, int C>
 __global__ void __launch_bounds__(C* PQ<N1>::P, 2) col_kernel(const PassArgs a) {
     constexpr int P = PQ<N1>::P, Q = PQ<N1>::Q;
-    extern __shared__ float2 smem[];
-    float2* sx = smem;            // N1*C exchange
-    float2* s_tc = sx + N1 * C;   // W_N1^e
-    float2* s_tl = s_tc + N1;     // W_N^e, e < N2
+    extern __shared__ float4 smem4[];
+    float4* s_tc = smem4;                           // W_N1^e (double-float)
+    float4* s_tl = s_tc + N1;                       // W_N^e, e < N2
+    float2* sx = reinterpret_cast<float2*>(s_tl + a.N2);  // N1*C exchange
     __shared__ float red[64];
 
     const int b = blockIdx.y;
@@ -148,14 +164,16 @@ __global__ void __launch_bounds__(C* PQ<N1>::P, 2) col_kernel(const PassArgs a) 
     const int mask = N2 - 1, sh = a.log2N2;
     float pk = 0.0f, sm = 0.0f;
     if (op != COL_FWD) {
+        // inverse six-step twiddle W_N^{-n2 k1} = conj(W_N1^{e>>sh} W_N^{e&mask}), e = n2*k1
 #pragma unroll
         for (int j = 0; j < Q; ++j) {
             const int e = n2 * (t + P * j);
-            v[j] = cmulc(v[j], cmul(s_tc[e >> sh], s_tl[e & mask]));
+            v[j] = cmulc_df(cmulc_df(v[j], s_tc[e >> sh]), s_tl[e & mask]);
         }
         fft_pq<P, Q, true, true>(v, sx, lay, t, s_tc);
     }
     if (op == COL_KERR) {
+        // src/focss/solver/ssfm.cpp:160-164: A *= exp(i kappa gamma h |A|^2)
         const float coef = (float)(a.prm.kappa * a.prm.gamma * st->h);
 #pragma unroll
         for (int j = 0; j < Q; ++j) {
@@ -177,7 +195,7 @@ __global__ void __launch_bounds__(C* PQ<N1>::P, 2) col_kernel(const PassArgs a) 
 #pragma unroll
         for (int j = 0; j < Q; ++j) {
             const int e = n2 * (t + P * j);
-            v[j] = cmul(v[j], cmul(s_tc[e >> sh], s_tl[e & mask]));
+            v[j] = cmul_df(cmul_df(v[j], s_tc[e >> sh]), s_tl[e & mask]);
         }
     }
 #pragma unroll
@@ -210,20 +228,24 @@ __global__ void __launch_bounds__(C* PQ<N1>::P, 2) col_kernel(const PassArgs a) 
 template <int N2, int R>
 __global__ void __launch_bounds__(R* PQ<N2>::P, 2) row_kernel(const PassArgs a) {
     constexpr int P = PQ<N2>::P, Q = PQ<N2>::Q;
-    extern __shared__ float2 smem[];
-    float2* sx = smem;                     // R * Q * (P+1)
-    float2* s_tw = sx + R * Q * (P + 1);   // W_N2^e
+    extern __shared__ float4 smem4[];
+    float4* s_tw = smem4;                                    // W_N2^e (double-float)
+    float4* s_T = s_tw + N2;                                 // exp(2 pi i j/512)
+    float2* sx = reinterpret_cast<float2*>(s_T + 512);       // R * Q * (P+1)
 
     const int b = blockIdx.y;
     const SsfmState* st = a.state ? a.state + b : nullptr;
-    unsigned long long fix = 0ull;
+    unsigned long long dhi = 0ull, dlo = 0ull;
     float g = a.scale;
     if (st) {
         if (!*(volatile const int*)&st->row_active) return;
-        fix = st->disp_fix;
+        dhi = st->disp_hi;
+        dlo = st->disp_lo << 32;
         g = st->lin_gain;
     }
     for (int i = threadIdx.x; i < N2; i += blockDim.x) s_tw[i] = a.tw[a.N1 + i];
+    if (st)
+        for (int i = threadIdx.x; i < 512; i += blockDim.x) s_T[i] = a.tw[a.N1 + 2 * N2 + i];
     const int rl = threadIdx.x / P, t = threadIdx.x % P;
     const int k1 = blockIdx.x * R + rl;
     float2* base = a.data + (size_t)b * a.N + (size_t)k1 * N2 + t;
@@ -236,15 +258,16 @@ __global__ void __launch_bounds__(R* PQ<N2>::P, 2) row_kernel(const PassArgs a) 
     if (op != ROW_INV) fft_pq<P, Q, false, false>(v, sx, lay, t, s_tw);
     const int N = a.N, N1 = a.N1;
     if (op == ROW_SSFM) {
+        // exp(-alpha hl/2)/N * exp(i beta2/2 hl w_k^2) (ssfm.cpp:142-158), w_k = k' dw,
+        // phase in turns = a k'^2 mod 1 formed exactly from the 96-bit fraction.
 #pragma unroll
         for (int j = 0; j < Q; ++j) {
             const int k = k1 + N1 * (t + P * j);
-            const unsigned kp = (unsigned)(k <= (N >> 1) ? k : N - k);
-            const unsigned long long prod = fix * ((unsigned long long)kp * kp);
-            const float x = (float)(long long)prod * 1.0842021724855044e-19f;  // 2^-63
-            float s, cs;
-            sincospif(x, &s, &cs);
-            v[j] = cmul(v[j], make_float2(cs * g, s * g));
+            const unsigned long long kp = (unsigned long long)(k <= (N >> 1) ? k : N - k);
+            const unsigned long long kk = kp * kp;
+            const unsigned long long X = dhi * kk + __umul64hi(dlo, kk);
+            const float4 rot = turns_rotation_df(X, s_T);
+            v[j] = cmul_df(cscale(v[j], g), rot);
         }
     } else if (op == ROW_TABLE) {
         const float2* tb = a.table + (size_t)k1 * N2 + t;
@@ -264,7 +287,6 @@ __global__ void __launch_bounds__(R* PQ<N2>::P, 2) row_kernel(const PassArgs a) 
 #pragma unroll
     for (int j = 0; j < Q; ++j) base[P * j] = v[j];
 }
-
 
 typedef void (*PassFn)(PassArgs);
 struct Launch {
