@@ -1,0 +1,414 @@
+#!/usr/bin/env python
+"""Benchmark: SSFM sample-steps/s on the 5-channel WDM precision-study link.
+
+Workload (one bench step = one forward propagation of the whole batch):
+  5 x 32 GBaud 16QAM channels on a 50 GHz grid, 2^15 symbols per channel,
+  RRC roll-off 0.1, 16 samples/symbol of the total band -> N = 2^19 complex
+  samples per realization; 20 x 80 km SSMF (alpha 0.2 dB/km, D 17 ps/nm/km,
+  gamma 1.3 /W/km), ADAPTIVE split step (max nonlinear phase 0.005 rad/step,
+  max step 1 km), EDFA after every span (gain = span loss, NF 5 dB, seeded
+  ASE).  Batch = 7 launch powers (-2..+4 dBm per channel) x 8 ASE seeds = 56
+  realizations (235 MB of complex64, larger than the 129 MB L2).
+  One sample-step = one complex sample advanced by one split step.
+
+Arms:
+  default            hand-written sm_103a kernels through libfocss_gpu (C ABI)
+  --impl reference   the reference algorithm on the host cores: the FP64 C
+                     restatement of src/focss/solver/ssfm.cpp (oracle port), a
+                     bounded sample of the same workload per step.
+
+Prints one JSON line on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "SSFM Gsample-steps/s (FP32 GPU; FP64 reference on host cores)"
+UNIT = "Gsample-steps/s"
+W = dict(
+    workload="wdm5_16qam_32GBd_n2^19_20x80km_ssmf_adaptive_ase",
+    channels=5, symbols_per_channel=2 ** 15, samples_per_symbol=16, spacing_hz=50e9, baud=32e9,
+    roll_off=0.1, spans=20, span_m=80e3, alpha_db_per_km=0.2, dispersion_ps_nm_km=17.0, gamma_per_w_km=1.3,
+    max_phase_shift=0.005, max_step_m=1000.0, noise_figure_db=5.0,
+    powers_dbm=[-2, -1, 0, 1, 2, 3, 4], ase_seeds=8,
+)
+N = W["symbols_per_channel"] * W["samples_per_symbol"]
+DT = 1.0 / (W["baud"] * W["samples_per_symbol"])
+F0 = 299792458.0 / 1.55e-6
+
+
+def fiber_params():
+    alpha = W["alpha_db_per_km"] * 1e-3 * np.log(10) / 10
+    beta2 = -(1.55e-6 ** 2) * (W["dispersion_ps_nm_km"] * 1e-6) / (2 * np.pi * 299792458.0)
+    gamma = W["gamma_per_w_km"] * 1e-3
+    return alpha, beta2, gamma
+
+
+def gray16():
+    s = np.sqrt(10.0)
+    re = np.array([-3, -1, 3, 1, -3, -1, 3, 1, -3, -1, 3, 1, -3, -1, 3, 1]) / s
+    im = np.array([-3, -3, -3, -3, -1, -1, -1, -1, 3, 3, 3, 3, 1, 1, 1, 1]) / s
+    return re + 1j * im
+
+
+def rrc_taps(n_symbols, osf, beta):
+    """Full-length RRC pulse normalized to sum|h|^2 = length (src/focss/processing/modulation.cpp:47-74)."""
+    t = np.arange(n_symbols * osf) / osf - n_symbols / 2.0
+    h = np.empty_like(t)
+    z = t == 0
+    q = np.abs(np.abs(t) - 1 / (4 * beta)) < 1e-12
+    o = ~(z | q)
+    h[z] = 1 - beta + 4 * beta / np.pi
+    h[q] = beta / np.sqrt(2) * ((1 + 2 / np.pi) * np.sin(np.pi / (4 * beta)) + (1 - 2 / np.pi) * np.cos(np.pi / (4 * beta)))
+    to = t[o]
+    h[o] = (np.sin(np.pi * to * (1 - beta)) + 4 * beta * to * np.cos(np.pi * to * (1 + beta))) / (
+        np.pi * to * (1 - 16 * beta ** 2 * to ** 2))
+    return h * (h.size / np.sum(h ** 2))
+
+
+def synth_wdm(seed=1):
+    """Seeded synthetic 5-channel WDM field at 1 W per channel (scaled per power later)."""
+    osf, ns = W["samples_per_symbol"], W["symbols_per_channel"]
+    H = np.fft.fft(np.fft.ifftshift(rrc_taps(ns, osf, W["roll_off"]))) / N
+    t = np.arange(N) * DT
+    x = np.zeros(N, complex)
+    g = gray16()
+    for ch in range(W["channels"]):
+        rng = np.random.default_rng(seed + ch)
+        up = np.zeros(N, complex)
+        up[::osf] = g[rng.integers(0, 16, ns)]
+        sig = np.fft.ifft(np.fft.fft(up) * H) * N * osf  # rrc_shaping (modulation.cpp:86-90) normalization
+        x += sig * np.exp(2j * np.pi * (ch - W["channels"] // 2) * W["spacing_hz"] * t)
+    return x
+
+
+def batch_inputs():
+    base = synth_wdm()
+    out = np.empty((len(W["powers_dbm"]) * W["ase_seeds"], 1, N), np.complex64)
+    i = 0
+    for p in W["powers_dbm"]:
+        s = np.sqrt(1e-3 * 10 ** (p / 10.0))
+        for _ in range(W["ase_seeds"]):
+            out[i, 0] = base * s
+            i += 1
+    return out
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        os.unlink(self.path)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for k, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(k)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU reference / baseline
+def cpu_sample(threads, n_steps):
+    """FP64 reference split steps (oracle port of ssfm.cpp) on the host cores:
+    `threads` realizations of the workload's field, n_steps uniform 1 km steps each."""
+    from oracle import build as obuild
+    from oracle import cpu
+    obuild.build_oracle()
+    alpha, beta2, gamma = fiber_params()
+    x = synth_wdm()[None, None, :] * np.sqrt(1e-3)
+    a = np.ascontiguousarray(np.repeat(x, threads, axis=0))
+    fib = cpu.Fiber(alpha, beta2, gamma, W["span_m"], 1.55e-6, 1.0)
+    t0 = time.perf_counter()
+    cpu.uniform_steps_batch(a, DT, fib, 1000.0, n_steps, threads)
+    dt = time.perf_counter() - t0
+    return threads * n_steps * N / dt / 1e9, dt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    n_steps = 12
+    for _ in range(args.warmup):
+        cpu_sample(threads, n_steps)
+    vals, times = [], []
+    for _ in range(args.steps):
+        v, t = cpu_sample(threads, n_steps)
+        vals.append(v)
+        times.append(t)
+    value = float(np.median(vals))
+    sample = "%d realizations x %d uniform 1 km split steps of the N=2^19 WDM field, FP64, %d threads" % (
+        threads, n_steps, threads)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.median(times)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": dict(W, note="reference arm: oracle port (reference sources need FFTW, absent on the GPU host)"),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_ours(args):
+    import focss_gb300 as fg
+    if not os.path.exists(fg.LIB_PATH):
+        from focss_gb300 import build as gbuild
+        gbuild.build()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    import torch
+
+    ctx = fg.Context(local)
+    alpha, beta2, gamma = fiber_params()
+    fib = fg.Fiber(alpha, beta2, gamma, W["span_m"])
+    G = 10 ** (W["alpha_db_per_km"] * W["span_m"] / 1e3 / 10)
+    NF = 10 ** (W["noise_figure_db"] / 10)
+    ssfm = fg.SSFM(fib)
+    ssfm.set_grid(fg.SSFM.ADAPTIVE)
+    ssfm.set_maximum_phase_shift(W["max_phase_shift"])
+    ssfm.set_maximum_step_size(W["max_step_m"])
+
+    host = batch_inputs()
+    B = host.shape[0]
+    dom = fg.Domain(1, N, DT, F0)
+    pristine = fg.Field(dom, data=host, batch=B, ctx=ctx)
+    field = fg.Field(dom, batch=B, ctx=ctx)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+
+    def propagate(f, seed):
+        steps = 0
+        amp = fg.Amplifier(G, NF, seed=seed)
+        for s in range(W["spans"]):
+            steps += int(ssfm.run(f, fg.SSFM.FORWARD).sum())
+            amp.amplify(f, counter=s)
+        return steps
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    for w in range(args.warmup):
+        field.assign(pristine)
+        propagate(field, 1000 + w)
+    ctx.sync()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize(local)
+    ctx.sync()
+    launches0 = fg.launch_count()
+    total_ms, total_steps = 0.0, 0
+    for k in range(args.steps):
+        field.assign(pristine)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        total_steps += propagate(field, 2000 + k)
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+    ctx.sync()
+    torch.cuda.synchronize(local)
+    barrier()
+    launches = fg.launch_count() - launches0  # field restores are copies, not kernels
+    clk = clocks.stop()
+    sample_steps = total_steps * N
+
+    t_max = total_ms
+    total_samples = sample_steps
+    if dist is not None:
+        tt = torch.tensor([total_ms, float(sample_steps)], dtype=torch.float64, device="cuda")
+        mx = tt.clone()
+        dist.all_reduce(mx[:1], op=dist.ReduceOp.MAX)
+        dist.all_reduce(tt[1:], op=dist.ReduceOp.SUM)
+        t_max = float(mx[0])
+        total_samples = float(tt[1])
+    value = total_samples / (t_max / 1e3) / 1e9
+
+    # ---- roofline probe: the split-step passes alone on the full batch
+    # (UNIFORM grid: every pass processes all B realizations).
+    probe = fg.SSFM(fib, 40)
+    field.assign(pristine)
+    probe.run(field)
+    ctx.profile_read(reset=True)
+    ctx.profile_enable(True)
+    field.assign(pristine)
+    probe.run(field)
+    prof = ctx.profile_read(reset=True)
+    ctx.profile_enable(False)
+    K = 40
+    bytes_per_pass = 16.0 * B * N  # one read + one write of complex64 per sample
+    col_bytes = bytes_per_pass * prof["col_launches"]           # FWD, K x KERR, INV: all full
+    row_bytes = bytes_per_pass * (prof["row_launches"] - 1)     # trailing pass is a no-op
+    col_gbs = col_bytes / (prof["col_ms"] / 1e3) / 1e9
+    row_gbs = row_bytes / (prof["row_ms"] / 1e3) / 1e9
+    dom_kernel = "col_kernel" if prof["col_ms"] >= prof["row_ms"] else "row_kernel"
+    achieved = col_gbs if dom_kernel == "col_kernel" else row_gbs
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+    except Exception:
+        peak, peak_src = 6800.0, "fallback"
+    roofline = {
+        "bound": "hbm", "kernel": dom_kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": achieved / peak, "peak_source": peak_src, "traffic": None,
+        "algorithmic_bytes_per_launch": bytes_per_pass,
+        "per_kernel_gbs": {"col_kernel": col_gbs, "row_kernel": row_gbs},
+        "per_kernel_avg_ms": {"col_kernel": prof["col_ms"] / max(1, prof["col_launches"]),
+                              "row_kernel": prof["row_ms"] / max(1, prof["row_launches"] - 1)},
+        "probe": "UNIFORM %d steps over the full batch, CUDA events around each pass" % K,
+    }
+    traffic_file = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(traffic_file):
+        try:
+            tr = json.load(open(traffic_file))
+            roofline["traffic"] = tr.get(dom_kernel)
+        except Exception:
+            pass
+
+    # ---- end to end through the public API with host buffers (pinned)
+    pin_in = torch.from_numpy(host.view(np.float32)).pin_memory()
+    pin_out = torch.empty_like(pin_in).pin_memory()
+    hin = pin_in.numpy().view(np.complex64)
+    hout = pin_out.numpy().view(np.complex64)
+    import ctypes as C
+    from focss_gb300._lib import check, lib
+    e2e_steps, t_e2e = 0, 0.0
+    for k in range(max(1, args.steps)):
+        ctx.sync()
+        t0 = time.perf_counter()
+        check(lib().focss_field_upload_c64(field.h, hin.ctypes.data_as(C.c_void_p), hin.size), ctx.h)
+        e2e_steps += propagate(field, 3000 + k)
+        check(lib().focss_field_download_c64(field.h, hout.ctypes.data_as(C.c_void_p), hout.size), ctx.h)
+        t_e2e += time.perf_counter() - t0
+    e2e_val = e2e_steps * N / t_e2e / 1e9
+    if dist is not None:
+        tt = torch.tensor([t_e2e, float(e2e_steps * N)], dtype=torch.float64, device="cuda")
+        mx = tt.clone()
+        dist.all_reduce(mx[:1], op=dist.ReduceOp.MAX)
+        dist.all_reduce(tt[1:], op=dist.ReduceOp.SUM)
+        e2e_val = float(tt[1]) / float(mx[0]) / 1e9
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / max(1, args.steps), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": dict(W, batch=B, samples=N, l2="batch of 235 MB complex64 exceeds the 129 MB L2",
+                       parallelism="replicas" if world > 1 else "single GPU",
+                       sample_steps_per_step=sample_steps / max(1, args.steps)),
+        "roofline": roofline,
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(hin.nbytes),
+                "d2h_bytes_per_step": int(hout.nbytes)},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    if world == 1 and rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, t = cpu_sample(threads, 12)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": "%d realizations x 12 uniform 1 km split steps of the N=2^19 WDM "
+                                          "field, FP64 oracle port of ssfm.cpp, %.1f s" % (threads, t)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def run_ncu_case(args):
+    """Small case for ncu captures: UNIFORM split steps on 40 realizations of
+    the N=2^19 WDM field (168 MB, above the L2 size), 4 steps."""
+    import focss_gb300 as fg
+    ctx = fg.Context(0)
+    alpha, beta2, gamma = fiber_params()
+    fib = fg.Fiber(alpha, beta2, gamma, W["span_m"])
+    x = (synth_wdm() * np.sqrt(1e-3)).astype(np.complex64)
+    B = args.ncu_batch
+    f = fg.Field(fg.Domain(1, N, DT, F0), data=np.broadcast_to(x, (B, 1, N)), batch=B, ctx=ctx)
+    fg.SSFM(fib, 4).run(f)
+    ctx.sync()
+    print("ncu case done: %d x N=%d, 4 uniform steps" % (B, N))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ncu-case", action="store_true", help="small fixed case for ncu captures")
+    ap.add_argument("--ncu-batch", type=int, default=40)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.ncu_case:
+        return run_ncu_case(args)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

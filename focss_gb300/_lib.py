@@ -66,6 +66,9 @@ SIGNATURES = {
     "focss_forward_propagation": (I, [P, P, C.POINTER(CFiber), C.POINTER(CSsfmOpts), D, D, U64, U64, I]),
     "focss_backward_propagation": (I, [P, P, C.POINTER(CFiber), C.POINTER(CSsfmOpts), D, I]),
     "focss_cd_compensation": (I, [P, P, C.POINTER(CFiber), I]),
+    "focss_profile_enable": (I, [P, I]),
+    "focss_profile_read": (I, [P, P, P, P, P, I]),
+    "focss_launch_count": (C.c_longlong, []),
 }
 
 _lib = None

@@ -22,6 +22,11 @@ PLANCK = 6.62607004081818181818181e-34
 LIGHT_SPEED = 299792458.0
 
 
+def launch_count() -> int:
+    """Kernel launches issued by libfocss_gpu in this process."""
+    return int(lib().focss_launch_count())
+
+
 # ---- unit conversions (src/focss/functions.cpp:82-96): plain host arithmetic
 def db_to_linear(db):
     return 10.0 ** (db / 10.0)
@@ -62,6 +67,16 @@ class Context:
     @property
     def stream(self):
         return lib().focss_ctx_stream(self.h)
+
+    def profile_enable(self, on=True):
+        check(lib().focss_profile_enable(self.h, 1 if on else 0), self.h)
+
+    def profile_read(self, reset=True):
+        cm, rm = C.c_double(), C.c_double()
+        cl, rl = C.c_longlong(), C.c_longlong()
+        check(lib().focss_profile_read(self.h, C.byref(cm), C.byref(cl), C.byref(rm), C.byref(rl),
+                                       1 if reset else 0), self.h)
+        return {"col_ms": cm.value, "col_launches": cl.value, "row_ms": rm.value, "row_launches": rl.value}
 
     def close(self):
         if self.h and alive():

@@ -114,6 +114,9 @@ void* scratch_buffer(Ctx* ctx, int slot, size_t bytes) {
     return ctx->scratch[slot];
 }
 
+static long long g_launches = 0;
+void count_launch(long long n) { __atomic_fetch_add(&g_launches, n, __ATOMIC_RELAXED); }
+
 }  // namespace fg
 
 namespace {
@@ -172,6 +175,7 @@ FOCSS_API focss_status focss_ctx_destroy(focss_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (auto& kv : c->plans) cudaFree(kv.second.tw);
     for (void* p : c->scratch) cudaFree(p);
+    for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
     cudaFree(c->d_state);
     cudaFree(c->d_counters);
     cudaFree(c->d_red);
@@ -392,5 +396,27 @@ FOCSS_API focss_status focss_cd_compensation(focss_ctx* c, focss_field* f, const
     focss_ssfm_opts o{FOCSS_UNIFORM, 1, 0.0, 0.0};
     return focss_ssfm_run(c, f, &d, &o, FOCSS_BACKWARD, nullptr);
 }
+
+FOCSS_API focss_status focss_profile_enable(focss_ctx* c, int enable) {
+    if (!c) return FOCSS_ERR_INVALID_ARG;
+    c->profiling = enable != 0;
+    return FOCSS_OK;
+}
+
+FOCSS_API focss_status focss_profile_read(focss_ctx* c, double* col_ms, long long* col_launches, double* row_ms,
+                                          long long* row_launches, int reset) {
+    if (!c) return FOCSS_ERR_INVALID_ARG;
+    if (col_ms) *col_ms = c->prof_ms[0];
+    if (row_ms) *row_ms = c->prof_ms[1];
+    if (col_launches) *col_launches = c->prof_launches[0];
+    if (row_launches) *row_launches = c->prof_launches[1];
+    if (reset) {
+        c->prof_ms[0] = c->prof_ms[1] = 0;
+        c->prof_launches[0] = c->prof_launches[1] = 0;
+    }
+    return FOCSS_OK;
+}
+
+FOCSS_API long long focss_launch_count(void) { return __atomic_load_n(&fg::g_launches, __ATOMIC_RELAXED); }
 
 }  // extern "C"

@@ -20,6 +20,7 @@ __global__ void scale_kernel(float2* __restrict__ d, size_t n, float2 s) {
 
 cudaError_t launch_scale(float2* d, size_t n, float2 s, cudaStream_t st) {
     scale_kernel<<<grid_for(n, 256), 256, 0, st>>>(d, n, s);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -51,6 +52,7 @@ cudaError_t launch_amplifier(float2* d, int modes, int samples, int batch, float
     amplifier_kernel<<<grid_for(n, 256), 256, 0, st>>>(d, modes, samples, n, scale, sigma,
                                                         make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)),
                                                         (uint32_t)counter, (uint32_t)(counter >> 32));
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -87,6 +89,7 @@ cudaError_t launch_power(const float2* d, int modes, int samples, int batch, dou
     int gx = (samples + 1023) / 1024;
     if (gx > 64) gx = 64;
     power_kernel<<<dim3(gx, batch), 256, 0, st>>>(d, modes, samples, avg, peak_bits);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -113,6 +116,7 @@ cudaError_t launch_transpose_to_natural(const float2* src, float2* dst, int N1, 
     // src is N1 rows x N2 cols; natural index k1 + N1*k2 = dst row k2, col k1.
     dim3 grid((N2 + 31) / 32, (N1 + 31) / 32, batch);
     transpose_kernel<<<grid, dim3(32, 8), 0, st>>>(src, dst, N1, N2);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -120,6 +124,7 @@ cudaError_t launch_transpose_from_natural(const float2* src, float2* dst, int N1
                                           cudaStream_t st) {
     dim3 grid((N1 + 31) / 32, (N2 + 31) / 32, batch);
     transpose_kernel<<<grid, dim3(32, 8), 0, st>>>(src, dst, N2, N1);
+    count_launch();
     return cudaGetLastError();
 }
 

@@ -79,7 +79,15 @@ struct Ctx {
     size_t red_cap = 0;
     std::vector<void*> scratch;      // generic device scratch buffers
     std::vector<size_t> scratch_cap;
+    // instrumentation (focss_profile_*)
+    bool profiling = false;
+    std::vector<cudaEvent_t> prof_events;
+    double prof_ms[2] = {0, 0};          // column, row
+    long long prof_launches[2] = {0, 0};
 };
+
+// Process-wide launch counter (focss_launch_count).
+void count_launch(long long n = 1);
 
 struct Field {
     Ctx* ctx = nullptr;

@@ -101,6 +101,7 @@ cudaError_t launch_col(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
     a.tw = p.tw;
     dim3 grid(p.N2 / l.per_block, batch);
     l.fn<<<grid, l.threads, smem, s>>>(a);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -128,10 +129,39 @@ cudaError_t launch_row(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
     if (p.N1 % R != 0) return cudaErrorInvalidValue;
     dim3 grid(p.N1 / R, batch);
     l.fn<<<grid, l.threads, smem, s>>>(a);
+    count_launch();
     return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------- SSFM driver
+namespace {
+// Event triples (before column pass, between, after row pass) for the
+// instrumentation mode; consumed by prof_collect after the run synchronizes.
+size_t prof_used = 0;
+cudaEvent_t* prof_events(Ctx* ctx, int n) {
+    while (ctx->prof_events.size() < prof_used + n) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        ctx->prof_events.push_back(e);
+    }
+    cudaEvent_t* r = ctx->prof_events.data() + prof_used;
+    prof_used += n;
+    return r;
+}
+void prof_collect(Ctx* ctx) {
+    for (size_t i = 0; i + 2 < prof_used; i += 3) {
+        float a = 0, b = 0;
+        cudaEventElapsedTime(&a, ctx->prof_events[i], ctx->prof_events[i + 1]);
+        cudaEventElapsedTime(&b, ctx->prof_events[i + 1], ctx->prof_events[i + 2]);
+        ctx->prof_ms[0] += a;
+        ctx->prof_ms[1] += b;
+        ctx->prof_launches[0] += 1;
+        ctx->prof_launches[1] += 1;
+    }
+    prof_used = 0;
+}
+}  // namespace
+
 focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ssfm_opts& o, double dir,
                       int* steps_out) {
     if (f->modes != 1)
@@ -193,8 +223,19 @@ focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ss
     while (!done) {
         const long long n = (o.grid == FOCSS_UNIFORM) ? cap : chunk;
         for (long long i = 0; i < n; ++i) {
-            cudaError_t e = launch_col(*p, a, f->batch, s);
-            if (e == cudaSuccess) e = launch_row(*p, a, f->batch, s);
+            cudaError_t e = cudaSuccess;
+            if (ctx->profiling) {
+                cudaEvent_t* pe = prof_events(ctx, 3);
+                if (!pe) e = cudaErrorMemoryAllocation;
+                if (e == cudaSuccess) e = cudaEventRecord(pe[0], s);
+                if (e == cudaSuccess) e = launch_col(*p, a, f->batch, s);
+                if (e == cudaSuccess) e = cudaEventRecord(pe[1], s);
+                if (e == cudaSuccess) e = launch_row(*p, a, f->batch, s);
+                if (e == cudaSuccess) e = cudaEventRecord(pe[2], s);
+            } else {
+                e = launch_col(*p, a, f->batch, s);
+                if (e == cudaSuccess) e = launch_row(*p, a, f->batch, s);
+            }
             if (e != cudaSuccess) {
                 if (ev) cudaEventDestroy(ev);
                 return cuda_check(ctx, e, "ssfm pass launch");
@@ -230,6 +271,7 @@ focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ss
     if (st != FOCSS_OK) return st;
     st = cuda_check(ctx, cudaStreamSynchronize(s), "ssfm sync");
     if (st != FOCSS_OK) return st;
+    if (ctx->profiling) prof_collect(ctx);
     for (int b = 0; b < f->batch; ++b) {
         if (hs[b].action != COL_IDLE)
             return set_error(ctx, FOCSS_ERR_TIMEOUT, "ssfm_run: a realization did not finish");

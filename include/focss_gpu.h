@@ -167,6 +167,18 @@ FOCSS_API focss_status focss_backward_propagation(focss_ctx* ctx, focss_field* f
 FOCSS_API focss_status focss_cd_compensation(focss_ctx* ctx, focss_field* field,
                                              const focss_fiber* fiber, int spans);
 
+/* ------------------------------------------------------- instrumentation */
+/* No reference counterpart (the reference only prints progress to std::cout,
+ * src/focss/solver/ssfm.cpp:117).
+ * When enabled, each split-step column/row pass launch is bracketed by CUDA
+ * events on the context stream; focss_profile_read returns the accumulated
+ * device time and launch counts per pass kind (and resets them if asked). */
+FOCSS_API focss_status focss_profile_enable(focss_ctx* ctx, int enable);
+FOCSS_API focss_status focss_profile_read(focss_ctx* ctx, double* col_ms, long long* col_launches,
+                                          double* row_ms, long long* row_launches, int reset);
+/* Total kernel launches issued by this library in this process. */
+FOCSS_API long long focss_launch_count(void);
+
 #ifdef __cplusplus
 }
 #endif
