@@ -90,7 +90,8 @@ def synth_wdm(seed=1):
         rng = np.random.default_rng(seed + ch)
         up = np.zeros(N, complex)
         up[::osf] = g[rng.integers(0, 16, ns)]
-        sig = np.fft.ifft(np.fft.fft(up) * H) * N * osf  # rrc_shaping (modulation.cpp:86-90) normalization
+        # rrc_shaping (modulation.cpp:86-90): IFFT(FFT(x)/N * FFT(h)/N) unnormalized, times osf
+        sig = np.fft.ifft(np.fft.fft(up) * H) * osf
         x += sig * np.exp(2j * np.pi * (ch - W["channels"] // 2) * W["spacing_hz"] * t)
     return x
 
