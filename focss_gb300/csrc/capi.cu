@@ -5,6 +5,7 @@
 #include <string>
 #include <vector>
 
+#include "fft.cuh"
 #include "internal.h"
 
 using fg::Ctx;
@@ -46,9 +47,9 @@ focss_status get_plan(Ctx* ctx, int N, const Plan** out) {
     p.log2N2 = lg - lg / 2;
     p.N1 = 1 << p.log2N1;
     p.N2 = 1 << p.log2N2;
-    // Twiddle tables from FP64 as double-float pairs {re_hi, im_hi, re_lo, im_lo}:
-    // [W_N1^e][W_N2^e][W_N^e (e < N2)][exp(+2 pi i j / 512)].
-    std::vector<float4> h(p.N1 + 2 * (size_t)p.N2 + 512);
+    // Twiddle tables from FP64 as double-float pairs {re_hi, im_hi, re_lo, im_lo}
+    // (layout documented in internal.h).
+    std::vector<float4> h(2 * (size_t)p.N1 + 2 * (size_t)p.N2 + 512);
     const double two_pi = 2.0 * 3.14159265358979323846;
     auto df = [](double re, double im) {
         const float rh = (float)re, ih = (float)im;
@@ -56,10 +57,19 @@ focss_status get_plan(Ctx* ctx, int N, const Plan** out) {
     };
     // cos/sin of 2 pi e / L evaluated on an exactly reduced argument (e mod L).
     auto w = [&](long long e, long long L) { return df(std::cos(two_pi * e / L), -std::sin(two_pi * e / L)); };
-    for (int e = 0; e < p.N1; ++e) h[e] = w(e, p.N1);
-    for (int e = 0; e < p.N2; ++e) h[p.N1 + e] = w(e, p.N2);
-    for (int e = 0; e < p.N2; ++e) h[p.N1 + p.N2 + e] = w(e, N);
-    for (int j = 0; j < 512; ++j) h[p.N1 + 2 * p.N2 + j] = df(std::cos(two_pi * j / 512), std::sin(two_pi * j / 512));
+    // Threads per group of a length-L sub-FFT (must match PQ<L>::P in fft.cuh).
+    auto groupP = [](int L) { return L <= 32 ? 4 : L <= 128 ? 8 : L <= 512 ? 16 : 32; };
+    auto fill_pq = [&](float4* dst, int L) {
+        const int P = groupP(L), Q = L / P;
+        for (int u = 0; u < Q; ++u)
+            for (int t = 0; t < P; ++t) dst[u * P + t] = w((long long)t * u % L, L);
+    };
+    fill_pq(h.data(), p.N1);
+    fill_pq(h.data() + p.N1, p.N2);
+    for (int e = 0; e < p.N1; ++e) h[p.N1 + p.N2 + e] = w(e, p.N1);
+    for (int e = 0; e < p.N2; ++e) h[2 * p.N1 + p.N2 + swz8(e)] = w(e, N);
+    for (int j = 0; j < 512; ++j)
+        h[2 * p.N1 + 2 * p.N2 + j] = df(std::cos(two_pi * j / 512), std::sin(two_pi * j / 512));
     cudaError_t e = cudaMalloc(&p.tw, sizeof(float4) * h.size());
     if (e != cudaSuccess) return cuda_check(ctx, e, "twiddle alloc");
     e = cudaMemcpy(p.tw, h.data(), sizeof(float4) * h.size(), cudaMemcpyHostToDevice);

@@ -147,17 +147,23 @@ struct ColLayout {
     __device__ __forceinline__ int operator()(int u, int s) const { return (u * P + s) * C + c; }
 };
 
-// Group-wide sub-FFT (see file comment).  twL[e] = exp(-2 pi i e / L) as
-// double-float {re_hi, im_hi, re_lo, im_lo}, e < L.
+// XOR swizzle of a table index inside groups of 8 entries (16-byte entries:
+// 8 per 128-byte shared-memory wavefront), so strided reads spread over banks.
+__host__ __device__ __forceinline__ int swz8(int e) { return e ^ (((e >> 3) ^ (e >> 6)) & 7); }
+
+// Group-wide sub-FFT (see file comment).  twPQ[u*P + t] = exp(-2 pi i t u / L)
+// as double-float {re_hi, im_hi, re_lo, im_lo}: the P threads of a group read
+// P consecutive entries (conflict-free).
 // BLOCK_SYNC selects __syncthreads (group spans warps) or __syncwarp.
 template <int P, int Q, bool INV, bool BLOCK_SYNC, class Lay>
 __device__ __forceinline__ void fft_pq(float2 (&v)[Q], float2* __restrict__ sm, const Lay lay, int t,
-                                       const float4* __restrict__ twL) {
+                                       const float4* __restrict__ twPQ) {
     static_assert(Q % P == 0, "Q must be a multiple of P");
     constexpr int M = Q / P;
     dft<Q, INV>(v);
 #pragma unroll
-    for (int u = 1; u < Q; ++u) v[u] = INV ? cmulc_df(v[u], twL[t * u]) : cmul_df(v[u], twL[t * u]);
+    for (int u = 1; u < Q; ++u)
+        v[u] = INV ? cmulc_df(v[u], twPQ[u * P + t]) : cmul_df(v[u], twPQ[u * P + t]);
 #pragma unroll
     for (int u = 0; u < Q; ++u) sm[lay(u, t)] = v[u];
     if (BLOCK_SYNC) __syncthreads(); else __syncwarp();
@@ -187,15 +193,25 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     e = (a - (s - bv)) + (b - bv);
 }
 
+// Exact float of a 23-bit unsigned integer (exponent trick, no conversion unit).
+__device__ __forceinline__ float u23_to_float(unsigned u) { return __int_as_float(0x4B000000u | u) - 8388608.0f; }
+
 __device__ __forceinline__ float4 turns_rotation_df(unsigned long long X, const float4* __restrict__ T512) {
-    const unsigned long long jr = (X + (1ull << 54)) >> 55;      // nearest j/512
-    const int j = (int)(jr & 511ull);
-    const long long r = (long long)(X - (jr << 55));              // |r| <= 2^54
-    const float r_hi = __ll2float_rn(r);
-    const float r_lo = __ll2float_rn(r - __float2ll_rn(r_hi));
-    const float c_hi = 3.4061216748705226e-19f, c_lo = -9.478396428567739e-27f;  // 2 pi / 2^64
-    const float th = r_hi * c_hi;
-    const float tl = fmaf(r_hi, c_hi, -th) + fmaf(r_hi, c_lo, r_lo * c_hi);
+    // Y = X + 2^54: j = Y >> 55 is the nearest multiple of 1/512 turn, and the
+    // remainder r = X - j 2^55 in [-2^54, 2^54) is (Y mod 2^55) - 2^54.
+    const unsigned long long Y = X + (1ull << 54);
+    const unsigned yh = (unsigned)(Y >> 32);
+    const int j = (int)((yh >> 23) & 511u);
+    // r + 2^54 = A 2^32 + B 2^9 + (9 dropped bits, < 2e-16 rad), A, B < 2^23.
+    const unsigned A = yh & 0x7FFFFFu;
+    const unsigned B = (unsigned)(Y >> 9) & 0x7FFFFFu;
+    const float fA = u23_to_float(A) - 4194304.0f;  // exact, in [-2^22, 2^22)
+    const float fB = u23_to_float(B);
+    // theta = 2 pi r / 2^64 = fA * 2pi/2^32 + fB * 2pi/2^55, as th + tl
+    const float c32_hi = 1.462918119976564e-09f, c32_lo = -4.070940267922164e-17f;
+    const float c9 = 1.7439342975337076e-16f;
+    const float th = fA * c32_hi;
+    const float tl = fmaf(fA, c32_hi, -th) + fmaf(fA, c32_lo, fB * c9);
     const float th2 = th * th;
     // sin(theta) = th + (tl - th^3/6),  cos(theta) - 1 = -th^2/2 - th*tl + th^4/24
     const float s_hi = th;

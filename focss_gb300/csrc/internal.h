@@ -48,7 +48,12 @@ struct SsfmParams {
 };
 
 // Twiddle tables, double-float {re_hi, im_hi, re_lo, im_lo}, packed in one
-// device buffer: [W_N1^e, e<N1][W_N2^e, e<N2][W_N^e, e<N2][exp(2 pi i j/512), j<512].
+// device buffer (offsets in entries):
+//   0            column sub-FFT table, entry u*P+t = W_N1^{t u}   (N1 entries)
+//   N1           row sub-FFT table,    entry u*P+t = W_N2^{t u}   (N2 entries)
+//   N1+N2        six-step high factor  W_N1^h, h < N1             (N1 entries)
+//   2N1+N2       six-step low factor   W_N^l at swz8(l), l < N2   (N2 entries)
+//   2N1+2N2      exp(+2 pi i j/512), j < 512                      (512 entries)
 struct PassArgs {
     float2* data;           // batch x N complex64
     const float4* tw;

@@ -86,7 +86,7 @@ cudaError_t launch_col(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
     Launch& l = cache[p.log2N1];
     if (!l.fn) l = col_launch_for(p.log2N1);
     if (!l.fn) return cudaErrorInvalidValue;
-    const size_t smem = sizeof(float4) * ((size_t)p.N1 + p.N2) + sizeof(float2) * (size_t)p.N1 * l.per_block;
+    const size_t smem = sizeof(float4) * (2 * (size_t)p.N1 + p.N2) + sizeof(float2) * (size_t)p.N1 * l.per_block;
     if (!l.attr_set || smem > l.smem) {
         cudaError_t e = cudaFuncSetAttribute((const void*)l.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);

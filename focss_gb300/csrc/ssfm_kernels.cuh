@@ -136,9 +136,10 @@ template <int N1, int C>
 __global__ void __launch_bounds__(C* PQ<N1>::P, 2) col_kernel(const PassArgs a) {
     constexpr int P = PQ<N1>::P, Q = PQ<N1>::Q;
     extern __shared__ float4 smem4[];
-    float4* s_tc = smem4;                           // W_N1^e (double-float)
-    float4* s_tl = s_tc + N1;                       // W_N^e, e < N2
-    float2* sx = reinterpret_cast<float2*>(s_tl + a.N2);  // N1*C exchange
+    float4* s_fc = smem4;                           // column sub-FFT twiddles, (u,t) order
+    float4* s_hi = s_fc + N1;                       // six-step W_N1^h
+    float4* s_lo = s_hi + N1;                       // six-step W_N^l, swizzled
+    float2* sx = reinterpret_cast<float2*>(s_lo + a.N2);  // N1*C exchange
     __shared__ float red[64];
 
     const int b = blockIdx.y;
@@ -149,8 +150,11 @@ __global__ void __launch_bounds__(C* PQ<N1>::P, 2) col_kernel(const PassArgs a) 
         if (op == COL_IDLE) return;
     }
     const int N2 = a.N2;
-    for (int i = threadIdx.x; i < N1; i += blockDim.x) s_tc[i] = a.tw[i];
-    for (int i = threadIdx.x; i < N2; i += blockDim.x) s_tl[i] = a.tw[N1 + N2 + i];
+    for (int i = threadIdx.x; i < N1; i += blockDim.x) {
+        s_fc[i] = a.tw[i];
+        s_hi[i] = a.tw[N1 + N2 + i];
+    }
+    for (int i = threadIdx.x; i < N2; i += blockDim.x) s_lo[i] = a.tw[2 * N1 + N2 + i];
 
     const int c = threadIdx.x % C, t = threadIdx.x / C;
     const int n2 = blockIdx.x * C + c;
@@ -168,9 +172,9 @@ __global__ void __launch_bounds__(C* PQ<N1>::P, 2) col_kernel(const PassArgs a) 
 #pragma unroll
         for (int j = 0; j < Q; ++j) {
             const int e = n2 * (t + P * j);
-            v[j] = cmulc_df(cmulc_df(v[j], s_tc[e >> sh]), s_tl[e & mask]);
+            v[j] = cmulc_df(cmulc_df(v[j], s_hi[e >> sh]), s_lo[swz8(e & mask)]);
         }
-        fft_pq<P, Q, true, true>(v, sx, lay, t, s_tc);
+        fft_pq<P, Q, true, true>(v, sx, lay, t, s_fc);
     }
     if (op == COL_KERR) {
         // src/focss/solver/ssfm.cpp:160-164: A *= exp(i kappa gamma h |A|^2)
@@ -191,11 +195,11 @@ __global__ void __launch_bounds__(C* PQ<N1>::P, 2) col_kernel(const PassArgs a) 
         }
     }
     if (op == COL_FWD || op == COL_KERR) {
-        fft_pq<P, Q, false, true>(v, sx, lay, t, s_tc);
+        fft_pq<P, Q, false, true>(v, sx, lay, t, s_fc);
 #pragma unroll
         for (int j = 0; j < Q; ++j) {
             const int e = n2 * (t + P * j);
-            v[j] = cmul_df(cmul_df(v[j], s_tc[e >> sh]), s_tl[e & mask]);
+            v[j] = cmul_df(cmul_df(v[j], s_hi[e >> sh]), s_lo[swz8(e & mask)]);
         }
     }
 #pragma unroll
@@ -245,7 +249,7 @@ __global__ void __launch_bounds__(R* PQ<N2>::P, 2) row_kernel(const PassArgs a) 
     }
     for (int i = threadIdx.x; i < N2; i += blockDim.x) s_tw[i] = a.tw[a.N1 + i];
     if (st)
-        for (int i = threadIdx.x; i < 512; i += blockDim.x) s_T[i] = a.tw[a.N1 + 2 * N2 + i];
+        for (int i = threadIdx.x; i < 512; i += blockDim.x) s_T[i] = a.tw[2 * a.N1 + 2 * N2 + i];
     const int rl = threadIdx.x / P, t = threadIdx.x % P;
     const int k1 = blockIdx.x * R + rl;
     float2* base = a.data + (size_t)b * a.N + (size_t)k1 * N2 + t;
