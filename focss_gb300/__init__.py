@@ -11,3 +11,5 @@ from .api import (  # noqa: F401
     db_to_linear, db_to_natural, dbm_to_watts, disp_to_beta2, forward_propagation, launch_count,
     LIGHT_SPEED, MATH_PI, PLANCK,
 )
+from . import dsp  # noqa: F401,E402
+from .dsp import PhaseShiftEqualizer, ScalarEqualizer  # noqa: F401,E402

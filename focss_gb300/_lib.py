@@ -66,6 +66,28 @@ SIGNATURES = {
     "focss_forward_propagation": (I, [P, P, C.POINTER(CFiber), C.POINTER(CSsfmOpts), D, D, U64, U64, I]),
     "focss_backward_propagation": (I, [P, P, C.POINTER(CFiber), C.POINTER(CSsfmOpts), D, I]),
     "focss_cd_compensation": (I, [P, P, C.POINTER(CFiber), I]),
+    "focss_qam16_map": (I, [P, P, SZ, P]),
+    "focss_upsample": (I, [P, P, I, P]),
+    "focss_downsample": (I, [P, P, I, P]),
+    "focss_decimate": (I, [P, P, I, P]),
+    "focss_rrc_pulse": (I, [P, I, I, D, P]),
+    "focss_filter": (I, [P, P, P, I]),
+    "focss_rrc_shaping": (I, [P, P, I, D, D, P]),
+    "focss_rrc_sampling": (I, [P, P, I, D, D, P]),
+    "focss_frequency_shift": (I, [P, P, D]),
+    "focss_bandpass": (I, [P, P, D]),
+    "focss_wdm_select": (I, [P, P, I, D, P]),
+    "focss_wdm_mux": (I, [P, P, D, P]),
+    "focss_hard_decision": (I, [P, P, P]),
+    "focss_hd_codes": (I, [P, P, P]),
+    "focss_error_counts": (I, [P, P, P, I, P, P]),
+    "focss_bit_error_rate": (I, [P, P, P, I, P]),
+    "focss_symbol_error_rate": (I, [P, P, P, I, P]),
+    "focss_q2_factor": (I, [P, P, P, I, P]),
+    "focss_pse_estimate": (I, [P, P, P, I, P]),
+    "focss_scalar_estimate": (I, [P, P, P, P]),
+    "focss_field_rotate": (I, [P, P, P]),
+    "focss_field_scale_each": (I, [P, P, P]),
     "focss_profile_enable": (I, [P, I]),
     "focss_profile_read": (I, [P, P, P, P, P, I]),
     "focss_launch_count": (C.c_longlong, []),

@@ -11,9 +11,6 @@
 using fg::Ctx;
 using fg::Field;
 
-struct focss_ctx : Ctx {};
-struct focss_field : Field {};
-
 namespace fg {
 
 focss_status set_error(Ctx* ctx, focss_status st, const std::string& msg) {
@@ -186,6 +183,7 @@ FOCSS_API focss_status focss_ctx_destroy(focss_ctx* c) {
     for (auto& kv : c->plans) cudaFree(kv.second.tw);
     for (void* p : c->scratch) cudaFree(p);
     for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
+    for (auto& kv : c->tables) cudaFree(kv.second);
     cudaFree(c->d_state);
     cudaFree(c->d_counters);
     cudaFree(c->d_red);

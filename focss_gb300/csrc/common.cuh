@@ -18,6 +18,23 @@ __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 __device__ __forceinline__ float cnorm(float2 a) { return fmaf(a.x, a.x, a.y * a.y); }
 
+// (cos phi, sin phi).  |phi| <= 1/4 (every step of an adaptive grid, whose
+// nonlinear phase is bounded by construction): Taylor polynomials to degree
+// 8/9 (truncation < 3e-13), about one FP32 rounding; larger phases fall back
+// to sincosf.
+__device__ __forceinline__ float2 phase_rotation(float phi) {
+    if (fabsf(phi) <= 0.25f) {
+        const float p2 = phi * phi;
+        const float s = phi * fmaf(p2, fmaf(p2, fmaf(p2, -1.0f / 5040.0f, 1.0f / 120.0f), -1.0f / 6.0f), 1.0f);
+        const float c = fmaf(p2, fmaf(p2, fmaf(p2, fmaf(p2, 1.0f / 40320.0f, -1.0f / 720.0f), 1.0f / 24.0f), -0.5f),
+                             1.0f);
+        return make_float2(c, s);
+    }
+    float s, c;
+    sincosf(phi, &s, &c);
+    return make_float2(c, s);
+}
+
 // Block-wide reductions (blockDim.x multiple of 32, <= 1024).
 __device__ __forceinline__ float warp_max(float v) {
 #pragma unroll

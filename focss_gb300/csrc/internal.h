@@ -84,6 +84,8 @@ struct Ctx {
     size_t red_cap = 0;
     std::vector<void*> scratch;      // generic device scratch buffers
     std::vector<size_t> scratch_cap;
+    // device-resident derived tables keyed by their parameters (RRC spectra, ...)
+    std::map<std::string, void*> tables;
     // instrumentation (focss_profile_*)
     bool profiling = false;
     std::vector<cudaEvent_t> prof_events;
@@ -138,3 +140,7 @@ cudaError_t launch_transpose_from_natural(const float2* src, float2* dst, int N1
                                           cudaStream_t st);
 
 }  // namespace fg
+
+// The opaque handles of the C ABI.
+struct focss_ctx : fg::Ctx {};
+struct focss_field : fg::Field {};

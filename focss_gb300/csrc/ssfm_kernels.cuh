@@ -181,9 +181,7 @@ __global__ void __launch_bounds__(C* PQ<N1>::P, 2) col_kernel(const PassArgs a) 
         const float coef = (float)(a.prm.kappa * a.prm.gamma * st->h);
 #pragma unroll
         for (int j = 0; j < Q; ++j) {
-            float s, cs;
-            sincosf(coef * cnorm(v[j]), &s, &cs);
-            v[j] = cmul(v[j], make_float2(cs, s));
+            v[j] = cmul(v[j], phase_rotation(coef * cnorm(v[j])));
             pk = fmaxf(pk, cnorm(v[j]));
         }
     } else if (op == COL_FWD && st) {

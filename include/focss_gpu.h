@@ -167,6 +167,81 @@ FOCSS_API focss_status focss_backward_propagation(focss_ctx* ctx, focss_field* f
 FOCSS_API focss_status focss_cd_compensation(focss_ctx* ctx, focss_field* field,
                                              const focss_fiber* fiber, int spans);
 
+/* --------------------------------------------------- TX / resampling DSP */
+/* Output fields must be created by the caller with the shape the reference
+ * would produce (same modes and batch; samples as stated).  Inputs are not
+ * modified unless stated. */
+
+/* gray_symbols_16qam (src/focss/processing/modulation.cpp:9-17):
+ * out[i] = Gray 16QAM point of codes[i] & 15, unit average power.
+ * codes: host int32 array of batch*modes*samples entries in field order. */
+FOCSS_API focss_status focss_qam16_map(focss_ctx* ctx, const int32_t* codes, size_t n, focss_field* out);
+/* Field::upsample / downsample (src/focss/field.cpp:272-297):
+ * out->samples = in->samples * factor  /  in->samples / factor. */
+FOCSS_API focss_status focss_upsample(focss_ctx* ctx, const focss_field* in, int factor, focss_field* out);
+FOCSS_API focss_status focss_downsample(focss_ctx* ctx, const focss_field* in, int factor, focss_field* out);
+/* Field::decimate (src/focss/field.cpp:299-320): spectral truncation,
+ * out->samples = in->samples / factor. */
+FOCSS_API focss_status focss_decimate(focss_ctx* ctx, const focss_field* in, int factor, focss_field* out);
+/* pulse::rrc (src/focss/processing/modulation.cpp:47-74), computed on the
+ * device in FP64; taps: host array of n_symbols*osf complex (interleaved). */
+FOCSS_API focss_status focss_rrc_pulse(focss_ctx* ctx, int n_symbols, int osf, double roll_off, double* taps);
+/* Field::filter_inplace (src/focss/field.cpp:358-372): circular convolution
+ * with an ifftshifted impulse response h (host, interleaved, h_len <= samples). */
+FOCSS_API focss_status focss_filter(focss_ctx* ctx, focss_field* field, const double* h, int h_len);
+/* rrc_shaping / rrc_sampling (src/focss/processing/modulation.cpp:85-96).
+ * The reference fixes the roll-off at 0.01 (:85); here it is a parameter. */
+FOCSS_API focss_status focss_rrc_shaping(focss_ctx* ctx, const focss_field* symbols, int osf, double roll_off,
+                                         double gain, focss_field* out);
+FOCSS_API focss_status focss_rrc_sampling(focss_ctx* ctx, const focss_field* signal, int osf, double roll_off,
+                                          double gain, focss_field* out);
+/* frequency_shift / bandpass_filter (src/focss/processing/modulation.cpp:255-277), in place. */
+FOCSS_API focss_status focss_frequency_shift(focss_ctx* ctx, focss_field* field, double frequency);
+FOCSS_API focss_status focss_bandpass(focss_ctx* ctx, focss_field* field, double frequency);
+/* wdm_select (src/focss/processing/modulation.cpp:248-253): out = channel
+ * `channel_index` of in, shifted to baseband and brick-wall filtered. */
+FOCSS_API focss_status focss_wdm_select(focss_ctx* ctx, const focss_field* in, int channel_index,
+                                        double channel_bandwidth, focss_field* out);
+/* wdm_mux (src/focss/processing/modulation.cpp:225-235): channel c is
+ * realization c of `channels` (batch = number of channels); out has batch 1. */
+FOCSS_API focss_status focss_wdm_mux(focss_ctx* ctx, const focss_field* channels, double channel_bandwidth,
+                                     focss_field* out);
+
+/* ------------------------------------------------- RX decisions / metrics */
+/* Per-realization outputs are host arrays of length batch.  A negative `cut`
+ * selects the reference's overload without a cut (same as cut = 0). */
+
+/* hard_decision_16qam (src/focss/processing/modulation.cpp:112-120). */
+FOCSS_API focss_status focss_hard_decision(focss_ctx* ctx, const focss_field* in, focss_field* out);
+/* hd_sequence_16qam (src/focss/processing/modulation.cpp:148-156): codes is a
+ * host int32 array of batch*modes*samples. */
+FOCSS_API focss_status focss_hd_codes(focss_ctx* ctx, const focss_field* in, int32_t* codes);
+/* Decision error counts behind bit_error_rate_16qam / symbol_error_rate_16qam
+ * (src/focss/processing/modulation.cpp:158-223), over samples [cut, samples-cut). */
+FOCSS_API focss_status focss_error_counts(focss_ctx* ctx, const focss_field* tx, const focss_field* rx, int cut,
+                                          uint64_t* bit_errors, uint64_t* symbol_errors);
+/* bit_error_rate_16qam (denominator 4*size - 8*cut, :200-201) and
+ * symbol_error_rate_16qam (denominator size - modes*cut, :221-222). */
+FOCSS_API focss_status focss_bit_error_rate(focss_ctx* ctx, const focss_field* tx, const focss_field* rx, int cut,
+                                            double* ber);
+FOCSS_API focss_status focss_symbol_error_rate(focss_ctx* ctx, const focss_field* tx, const focss_field* rx,
+                                               int cut, double* ser);
+/* q2_factor / evm2_factor (src/focss/functions.cpp:27-80), FP64 sums. */
+FOCSS_API focss_status focss_q2_factor(focss_ctx* ctx, const focss_field* tx, const focss_field* rx, int cut,
+                                       double* q2);
+/* PhaseShiftEqualizer::estimate (src/focss/equalizer/phase_shift_equalizer.cpp:30-46):
+ * argmax over the angle grid 2 pi i / angle_steps of q2(desired, actual e^{i angle}). */
+FOCSS_API focss_status focss_pse_estimate(focss_ctx* ctx, const focss_field* desired, const focss_field* actual,
+                                          int angle_steps, double* angle);
+/* ScalarEqualizer::estimate (src/focss/equalizer/scalar_equalizer.cpp:22-33):
+ * sum conj(a) d / sum |a|^2; scalar is 2*batch doubles (re, im). */
+FOCSS_API focss_status focss_scalar_estimate(focss_ctx* ctx, const focss_field* desired, const focss_field* actual,
+                                             double* scalar);
+/* Field * i_exp(angle[b]) and Field * scalar[b] per realization
+ * (PhaseShiftEqualizer::equalize :17-19, ScalarEqualizer::equalize :12-14). */
+FOCSS_API focss_status focss_field_rotate(focss_ctx* ctx, focss_field* field, const double* angle);
+FOCSS_API focss_status focss_field_scale_each(focss_ctx* ctx, focss_field* field, const double* scalar);
+
 /* ------------------------------------------------------- instrumentation */
 /* No reference counterpart (the reference only prints progress to std::cout,
  * src/focss/solver/ssfm.cpp:117).
