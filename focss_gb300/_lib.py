@@ -88,6 +88,8 @@ SIGNATURES = {
     "focss_scalar_estimate": (I, [P, P, P, P]),
     "focss_field_rotate": (I, [P, P, P]),
     "focss_field_scale_each": (I, [P, P, P]),
+    "focss_triplet_apply": (I, [P, P, I, I, P, P, P, P]),
+    "focss_sino_equalize": (I, [P, P, P, I, I, P, P, P, D, D, P]),
     "focss_ssfm_run_noalloc": (I, [P, P, I, I, D, C.POINTER(CFiber), C.POINTER(CSsfmOpts), D, P]),
     "focss_profile_enable": (I, [P, I]),
     "focss_profile_read": (I, [P, P, P, P, P, I]),

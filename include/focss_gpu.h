@@ -242,6 +242,23 @@ FOCSS_API focss_status focss_scalar_estimate(focss_ctx* ctx, const focss_field* 
 FOCSS_API focss_status focss_field_rotate(focss_ctx* ctx, focss_field* field, const double* angle);
 FOCSS_API focss_status focss_field_scale_each(focss_ctx* ctx, focss_field* field, const double* scalar);
 
+/* ---------------------------------------- perturbation (triplet) equalizer */
+/* SINO::cubic (src/focss/equalizer/sino.cpp:161-171, 203-220) over an
+ * explicit term list: out[mode][k] = sum_i C_i A_mode[k+m_i]
+ * sum_p A_p[k+n_i] conj(A_p[k+m_i+n_i]) for k in [radius, samples-radius),
+ * zero elsewhere.  Samples outside the field count as zero (box-shaped term
+ * sets are accepted as well as the reference's |m|+|n| <= radius diamond).
+ * coef: n_terms complex (interleaved FP64 on the host, complex64 on the
+ * device); duplicate (m, n) entries add.  |m|, |n| <= 4096.  1 or 2 modes. */
+FOCSS_API focss_status focss_triplet_apply(focss_ctx* ctx, const focss_field* in, int radius, int n_terms,
+                                           const int32_t* m, const int32_t* n, const double* coef,
+                                           focss_field* out);
+/* SINO::equalize (src/focss/equalizer/sino.cpp:193-196):
+ * out = (rx - cubic(tx)) / linear_weight. */
+FOCSS_API focss_status focss_sino_equalize(focss_ctx* ctx, const focss_field* rx, const focss_field* tx, int radius,
+                                           int n_terms, const int32_t* m, const int32_t* n, const double* coef,
+                                           double linear_weight_re, double linear_weight_im, focss_field* out);
+
 /* ------------------------------------------------- allocation-free SSFM */
 /* No counterpart in the reference.  The same computation as focss_ssfm_run
  * (SSFM::run on every realization) for callers that cannot let a library

@@ -771,12 +771,23 @@ void ofc_sino_cubic(int modes, int samples, const double* a, int radius,
 void ofc_triplet_sparse(int modes, int samples, const double* a, int radius,
                         int n_terms, const int32_t* m, const int32_t* n,
                         const double* c, double* out) {
+    /* Terms may reach k + m + n outside [0, samples) (|m|,|n| <= R box sets):
+     * such samples count as zero.  Diamond sets (|m|+|n| <= R, the
+     * reference's SINO::cubic) never leave the range. */
     memset(out, 0, sizeof(double) * 2 * (size_t)modes * samples);
     for (int mode = 0; mode < modes; ++mode)
         for (int k = radius; k < samples - radius; ++k) {
             double sr = 0, si = 0;
             for (int i = 0; i < n_terms; ++i) {
                 double t[2];
+                int lo = k + (m[i] < 0 ? m[i] : 0) + (n[i] < 0 ? n[i] : 0);
+                int hi = k + (m[i] > 0 ? m[i] : 0) + (n[i] > 0 ? n[i] : 0);
+                if (lo < 0 || hi >= samples) {
+                    /* evaluate with zero padding */
+                    int km = k + m[i], kn = k + n[i], kmn = k + m[i] + n[i];
+                    if (km < 0 || km >= samples || kn < 0 || kn >= samples || kmn < 0 || kmn >= samples)
+                        continue;
+                }
                 sino_term(modes, samples, a, mode, k, m[i], n[i], t);
                 sr += c[2 * i] * t[0] - c[2 * i + 1] * t[1];
                 si += c[2 * i] * t[1] + c[2 * i + 1] * t[0];
