@@ -90,6 +90,14 @@ SIGNATURES = {
     "focss_field_scale_each": (I, [P, P, P]),
     "focss_triplet_apply": (I, [P, P, I, I, P, P, P, P]),
     "focss_sino_equalize": (I, [P, P, P, I, I, P, P, P, D, D, P]),
+    "focss_ldbp_create": (I, [P, I, I, I, I, I, I, D, C.POINTER(P)]),
+    "focss_ldbp_destroy": (I, [P]),
+    "focss_ldbp_num_params": (I, [P]),
+    "focss_ldbp_set_params": (I, [P, P, I]),
+    "focss_ldbp_get_params": (I, [P, P, P, I]),
+    "focss_ldbp_forward": (I, [P, P, P]),
+    "focss_ldbp_loss_grad": (I, [P, P, P, P]),
+    "focss_ldbp_adam_step": (I, [P, D, D, D, D]),
     "focss_ssfm_run_noalloc": (I, [P, P, I, I, D, C.POINTER(CFiber), C.POINTER(CSsfmOpts), D, P]),
     "focss_profile_enable": (I, [P, I]),
     "focss_profile_read": (I, [P, P, P, P, P, I]),

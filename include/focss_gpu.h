@@ -259,6 +259,30 @@ FOCSS_API focss_status focss_sino_equalize(focss_ctx* ctx, const focss_field* rx
                                            int n_terms, const int32_t* m, const int32_t* n, const double* coef,
                                            double linear_weight_re, double linear_weight_im, focss_field* out);
 
+/* ---------------------------------------------------------- learned DBP */
+/* No reference counterpart: a few-step learned replacement of
+ * backward_propagation (src/tasks/systems.cpp:73-91).  Per realization (one
+ * mode, `samples` at 2 samples/symbol): for each span, x *= span_scale
+ * (drop_power), then steps_per_span x [circular FIR of `taps` complex taps,
+ * x *= exp(i xi |x|^2)]; then a matched FIR of `mf_taps` taps and symbols =
+ * y[0::2].  FIR(x, h)[n] = sum_t h[t] x[(n + t - (T-1)/2) mod samples].
+ * Parameters (float, host layout): [taps: spans*steps*taps complex]
+ * [xi: spans*steps, padded to an even count][matched taps: mf_taps complex].
+ * Training: focss_ldbp_loss_grad runs forward and backward (hand-written
+ * kernels, Wirtinger gradients dL/dconj(z)) for L = mean |symbols - tx|^2;
+ * focss_ldbp_adam_step updates the parameters on the device. */
+typedef struct focss_ldbp focss_ldbp;
+FOCSS_API focss_status focss_ldbp_create(focss_ctx* ctx, int spans, int steps_per_span, int taps, int mf_taps,
+                                         int samples, int batch, double span_scale, focss_ldbp** out);
+FOCSS_API focss_status focss_ldbp_destroy(focss_ldbp* model);
+FOCSS_API int focss_ldbp_num_params(const focss_ldbp* model);
+FOCSS_API focss_status focss_ldbp_set_params(focss_ldbp* model, const float* params, int n);
+FOCSS_API focss_status focss_ldbp_get_params(focss_ldbp* model, float* params, float* grads, int n);
+FOCSS_API focss_status focss_ldbp_forward(focss_ldbp* model, const focss_field* in, focss_field* symbols);
+FOCSS_API focss_status focss_ldbp_loss_grad(focss_ldbp* model, const focss_field* in, const focss_field* tx,
+                                            double* loss);
+FOCSS_API focss_status focss_ldbp_adam_step(focss_ldbp* model, double lr, double beta1, double beta2, double eps);
+
 /* ------------------------------------------------- allocation-free SSFM */
 /* No counterpart in the reference.  The same computation as focss_ssfm_run
  * (SSFM::run on every realization) for callers that cannot let a library
