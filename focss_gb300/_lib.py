@@ -98,6 +98,14 @@ SIGNATURES = {
     "focss_ldbp_forward": (I, [P, P, P]),
     "focss_ldbp_loss_grad": (I, [P, P, P, P]),
     "focss_ldbp_adam_step": (I, [P, D, D, D, D]),
+    "focss_cnn_create": (I, [P, I, I, I, I, D, C.POINTER(P)]),
+    "focss_cnn_destroy": (I, [P]),
+    "focss_cnn_num_params": (I, [P]),
+    "focss_cnn_set_params": (I, [P, P, I]),
+    "focss_cnn_get_params": (I, [P, P, P, I]),
+    "focss_cnn_forward": (I, [P, P, P]),
+    "focss_cnn_loss_grad": (I, [P, P, P, P]),
+    "focss_cnn_adam_step": (I, [P, D, D, D, D]),
     "focss_ssfm_run_noalloc": (I, [P, P, I, I, D, C.POINTER(CFiber), C.POINTER(CSsfmOpts), D, P]),
     "focss_profile_enable": (I, [P, I]),
     "focss_profile_read": (I, [P, P, P, P, P, I]),

@@ -1,0 +1,92 @@
+"""Convolutional correction of the learned-DBP output (focss_cnn_*): a 4-layer
+1D CNN (64 channels, kernel 9) on [Re y, Im y] whose output is added back to
+the symbols.  Training (forward, backward, Adam) runs on the GPU."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import check, lib
+from .api import Context, Field
+
+P = C.c_void_p
+LAYERS = ((16, 64), (64, 64), (64, 64), (64, 16))  # (cin, cout), padded
+KW = 9
+
+
+def layout():
+    """[(w_offset, w_shape, b_offset, cout)] of the flat parameter vector."""
+    out, o = [], 0
+    for cin, cout in LAYERS:
+        out.append((o, (cout, KW, cin), o + cout * KW * cin, cout))
+        o += cout * KW * cin + cout
+    return out, o
+
+
+def he_init(rng, zero_last=True):
+    lay, total = layout()
+    p = np.zeros(total, np.float32)
+    fan = [2 * KW, 64 * KW, 64 * KW, 64 * KW]  # real fan-in (2 used input channels in layer 1)
+    for l, (wo, shape, bo, cout) in enumerate(lay):
+        w = rng.standard_normal(shape) * np.sqrt(2.0 / fan[l])
+        if l == 0:
+            w[:, :, 2:] = 0
+        if l == 3:
+            w[2:] = 0
+            if zero_last:
+                w[:] = 0
+        p[wo:wo + w.size] = w.ravel()
+    return p
+
+
+class CorrectionCNN:
+    def __init__(self, length, batch, input_scale, ctx=None):
+        self.ctx = ctx or Context.default()
+        self.length, self.batch = length, batch
+        h = C.c_void_p()
+        check(lib().focss_cnn_create(self.ctx.h, 64, KW, length, batch, input_scale, C.byref(h)), self.ctx.h)
+        self.h = h
+        self.n_params = lib().focss_cnn_num_params(h)
+
+    def set_params(self, flat):
+        f = np.ascontiguousarray(flat, np.float32)
+        check(lib().focss_cnn_set_params(self.h, f.ctypes.data_as(P), f.size), self.ctx.h)
+
+    def get_params(self):
+        p = np.zeros(self.n_params, np.float32)
+        g = np.zeros(self.n_params, np.float32)
+        check(lib().focss_cnn_get_params(self.h, p.ctypes.data_as(P), g.ctypes.data_as(P), p.size), self.ctx.h)
+        return p, g
+
+    def forward(self, y: Field) -> Field:
+        z = Field(y.domain, batch=y.batch, ctx=self.ctx)
+        check(lib().focss_cnn_forward(self.h, y.h, z.h), self.ctx.h)
+        return z
+
+    def loss_grad(self, y: Field, tx: Field) -> float:
+        loss = C.c_double()
+        check(lib().focss_cnn_loss_grad(self.h, y.h, tx.h, C.byref(loss)), self.ctx.h)
+        return loss.value
+
+    def adam_step(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
+        check(lib().focss_cnn_adam_step(self.h, lr, beta1, beta2, eps), self.ctx.h)
+
+    def fit(self, y: Field, tx: Field, iters=100, lr=1e-3):
+        hist = []
+        for _ in range(iters):
+            hist.append(self.loss_grad(y, tx))
+            self.adam_step(lr)
+        return hist
+
+    def close(self):
+        from ._lib import alive
+        if getattr(self, "h", None) and alive():
+            lib().focss_cnn_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

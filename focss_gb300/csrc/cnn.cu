@@ -1,0 +1,537 @@
+// cnn.cu -- 1D convolutional correction network for the learned-DBP output.
+//
+// z = y + s * (Delta_re + i Delta_im), Delta = conv4(relu(conv3(relu(conv2(
+//     relu(conv1(x0))))))), x0 = [Re y / s, Im y / s] (2 channels, padded to
+// 16), 64 channels, kernel 9, zero padding at the sequence ends.  Weights are
+// BF16 (FP32 master copy for Adam), activations BF16 channels-last, all
+// products accumulate in FP32 on the tensor cores (warp-level
+// mma.sync.m16n8k16 BF16 implicit GEMMs).  Loss L = mean |z - tx|^2.
+//
+// Forward conv: out[p][co] = b[co] + sum_{kk<9, ci} W[co][kk][ci] in[p+kk-4][ci]
+//   GEMM D[co][p], M = COUT, N = positions, K = 9*CIN.
+// Input gradient: the same conv with W'[ci][kk][co] = W[co][8-kk][ci].
+// Weight gradient: gW[co][kk][ci] = sum_p g[p][co] in[p+kk-4][ci]
+//   GEMM M = COUT, N = CIN per tap, K = positions (chunked, atomics).
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <new>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace fg {
+namespace {
+
+typedef __nv_bfloat16 bf16;
+constexpr int KW = 9;       // kernel width
+constexpr int HALF = 4;     // (KW - 1) / 2
+constexpr int NP = 128;     // positions per forward CTA (4 warps x 32)
+constexpr int CW = 64;      // hidden channels
+constexpr int CIN0 = 16;    // padded input channels (2 used)
+constexpr int COUT4 = 16;   // padded output channels (2 used)
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ uint32_t ld32(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+__device__ __forceinline__ uint32_t pack2(bf16 lo, bf16 hi) {
+    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+// ------------------------------------------------------------ forward conv
+// in: [B][L][CIN] bf16, W: [COUT][KW][CIN] bf16, bias: [COUT] f32.
+// out: [B][L][COUT] (bf16, or f32 when OUT_F32).  relu: apply max(0, .).
+// mask (optional, [B][L][COUT] bf16): multiply the result by (mask > 0).
+template <int CIN, int COUT, bool OUT_F32>
+__global__ void __launch_bounds__(128) conv_fwd_kernel(const bf16* __restrict__ in, const bf16* __restrict__ W,
+                                                       const float* __restrict__ bias, void* __restrict__ out,
+                                                       int L, int relu, const bf16* __restrict__ mask) {
+    constexpr int KS = KW * CIN + 8;   // padded weight row (bank spread)
+    constexpr int AS = CIN + 8;        // padded activation row
+    constexpr int MT = COUT / 16;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    bf16* Ws = reinterpret_cast<bf16*>(smem_raw);
+    bf16* As = Ws + COUT * KS;
+    const int b = blockIdx.y;
+    const int p0 = blockIdx.x * NP;
+    const bf16* inb = in + (size_t)b * L * CIN;
+    for (int i = threadIdx.x; i < COUT * KW * CIN; i += blockDim.x) {
+        const int co = i / (KW * CIN), k = i % (KW * CIN);
+        Ws[co * KS + k] = W[i];
+    }
+    for (int i = threadIdx.x; i < (NP + 2 * HALF) * CIN; i += blockDim.x) {
+        const int r = i / CIN, ci = i % CIN;
+        const int p = p0 - HALF + r;
+        As[r * AS + ci] = (p >= 0 && p < L) ? inb[(size_t)p * CIN + ci] : __float2bfloat16(0.f);
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    float acc[MT][4][4];
+#pragma unroll
+    for (int mt = 0; mt < MT; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[mt][nt][q] = 0.f;
+#pragma unroll 1
+    for (int kk = 0; kk < KW; ++kk) {
+#pragma unroll
+        for (int c0 = 0; c0 < CIN; c0 += 16) {
+            uint32_t af[MT][4];
+#pragma unroll
+            for (int mt = 0; mt < MT; ++mt) {
+                const bf16* w0 = Ws + (16 * mt + g) * KS + kk * CIN + c0 + 2 * t;
+                af[mt][0] = ld32(w0);
+                af[mt][1] = ld32(w0 + 8 * KS);
+                af[mt][2] = ld32(w0 + 8);
+                af[mt][3] = ld32(w0 + 8 * KS + 8);
+            }
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt) {
+                const int n = 32 * warp + 8 * nt + g;
+                const bf16* a0 = As + (n + kk) * AS + c0 + 2 * t;
+                const uint32_t bfr[2] = {ld32(a0), ld32(a0 + 8)};
+#pragma unroll
+                for (int mt = 0; mt < MT; ++mt) mma_bf16(acc[mt][nt], af[mt], bfr);
+            }
+        }
+    }
+    const size_t ob = (size_t)b * L * COUT;
+#pragma unroll
+    for (int mt = 0; mt < MT; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int co = 16 * mt + g + (q >= 2 ? 8 : 0);
+                const int p = p0 + 32 * warp + 8 * nt + 2 * t + (q & 1);
+                if (p >= L) continue;
+                float v = acc[mt][nt][q] + (bias ? bias[co] : 0.f);
+                if (relu) v = fmaxf(v, 0.f);
+                if (mask && !(__bfloat162float(mask[ob + (size_t)p * COUT + co]) > 0.f)) v = 0.f;
+                if (OUT_F32)
+                    reinterpret_cast<float*>(out)[ob + (size_t)p * COUT + co] = v;
+                else
+                    reinterpret_cast<bf16*>(out)[ob + (size_t)p * COUT + co] = __float2bfloat16(v);
+            }
+}
+
+// ------------------------------------------------------------ weight gradient
+// gW[co][kk][ci] += sum_p g[p][co] in[p+kk-4][ci] over the CTA's position
+// chunk; grid = (KW, chunks, B).  Tiles of 64 positions are staged transposed
+// (channel-major) so fragments are 32-bit shared loads.
+constexpr int WG_TILE = 64;
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(128) conv_wgrad_kernel(const bf16* __restrict__ gout, const bf16* __restrict__ in,
+                                                         float* __restrict__ gW, int L, int chunk) {
+    constexpr int PS = WG_TILE + 8;   // padded position stride
+    constexpr int MT = COUT / 16;     // m16 tiles (COUT)
+    constexpr int NT = CIN / 8;       // n8 tiles (CIN)
+    constexpr int WM = MT >= 4 ? MT / 4 : 1;   // m tiles per warp
+    constexpr int WN = MT >= 4 ? NT : NT / 4;  // n tiles per warp (split N when COUT < 64)
+    __shared__ __align__(16) bf16 gT[COUT][PS];
+    __shared__ __align__(16) bf16 iT[CIN][PS];
+    const int kk = blockIdx.x, b = blockIdx.z;
+    const int pstart = blockIdx.y * chunk, pend = min(L, pstart + chunk);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int m_base = MT >= 4 ? warp * WM : 0;
+    const int n_base = MT >= 4 ? 0 : warp * WN;
+    float acc[WM][WN][4];
+#pragma unroll
+    for (int i = 0; i < WM; ++i)
+#pragma unroll
+        for (int j = 0; j < WN; ++j)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
+    const bf16* gb = gout + (size_t)b * L * COUT;
+    const bf16* ib = in + (size_t)b * L * CIN;
+    for (int p0 = pstart; p0 < pend; p0 += WG_TILE) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < WG_TILE * COUT; i += blockDim.x) {
+            const int pp = i / COUT, co = i % COUT, p = p0 + pp;
+            gT[co][pp] = (p < pend) ? gb[(size_t)p * COUT + co] : __float2bfloat16(0.f);
+        }
+        for (int i = threadIdx.x; i < WG_TILE * CIN; i += blockDim.x) {
+            const int pp = i / CIN, ci = i % CIN, p = p0 + pp, s = p + kk - HALF;
+            iT[ci][pp] = (p < pend && s >= 0 && s < L) ? ib[(size_t)s * CIN + ci] : __float2bfloat16(0.f);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k0 = 0; k0 < WG_TILE; k0 += 16) {
+#pragma unroll
+            for (int i = 0; i < WM; ++i) {
+                const int m0 = 16 * (m_base + i);
+                uint32_t af[4] = {ld32(&gT[m0 + g][k0 + 2 * t]), ld32(&gT[m0 + g + 8][k0 + 2 * t]),
+                                  ld32(&gT[m0 + g][k0 + 2 * t + 8]), ld32(&gT[m0 + g + 8][k0 + 2 * t + 8])};
+#pragma unroll
+                for (int j = 0; j < WN; ++j) {
+                    const int n0 = 8 * (n_base + j);
+                    const uint32_t bfr[2] = {ld32(&iT[n0 + g][k0 + 2 * t]), ld32(&iT[n0 + g][k0 + 2 * t + 8])};
+                    mma_bf16(acc[i][j], af, bfr);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < WM; ++i)
+#pragma unroll
+        for (int j = 0; j < WN; ++j)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int co = 16 * (m_base + i) + g + (q >= 2 ? 8 : 0);
+                const int ci = 8 * (n_base + j) + 2 * t + (q & 1);
+                atomicAdd(&gW[((size_t)co * KW + kk) * CIN + ci], acc[i][j][q]);
+            }
+}
+
+// bias gradient: gb[co] += sum_p g[p][co]
+template <int C>
+__global__ void bias_grad_kernel(const bf16* __restrict__ g, size_t positions, float* __restrict__ gb) {
+    float acc[C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) acc[c] = 0.f;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < positions; p += (size_t)gridDim.x * blockDim.x)
+#pragma unroll
+        for (int c = 0; c < C; ++c) acc[c] += __bfloat162float(g[p * C + c]);
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        const float v = warp_sum(acc[c]);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&gb[c], v);
+    }
+}
+
+// x0 = [Re y / s, Im y / s, 0 ...] (16 channels)
+__global__ void cnn_input_kernel(const float2* __restrict__ y, size_t n, float inv_s, bf16* __restrict__ x0) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float2 v = y[i];
+        bf16* o = x0 + i * CIN0;
+        o[0] = __float2bfloat16(v.x * inv_s);
+        o[1] = __float2bfloat16(v.y * inv_s);
+#pragma unroll
+        for (int c = 2; c < CIN0; ++c) o[c] = __float2bfloat16(0.f);
+    }
+}
+
+// z = y + s (d0 + i d1); with tx: loss += |z - tx|^2 / M, g4 = dL/dDelta (bf16, 16 ch)
+__global__ void cnn_output_kernel(const float2* __restrict__ y, const float* __restrict__ d4, size_t n, float s,
+                                  const float2* __restrict__ tx, float inv_m, float2* __restrict__ z,
+                                  bf16* __restrict__ g4, double* __restrict__ loss) {
+    double acc = 0.0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float2 v = make_float2(fmaf(s, d4[i * COUT4], y[i].x), fmaf(s, d4[i * COUT4 + 1], y[i].y));
+        if (z) z[i] = v;
+        if (tx) {
+            const float2 d = csub(v, tx[i]);
+            acc += (double)cnorm(d);
+            bf16* o = g4 + i * COUT4;
+            o[0] = __float2bfloat16(2.f * s * d.x * inv_m);
+            o[1] = __float2bfloat16(2.f * s * d.y * inv_m);
+#pragma unroll
+            for (int c = 2; c < COUT4; ++c) o[c] = __float2bfloat16(0.f);
+        }
+    }
+    __shared__ double sd[32];
+    acc = block_sum_d(acc, sd);
+    if (threadIdx.x == 0 && loss) atomicAdd(loss, acc * inv_m);
+}
+
+// BF16 weights and flipped transposes from the FP32 masters.
+__global__ void refresh_weights_kernel(const float* __restrict__ Wm, int cout, int cin, bf16* __restrict__ Wb,
+                                       bf16* __restrict__ Wt) {
+    const int n = cout * KW * cin;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int co = i / (KW * cin), kk = (i / cin) % KW, ci = i % cin;
+        const bf16 v = __float2bfloat16(Wm[i]);
+        Wb[i] = v;
+        Wt[((size_t)ci * KW + (KW - 1 - kk)) * cout + co] = v;   // W'[ci][8-kk][co]
+    }
+}
+
+__global__ void cnn_adam_kernel(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1,
+                                float* __restrict__ m2, int n, float lr, float b1, float b2, float eps, float c1,
+                                float c2) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float a = b1 * m1[i] + (1.f - b1) * gi;
+        const float v = b2 * m2[i] + (1.f - b2) * gi * gi;
+        m1[i] = a;
+        m2[i] = v;
+        p[i] -= lr * (a * c1) / (sqrtf(v * c2) + eps);
+    }
+}
+
+inline int gridn(size_t n) { return (int)std::max<size_t>(1, std::min<size_t>((n + 255) / 256, 152 * 16)); }
+
+template <int CIN, int COUT, bool F32>
+cudaError_t conv_fwd(const bf16* in, const bf16* W, const float* bias, void* out, int L, int B, int relu,
+                     const bf16* mask, cudaStream_t s) {
+    const size_t smem = sizeof(bf16) * ((size_t)COUT * (KW * CIN + 8) + (size_t)(NP + 2 * HALF) * (CIN + 8));
+    cudaError_t e = cudaFuncSetAttribute(conv_fwd_kernel<CIN, COUT, F32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    conv_fwd_kernel<CIN, COUT, F32><<<dim3((L + NP - 1) / NP, B), 128, smem, s>>>(in, W, bias, out, L, relu, mask);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <int CIN, int COUT>
+cudaError_t conv_wgrad(const bf16* g, const bf16* in, float* gW, int L, int B, cudaStream_t s) {
+    const int chunk = 2048;
+    conv_wgrad_kernel<CIN, COUT><<<dim3(KW, (L + chunk - 1) / chunk, B), 128, 0, s>>>(g, in, gW, L, chunk);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace
+}  // namespace fg
+
+// ---------------------------------------------------------------- model
+namespace {
+using fg::bf16;
+// parameter blocks (FP32 masters): W1 [64][9][16], b1 [64], W2 [64][9][64], b2,
+// W3 [64][9][64], b3, W4 [16][9][64], b4 [16]
+struct CnnLayout {
+    size_t w[4], b[4], total;
+    int cout[4] = {fg::CW, fg::CW, fg::CW, fg::COUT4}, cin[4] = {fg::CIN0, fg::CW, fg::CW, fg::CW};
+    CnnLayout() {
+        size_t o = 0;
+        for (int l = 0; l < 4; ++l) {
+            w[l] = o;
+            o += (size_t)cout[l] * fg::KW * cin[l];
+            b[l] = o;
+            o += cout[l];
+        }
+        total = o;
+    }
+};
+}  // namespace
+
+struct focss_cnn {
+    focss_ctx* ctx = nullptr;
+    int length = 0, batch = 0;
+    float scale = 1.f;
+    CnnLayout lay;
+    float* params = nullptr;   // masters, grads, m1, m2
+    float* grads = nullptr;
+    float* m1 = nullptr;
+    float* m2 = nullptr;
+    bf16* wb[4] = {};          // bf16 weights
+    bf16* wt[4] = {};          // bf16 flipped transposes
+    bf16* act[4] = {};         // x0 (16 ch), out1..out3 (64 ch)
+    float* d4 = nullptr;       // output (16 ch f32)
+    bf16* g64a = nullptr;      // gradient buffers
+    bf16* g64b = nullptr;
+    bf16* g16 = nullptr;
+    double* loss = nullptr;
+    void* block = nullptr;
+    int adam_t = 0;
+    size_t positions() const { return (size_t)length * batch; }
+};
+
+static cudaError_t cnn_forward(focss_cnn* m, const focss_field* y) {
+    cudaStream_t s = m->ctx->stream;
+    const int L = m->length, B = m->batch;
+    const size_t n = m->positions();
+    fg::cnn_input_kernel<<<fg::gridn(n), 256, 0, s>>>(y->d, n, 1.f / m->scale, m->act[0]);
+    fg::count_launch();
+    cudaError_t e = cudaGetLastError();
+    const float* P = m->params;
+    if (e == cudaSuccess)
+        e = fg::conv_fwd<fg::CIN0, fg::CW, false>(m->act[0], m->wb[0], P + m->lay.b[0], m->act[1], L, B, 1, nullptr, s);
+    if (e == cudaSuccess)
+        e = fg::conv_fwd<fg::CW, fg::CW, false>(m->act[1], m->wb[1], P + m->lay.b[1], m->act[2], L, B, 1, nullptr, s);
+    if (e == cudaSuccess)
+        e = fg::conv_fwd<fg::CW, fg::CW, false>(m->act[2], m->wb[2], P + m->lay.b[2], m->act[3], L, B, 1, nullptr, s);
+    if (e == cudaSuccess)
+        e = fg::conv_fwd<fg::CW, fg::COUT4, true>(m->act[3], m->wb[3], P + m->lay.b[3], m->d4, L, B, 0, nullptr, s);
+    return e;
+}
+
+static cudaError_t cnn_refresh(focss_cnn* m) {
+    cudaError_t e = cudaSuccess;
+    for (int l = 0; l < 4 && e == cudaSuccess; ++l) {
+        const int n = m->lay.cout[l] * fg::KW * m->lay.cin[l];
+        fg::refresh_weights_kernel<<<fg::gridn(n), 256, 0, m->ctx->stream>>>(m->params + m->lay.w[l], m->lay.cout[l],
+                                                                            m->lay.cin[l], m->wb[l], m->wt[l]);
+        fg::count_launch();
+        e = cudaGetLastError();
+    }
+    return e;
+}
+
+extern "C" {
+
+FOCSS_API focss_status focss_cnn_create(focss_ctx* c, int channels, int kernel, int length, int batch,
+                                        double input_scale, focss_cnn** out) {
+    if (!c || !out || length <= 0 || batch <= 0 || !(input_scale > 0)) return FOCSS_ERR_INVALID_ARG;
+    if (channels != fg::CW || kernel != fg::KW)
+        return fg::set_error(c, FOCSS_ERR_UNSUPPORTED, "cnn: 64 channels and kernel 9 are implemented");
+    focss_cnn* m = new (std::nothrow) focss_cnn();
+    if (!m) return FOCSS_ERR_OOM;
+    m->ctx = c;
+    m->length = length;
+    m->batch = batch;
+    m->scale = (float)input_scale;
+    const size_t P = m->lay.total, n = m->positions();
+    size_t bytes = sizeof(float) * 4 * P;
+    size_t wbytes = 0;
+    for (int l = 0; l < 4; ++l) wbytes += 2 * sizeof(bf16) * m->lay.cout[l] * fg::KW * m->lay.cin[l];
+    const size_t abytes = sizeof(bf16) * n * (fg::CIN0 + 3 * fg::CW) + sizeof(float) * n * fg::COUT4 +
+                          sizeof(bf16) * n * (2 * fg::CW + fg::COUT4) + 64;
+    cudaError_t e = cudaMalloc(&m->block, bytes + wbytes + abytes + 1024);
+    if (e != cudaSuccess) {
+        delete m;
+        return fg::cuda_check(c, e, "cnn alloc");
+    }
+    char* p = (char*)m->block;
+    auto take = [&](size_t b) { char* r = p; p += (b + 255) / 256 * 256; return (void*)r; };
+    m->params = (float*)take(sizeof(float) * 4 * P);
+    m->grads = m->params + P;
+    m->m1 = m->grads + P;
+    m->m2 = m->m1 + P;
+    for (int l = 0; l < 4; ++l) {
+        const size_t nw = (size_t)m->lay.cout[l] * fg::KW * m->lay.cin[l];
+        m->wb[l] = (bf16*)take(sizeof(bf16) * nw);
+        m->wt[l] = (bf16*)take(sizeof(bf16) * nw);
+    }
+    m->act[0] = (bf16*)take(sizeof(bf16) * n * fg::CIN0);
+    for (int l = 1; l < 4; ++l) m->act[l] = (bf16*)take(sizeof(bf16) * n * fg::CW);
+    m->d4 = (float*)take(sizeof(float) * n * fg::COUT4);
+    m->g64a = (bf16*)take(sizeof(bf16) * n * fg::CW);
+    m->g64b = (bf16*)take(sizeof(bf16) * n * fg::CW);
+    m->g16 = (bf16*)take(sizeof(bf16) * n * fg::COUT4);
+    m->loss = (double*)take(sizeof(double) * 2);
+    e = cudaMemsetAsync(m->params, 0, sizeof(float) * 4 * P, c->stream);
+    if (e == cudaSuccess) e = cnn_refresh(m);
+    if (e != cudaSuccess) {
+        cudaFree(m->block);
+        delete m;
+        return fg::cuda_check(c, e, "cnn init");
+    }
+    *out = m;
+    return FOCSS_OK;
+}
+
+FOCSS_API focss_status focss_cnn_destroy(focss_cnn* m) {
+    if (!m) return FOCSS_OK;
+    cudaStreamSynchronize(m->ctx->stream);
+    cudaFree(m->block);
+    delete m;
+    return FOCSS_OK;
+}
+
+FOCSS_API int focss_cnn_num_params(const focss_cnn* m) { return m ? (int)m->lay.total : 0; }
+
+FOCSS_API focss_status focss_cnn_set_params(focss_cnn* m, const float* host, int n) {
+    if (!m || !host || n != (int)m->lay.total) return FOCSS_ERR_INVALID_ARG;
+    cudaStream_t s = m->ctx->stream;
+    cudaError_t e = cudaMemcpyAsync(m->params, host, sizeof(float) * n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->m1, 0, sizeof(float) * 2 * n, s);
+    if (e == cudaSuccess) e = cnn_refresh(m);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    m->adam_t = 0;
+    return fg::cuda_check(m->ctx, e, "cnn set params");
+}
+
+FOCSS_API focss_status focss_cnn_get_params(focss_cnn* m, float* params, float* grads, int n) {
+    if (!m || n != (int)m->lay.total) return FOCSS_ERR_INVALID_ARG;
+    cudaStream_t s = m->ctx->stream;
+    cudaError_t e = cudaSuccess;
+    if (params) e = cudaMemcpyAsync(params, m->params, sizeof(float) * n, cudaMemcpyDeviceToHost, s);
+    if (grads && e == cudaSuccess) e = cudaMemcpyAsync(grads, m->grads, sizeof(float) * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return fg::cuda_check(m->ctx, e, "cnn get params");
+}
+
+static bool cnn_shape_ok(const focss_cnn* m, const focss_field* f) {
+    return f && f->modes == 1 && f->samples == m->length && f->batch == m->batch;
+}
+
+FOCSS_API focss_status focss_cnn_forward(focss_cnn* m, const focss_field* y, focss_field* z) {
+    if (!m || !cnn_shape_ok(m, y) || !cnn_shape_ok(m, z)) return FOCSS_ERR_INVALID_ARG;
+    cudaError_t e = cnn_forward(m, y);
+    const size_t n = m->positions();
+    if (e == cudaSuccess) {
+        fg::cnn_output_kernel<<<fg::gridn(n), 256, 0, m->ctx->stream>>>(y->d, m->d4, n, m->scale, nullptr, 0.f, z->d,
+                                                                         nullptr, nullptr);
+        fg::count_launch();
+        e = cudaGetLastError();
+    }
+    return fg::cuda_check(m->ctx, e, "cnn forward");
+}
+
+FOCSS_API focss_status focss_cnn_loss_grad(focss_cnn* m, const focss_field* y, const focss_field* tx, double* loss) {
+    if (!m || !cnn_shape_ok(m, y) || !cnn_shape_ok(m, tx)) return FOCSS_ERR_INVALID_ARG;
+    cudaStream_t s = m->ctx->stream;
+    const int L = m->length, B = m->batch;
+    const size_t n = m->positions();
+    const CnnLayout& Y = m->lay;
+    cudaError_t e = cnn_forward(m, y);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->grads, 0, sizeof(float) * Y.total, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->loss, 0, sizeof(double), s);
+    if (e == cudaSuccess) {
+        fg::cnn_output_kernel<<<fg::gridn(n), 256, 0, s>>>(y->d, m->d4, n, m->scale, tx->d, 1.f / (float)n, nullptr,
+                                                          m->g16, m->loss);
+        fg::count_launch();
+        e = cudaGetLastError();
+    }
+    float* G = m->grads;
+    // layer 4 (no activation): weights, bias, input gradient masked by out3 > 0
+    if (e == cudaSuccess) e = fg::conv_wgrad<fg::CW, fg::COUT4>(m->g16, m->act[3], G + Y.w[3], L, B, s);
+    if (e == cudaSuccess) {
+        fg::bias_grad_kernel<fg::COUT4><<<fg::gridn(n), 256, 0, s>>>(m->g16, n, G + Y.b[3]);
+        fg::count_launch();
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = fg::conv_fwd<fg::COUT4, fg::CW, false>(m->g16, m->wt[3], nullptr, m->g64a, L, B, 0, m->act[3], s);
+    // layers 3, 2 (64 -> 64)
+    bf16* g = m->g64a;
+    bf16* g2 = m->g64b;
+    for (int l = 2; l >= 1 && e == cudaSuccess; --l) {
+        e = fg::conv_wgrad<fg::CW, fg::CW>(g, m->act[l], G + Y.w[l], L, B, s);
+        if (e == cudaSuccess) {
+            fg::bias_grad_kernel<fg::CW><<<fg::gridn(n), 256, 0, s>>>(g, n, G + Y.b[l]);
+            fg::count_launch();
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = fg::conv_fwd<fg::CW, fg::CW, false>(g, m->wt[l], nullptr, g2, L, B, 0, m->act[l], s);
+        std::swap(g, g2);
+    }
+    // layer 1: weights and bias only
+    if (e == cudaSuccess) e = fg::conv_wgrad<fg::CIN0, fg::CW>(g, m->act[0], G + Y.w[0], L, B, s);
+    if (e == cudaSuccess) {
+        fg::bias_grad_kernel<fg::CW><<<fg::gridn(n), 256, 0, s>>>(g, n, G + Y.b[0]);
+        fg::count_launch();
+        e = cudaGetLastError();
+    }
+    double h = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, m->loss, sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (loss) *loss = h;
+    return fg::cuda_check(m->ctx, e, "cnn loss/grad");
+}
+
+FOCSS_API focss_status focss_cnn_adam_step(focss_cnn* m, double lr, double beta1, double beta2, double eps) {
+    if (!m) return FOCSS_ERR_INVALID_ARG;
+    m->adam_t += 1;
+    const float c1 = (float)(1.0 / (1.0 - std::pow(beta1, m->adam_t)));
+    const float c2 = (float)(1.0 / (1.0 - std::pow(beta2, m->adam_t)));
+    const int n = (int)m->lay.total;
+    fg::cnn_adam_kernel<<<fg::gridn(n), 256, 0, m->ctx->stream>>>(m->params, m->grads, m->m1, m->m2, n, (float)lr,
+                                                                  (float)beta1, (float)beta2, (float)eps, c1, c2);
+    fg::count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cnn_refresh(m);
+    return fg::cuda_check(m->ctx, e, "cnn adam");
+}
+
+}  // extern "C"

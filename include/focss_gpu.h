@@ -283,6 +283,26 @@ FOCSS_API focss_status focss_ldbp_loss_grad(focss_ldbp* model, const focss_field
                                             double* loss);
 FOCSS_API focss_status focss_ldbp_adam_step(focss_ldbp* model, double lr, double beta1, double beta2, double eps);
 
+/* No reference counterpart: the convolutional correction stage after the
+ * learned DBP.  z = y + s (d_re + i d_im) with d = a 4-layer 1D CNN
+ * (64 channels, kernel 9, ReLU, zero padding) of x = [Re y/s, Im y/s];
+ * BF16 weights (FP32 masters), FP32 accumulation on the tensor cores.
+ * y, z, tx: fields of `length` symbols x `batch`, one mode.
+ * Parameters (float): per layer l = 1..4 W_l[cout][9][cin] then b_l[cout],
+ * with (cin, cout) = (16, 64), (64, 64), (64, 64), (64, 16); input channels
+ * 2..15 and output channels 2..15 are padding. */
+typedef struct focss_cnn focss_cnn;
+FOCSS_API focss_status focss_cnn_create(focss_ctx* ctx, int channels, int kernel, int length, int batch,
+                                        double input_scale, focss_cnn** out);
+FOCSS_API focss_status focss_cnn_destroy(focss_cnn* model);
+FOCSS_API int focss_cnn_num_params(const focss_cnn* model);
+FOCSS_API focss_status focss_cnn_set_params(focss_cnn* model, const float* params, int n);
+FOCSS_API focss_status focss_cnn_get_params(focss_cnn* model, float* params, float* grads, int n);
+FOCSS_API focss_status focss_cnn_forward(focss_cnn* model, const focss_field* y, focss_field* z);
+FOCSS_API focss_status focss_cnn_loss_grad(focss_cnn* model, const focss_field* y, const focss_field* tx,
+                                           double* loss);
+FOCSS_API focss_status focss_cnn_adam_step(focss_cnn* model, double lr, double beta1, double beta2, double eps);
+
 /* ------------------------------------------------- allocation-free SSFM */
 /* No counterpart in the reference.  The same computation as focss_ssfm_run
  * (SSFM::run on every realization) for callers that cannot let a library

@@ -1,0 +1,56 @@
+"""Correction CNN on the GPU (mma.sync BF16 implicit GEMMs): outputs, loss and
+gradients against the numpy restatement with the same BF16 rounding points
+(oracle/cnn_ref.py), and training on a structured distortion.  BF16 weights
+and activations: 1e-3 relative on outputs and loss, 1e-2 on gradients."""
+import numpy as np
+import pytest
+
+import focss_gb300 as fg
+from focss_gb300.cnn import CorrectionCNN, he_init
+from oracle import cnn_ref as R
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def fld(x, ctx):
+    return fg.Field(fg.Domain(1, x.shape[1], 1 / 32e9), data=x[:, None, :], batch=x.shape[0], ctx=ctx)
+
+
+def test_outputs_loss_and_gradients_match_reference(ctx):
+    rng = np.random.default_rng(2)
+    B, L, s = 2, 1000, 0.3
+    y = (rng.standard_normal((B, L)) + 1j * rng.standard_normal((B, L))) * s
+    tx = y + 0.05 * (rng.standard_normal((B, L)) + 1j * rng.standard_normal((B, L)))
+    y = y.astype(np.complex64).astype(complex)
+    tx = tx.astype(np.complex64).astype(complex)
+    p = he_init(rng, zero_last=False) * 0.5
+    net = CorrectionCNN(L, B, s, ctx=ctx)
+    net.set_params(p)
+    yf, tf = fld(y, ctx), fld(tx, ctx)
+    z = net.forward(yf).numpy()[:, 0]
+    loss = net.loss_grad(yf, tf)
+    _, g = net.get_params()
+    want_loss, want_g, want_z = R.loss_grad(p.astype(np.float64), y, tx, s)
+    assert rel_l2(z, want_z) < 1e-3
+    assert abs(loss - want_loss) < 1e-3 * want_loss
+    off = 0
+    for (cin, cout) in R.LAYERS:
+        n = cout * R.KW * cin + cout
+        assert rel_l2(g[off:off + n], want_g[off:off + n]) < 1e-2
+        off += n
+
+
+def test_training_learns_a_symbol_memory_distortion(ctx):
+    """y_k = t_k + 0.08 t_{k-1} |t_{k+1}|^2 (a triplet-like memory term):
+    the CNN trained on the GPU removes most of it."""
+    rng = np.random.default_rng(3)
+    B, L = 4, 4096
+    g = np.array([-3, -1, 1, 3]) / np.sqrt(10)
+    t = rng.choice(g, (B, L)) + 1j * rng.choice(g, (B, L))
+    y = t + 0.08 * np.roll(t, 1, axis=1) * np.abs(np.roll(t, -1, axis=1)) ** 2
+    net = CorrectionCNN(L, B, 1.0, ctx=ctx)
+    net.set_params(he_init(rng))
+    yf, tf = fld(y, ctx), fld(t, ctx)
+    hist = net.fit(yf, tf, iters=300, lr=2e-3)
+    assert hist[-1] < 0.2 * hist[0]
