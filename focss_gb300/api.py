@@ -187,6 +187,14 @@ class Field:
     def device_ptr(self):
         return lib().focss_field_device_ptr(self.h)
 
+    def copy_realizations(self, dst_first: int, src: "Field", src_first: int, count: int):
+        check(lib().focss_field_copy_realizations(self.h, dst_first, src.h, src_first, count), self.ctx.h)
+        return self
+
+    def slice(self, first: int, count: int) -> "Field":
+        out = Field(self.domain, batch=count, ctx=self.ctx)
+        return out.copy_realizations(0, self, first, count)
+
     # src/focss/field.cpp:381-391
     def __imul__(self, s):
         s = complex(s)

@@ -290,6 +290,19 @@ FOCSS_API focss_status focss_field_copy(focss_field* dst, const focss_field* src
                           "copy");
 }
 
+FOCSS_API focss_status focss_field_copy_realizations(focss_field* dst, int dst_first, const focss_field* src,
+                                                     int src_first, int count) {
+    if (!dst || !src || count < 0 || dst_first < 0 || src_first < 0) return FOCSS_ERR_INVALID_ARG;
+    if (dst->modes != src->modes || dst->samples != src->samples || dst_first + count > dst->batch ||
+        src_first + count > src->batch)
+        return fg::set_error(dst->ctx, FOCSS_ERR_INVALID_ARG, "copy_realizations: shapes");
+    const size_t per = (size_t)src->modes * src->samples;
+    return fg::cuda_check(dst->ctx,
+                          cudaMemcpyAsync(dst->d + per * dst_first, src->d + per * src_first,
+                                          sizeof(float2) * per * count, cudaMemcpyDeviceToDevice, dst->ctx->stream),
+                          "copy_realizations");
+}
+
 FOCSS_API focss_status focss_field_scale(focss_field* f, double re, double im) {
     if (!f) return FOCSS_ERR_INVALID_ARG;
     return fg::cuda_check(f->ctx, fg::launch_scale(f->d, f->n(), make_float2((float)re, (float)im), f->ctx->stream),

@@ -1,0 +1,153 @@
+"""End-to-end link helpers on the GPU: WDM 16QAM transmitter, amplified SSMF
+propagation, centre-channel receiver, plain DBP and learned DBP scoring.
+
+These follow the reference's experiment drivers (src/tasks/wdm_run.cpp:79-155,
+src/tasks/sp_run.cpp:10-53, src/tasks/systems.cpp) with the benchmark
+configurations' parameters; every step is a call into libfocss_gpu.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import dsp
+from .api import (Amplifier, Domain, Fiber, Field, SSFM, backward_propagation, db_to_linear, db_to_natural,
+                  dbm_to_watts, disp_to_beta2)
+
+LIGHT_SPEED = 299792458.0
+
+
+@dataclass
+class Link:
+    spans: int = 20
+    span_m: float = 80e3
+    alpha_db_km: float = 0.2
+    dispersion: float = 17e-6     # s/m^2 (17 ps/nm/km)
+    gamma: float = 1.3e-3         # 1/W/m
+    wavelength: float = 1.55e-6
+    noise_figure_db: float = 5.0
+    max_phase: float = 0.005
+    max_step: float = 1000.0
+    baud: float = 32e9
+    channels: int = 5
+    spacing: float = 50e9
+    osf: int = 16
+    roll_off: float = 0.1
+
+    def fiber(self):
+        return Fiber(db_to_natural(self.alpha_db_km * 1e-3), disp_to_beta2(self.dispersion, self.wavelength),
+                     self.gamma, self.span_m, self.wavelength, 1.0)
+
+    def gain(self):
+        return db_to_linear(self.alpha_db_km * self.span_m / 1e3)
+
+    def f0(self):
+        return LIGHT_SPEED / self.wavelength
+
+
+def wdm_transmitter(link: Link, n_symbols, batch, power_dbm, seed, ctx=None):
+    """Per realization: `channels` independent 16QAM sequences, RRC shaped at
+    `osf` samples/symbol and multiplexed (wdm_run.cpp:89-100).  Returns the
+    field (batch realizations) and the centre channel's symbols."""
+    p = np.sqrt(dbm_to_watts(power_dbm))
+    rng = np.random.default_rng(seed)
+    codes = rng.integers(0, 16, (batch * link.channels, 1, n_symbols))
+    sym = dsp.qam16_map(codes, Domain(1, n_symbols, 1 / link.baud), batch=batch * link.channels, ctx=ctx)
+    sym *= p
+    shaped = dsp.rrc_shaping(sym, link.osf, link.roll_off)
+    dt = shaped.domain.time_step
+    n = shaped.domain.samples
+    out = Field(Domain(1, n, dt, link.f0()), batch=batch, ctx=ctx)
+    for b in range(batch):
+        mux = dsp.wdm_mux(shaped.slice(b * link.channels, link.channels), link.spacing)
+        out.copy_realizations(b, mux, 0, 1)
+    centre = codes.reshape(batch, link.channels, n_symbols)[:, link.channels // 2]
+    tx = dsp.qam16_map(centre[:, None, :], Domain(1, n_symbols, 1 / link.baud), batch=batch, ctx=ctx)
+    tx *= p
+    return out, tx
+
+
+def propagate(link: Link, field: Field, seed=1):
+    """forward_propagation (systems.cpp:39-56) with ADAPTIVE steps and ASE; returns total steps."""
+    s = SSFM(link.fiber())
+    s.set_grid(SSFM.ADAPTIVE)
+    s.set_maximum_phase_shift(link.max_phase)
+    s.set_maximum_step_size(link.max_step)
+    amp = Amplifier(link.gain(), db_to_linear(link.noise_figure_db), seed=seed)
+    steps = 0
+    for i in range(link.spans):
+        steps += int(s.run(field).sum())
+        amp.amplify(field, counter=i)
+    return steps
+
+
+def centre_channel(link: Link, field: Field, dbp_osf=2):
+    """wdm_select(centre) then decimate to dbp_osf samples/symbol (wdm_run.cpp:33-35)."""
+    sel = dsp.wdm_select(field, 0, link.spacing)
+    return dsp.decimate(sel, link.osf // dbp_osf)
+
+
+def _timed(fn, ctx, repeat=3):
+    fn()
+    ctx.sync()
+    t0 = time.perf_counter()
+    for _ in range(repeat):
+        out = fn()
+    ctx.sync()
+    return out, (time.perf_counter() - t0) * 1e3 / repeat
+
+
+def learned_dbp(link: Link, rx_train: Field, tx_train: Field, rx_test: Field, tx_test: Field, steps_per_span=2,
+                taps=63, mf_taps=63, iters=300, lr=2e-3, cnn_iters=300, cnn_lr=2e-3, cut=100, angle_steps=720,
+                seed=0):
+    """Train the learned DBP (initialised from split-step DBP) and then the
+    correction CNN on (rx_train, tx_train); score both on the independent
+    (rx_test, tx_test).  Returns a dict of Q per realization and GPU times."""
+    from .cnn import CorrectionCNN, he_init
+    from .ldbp import LearnedDBP, matched_filter_taps
+    ctx = rx_train.ctx
+    B = rx_train.batch
+    n2 = rx_train.domain.samples
+    ns = tx_train.domain.samples
+    fib = link.fiber()
+    model = LearnedDBP(link.spans, steps_per_span, taps, mf_taps, n2, B, 1 / np.sqrt(link.gain()), ctx=ctx)
+    model.init_from_dbp(fib.alpha, fib.beta2, fib.gamma, fib.kappa, link.span_m, rx_train.domain.time_step,
+                        matched_filter_taps(ns, n2 // ns, link.roll_off, mf_taps, ctx=ctx))
+    pse = dsp.PhaseShiftEqualizer(angle_steps)
+    q_init = dsp.q2_factor(tx_test, pse.train_equalize(tx_test, model.forward(rx_test)), cut)
+    t0 = time.perf_counter()
+    hist = model.fit(rx_train, tx_train, iters=iters, lr=lr)
+    ctx.sync()
+    train_s = time.perf_counter() - t0
+    y_test, ms = _timed(lambda: model.forward(rx_test), ctx)
+    q_ldbp = dsp.q2_factor(tx_test, pse.train_equalize(tx_test, y_test), cut)
+    y_train = model.forward(rx_train)
+    p_rms = float(np.sqrt(np.mean(np.abs(tx_train.numpy(np.complex64)) ** 2)))
+    net = CorrectionCNN(ns, B, p_rms, ctx=ctx)
+    net.set_params(he_init(np.random.default_rng(seed)))
+    t0 = time.perf_counter()
+    chist = net.fit(y_train, tx_train, iters=cnn_iters, lr=cnn_lr)
+    ctx.sync()
+    cnn_train_s = time.perf_counter() - t0
+    z_test, ms_cnn = _timed(lambda: net.forward(y_test), ctx)
+    q_cnn = dsp.q2_factor(tx_test, pse.train_equalize(tx_test, z_test), cut)
+    return {"q_init": q_init, "q_learned": q_ldbp, "q_learned_cnn": q_cnn, "ms_learned": ms,
+            "ms_learned_cnn": ms + ms_cnn, "loss_first": hist[0], "loss_last": hist[-1],
+            "cnn_loss_first": chist[0], "cnn_loss_last": chist[-1], "train_s": train_s, "cnn_train_s": cnn_train_s}
+
+
+def plain_dbp_q(link: Link, rx2: Field, tx: Field, steps_per_span, cut=100, angle_steps=720):
+    """backward_propagation with UNIFORM steps (systems.cpp:86-103), matched
+    filter, phase-shift equalizer, Q per realization and the DBP GPU time."""
+    f = rx2.copy()
+    s = SSFM(link.fiber(), steps_per_span)
+    f.ctx.sync()
+    t0 = time.perf_counter()
+    backward_propagation(f, link.fiber(), s, link.gain(), link.spans)
+    f.ctx.sync()
+    ms = (time.perf_counter() - t0) * 1e3
+    sym = dsp.rrc_sampling(f, rx2.domain.samples // tx.domain.samples, link.roll_off)
+    eq = dsp.PhaseShiftEqualizer(angle_steps).train_equalize(tx, sym)
+    return dsp.q2_factor(tx, eq, cut), ms

@@ -117,6 +117,10 @@ FOCSS_API focss_status focss_field_upload_c64(focss_field* field, const float* i
 FOCSS_API focss_status focss_field_download_c64(focss_field* field, float* interleaved, size_t n_complex);
 /* Field::operator=(const Field&) (src/focss/field.cpp:87-105); same shape. */
 FOCSS_API focss_status focss_field_copy(focss_field* dst, const focss_field* src);
+/* Copy `count` realizations src[src_first ...] to dst[dst_first ...] (same
+ * modes and samples): Field copies (src/focss/field.cpp:56-68) of batch slices. */
+FOCSS_API focss_status focss_field_copy_realizations(focss_field* dst, int dst_first, const focss_field* src,
+                                                     int src_first, int count);
 /* Device pointer to the complex64 data (for interop); valid until destroy. */
 FOCSS_API void* focss_field_device_ptr(focss_field* field);
 /* Field::operator*=(const complex_t&) (src/focss/field.cpp:387-391). */
