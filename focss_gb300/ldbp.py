@@ -18,17 +18,33 @@ from .api import Context, Field
 P = C.c_void_p
 
 
-def dispersion_taps(length, alpha, beta2, dt, n_fft, taps):
-    """Truncated impulse response of one backward step of `length` metres:
-    H(w) = exp(+alpha L/2) exp(-i beta2/2 L w^2) (the sign of a BACKWARD
-    linear step, src/focss/solver/ssfm.cpp:142-150 with step < 0), laid out for
-    FIR(x, h)[n] = sum_t h[t] x[n + t - c]."""
-    w = 2 * np.pi * np.fft.fftfreq(n_fft, dt)
-    H = np.exp(0.5 * alpha * length) * np.exp(-0.5j * beta2 * length * w ** 2)
-    g = np.fft.fft(H) / n_fft  # h[c + d] = fft(H)[d] / N
+def taps_from_response(H, taps):
+    """Truncated FIR taps (layout FIR(x, h)[n] = sum_t h[t] x[n + t - c]) of a
+    circular filter with frequency response H (numpy FFT bin order)."""
+    n = H.size
+    g = np.fft.fft(H) / n  # h[c + d] = fft(H)[d] / N
     c = (taps - 1) // 2
     d = np.arange(-c, c + 1)
-    return g[d % n_fft]
+    return g[d % n]
+
+
+def dispersion_response(length, alpha, beta2, dt, n_fft):
+    """A BACKWARD linear step of `length` metres: exp(+alpha L/2) exp(-i beta2/2 L w^2)
+    (src/focss/solver/ssfm.cpp:142-150 with a negative step)."""
+    w = 2 * np.pi * np.fft.fftfreq(n_fft, dt)
+    return np.exp(0.5 * alpha * length) * np.exp(-0.5j * beta2 * length * w ** 2)
+
+
+def dispersion_taps(length, alpha, beta2, dt, n_fft, taps):
+    return taps_from_response(dispersion_response(length, alpha, beta2, dt, n_fft), taps)
+
+
+def rrc_response(n_symbols, osf, roll_off, ctx=None):
+    """Frequency response of rrc_sampling's circular filter (modulation.cpp:92-96,
+    field.cpp:358-372): FFT(ifftshift(pulse)) / N."""
+    from .dsp import rrc_pulse
+    p = rrc_pulse(n_symbols, osf, roll_off, ctx=ctx)
+    return np.fft.fft(np.fft.ifftshift(p)) / p.size
 
 
 def matched_filter_taps(n_symbols, osf, roll_off, taps, ctx=None):
@@ -86,15 +102,24 @@ class LearnedDBP:
         check(lib().focss_ldbp_get_params(self.h, p.ctypes.data_as(P), g.ctypes.data_as(P), p.size), self.ctx.h)
         return self.unpack(p), self.unpack(g)
 
-    def init_from_dbp(self, alpha, beta2, gamma, kappa, span_length, dt, mf_taps_values):
-        """Split-step DBP initialisation: each step = the backward linear
-        operator of span_length/steps (gain + dispersion) and a Kerr phase
-        -kappa gamma h (the raw-step Kerr of ssfm.cpp:160-164, reversed)."""
+    def init_from_dbp(self, alpha, beta2, gamma, kappa, span_length, dt, mf_response):
+        """Initialise as the reference's uniform split-step DBP
+        (ssfm.cpp:62-72 run BACKWARD per span after drop_power): per span
+        L(h/2) N(h) L(h) N(h) ... N(h) L(h/2), h = span/steps, Kerr phase
+        -kappa gamma h (raw step, ssfm.cpp:160-164).  The trailing L(h/2) of a
+        span and the leading L(h/2) of the next merge into one L(h) filter
+        (drop_power is a scalar between them); the last span's trailing
+        L(h/2) is folded into the matched filter, whose frequency response
+        `mf_response` (e.g. rrc_response) is given at the field's length."""
         hstep = span_length / self.steps
-        h1 = dispersion_taps(hstep, alpha, beta2, dt, self.samples, self.taps)
-        h = np.tile(h1, (self.layers, 1))
+        full = dispersion_taps(hstep, alpha, beta2, dt, self.samples, self.taps)
+        half = dispersion_taps(0.5 * hstep, alpha, beta2, dt, self.samples, self.taps)
+        h = np.tile(full, (self.layers, 1))
+        h[0] = half
         xi = np.full(self.layers, -kappa * gamma * hstep)
-        self.set_params(h, xi, mf_taps_values)
+        mf = taps_from_response(np.asarray(mf_response) *
+                                dispersion_response(0.5 * hstep, alpha, beta2, dt, self.samples), self.mf_taps)
+        self.set_params(h, xi, mf)
 
     def forward(self, field: Field) -> Field:
         from .api import Domain

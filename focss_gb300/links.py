@@ -106,7 +106,7 @@ def learned_dbp(link: Link, rx_train: Field, tx_train: Field, rx_test: Field, tx
     correction CNN on (rx_train, tx_train); score both on the independent
     (rx_test, tx_test).  Returns a dict of Q per realization and GPU times."""
     from .cnn import CorrectionCNN, he_init
-    from .ldbp import LearnedDBP, matched_filter_taps
+    from .ldbp import LearnedDBP, rrc_response
     ctx = rx_train.ctx
     B = rx_train.batch
     n2 = rx_train.domain.samples
@@ -114,7 +114,7 @@ def learned_dbp(link: Link, rx_train: Field, tx_train: Field, rx_test: Field, tx
     fib = link.fiber()
     model = LearnedDBP(link.spans, steps_per_span, taps, mf_taps, n2, B, 1 / np.sqrt(link.gain()), ctx=ctx)
     model.init_from_dbp(fib.alpha, fib.beta2, fib.gamma, fib.kappa, link.span_m, rx_train.domain.time_step,
-                        matched_filter_taps(ns, n2 // ns, link.roll_off, mf_taps, ctx=ctx))
+                        rrc_response(ns, n2 // ns, link.roll_off, ctx=ctx))
     pse = dsp.PhaseShiftEqualizer(angle_steps)
     q_init = dsp.q2_factor(tx_test, pse.train_equalize(tx_test, model.forward(rx_test)), cut)
     t0 = time.perf_counter()

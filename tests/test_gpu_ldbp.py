@@ -7,7 +7,7 @@ import pytest
 
 import focss_gb300 as fg
 from focss_gb300 import dsp
-from focss_gb300.ldbp import LearnedDBP, matched_filter_taps
+from focss_gb300.ldbp import LearnedDBP, rrc_response
 from oracle import ldbp_ref as R
 from conftest import ALPHA, BETA2, GAMMA, rel_l2
 
@@ -67,7 +67,7 @@ def test_training_on_ssfm_link_beats_its_dbp_initialisation(ctx):
     G = fg.db_to_linear(0.2 * 80)
     fg.forward_propagation(sig, fib, fg.SSFM(fib, 200), fg.Amplifier(G), spans)
     m = LearnedDBP(spans, 1, 41, 63, ns * osf, B, 1 / np.sqrt(G), ctx=ctx)
-    m.init_from_dbp(ALPHA, BETA2, GAMMA, 1.0, 80e3, dt, matched_filter_taps(ns, osf, 0.1, 63, ctx=ctx))
+    m.init_from_dbp(ALPHA, BETA2, GAMMA, 1.0, 80e3, dt, rrc_response(ns, osf, 0.1, ctx=ctx))
     q0 = dsp.q2_factor(sym, m.forward(sig), 100)
     hist = m.fit(sig, sym, iters=150, lr=2e-3)
     q1 = dsp.q2_factor(sym, m.forward(sig), 100)
