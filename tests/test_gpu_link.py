@@ -60,7 +60,7 @@ def test_single_channel_chain_matches_oracle(ctx, oracle_cpu):
 
 def test_learned_dbp_on_wdm_link(ctx):
     link = links.Link(spans=3)
-    ns, B = 1 << 12, 4
+    ns, B = 1 << 13, 8
     tx_train_f, tx_train = links.wdm_transmitter(link, ns, B, 3.0, seed=11, ctx=ctx)
     tx_test_f, tx_test = links.wdm_transmitter(link, ns, B, 3.0, seed=12, ctx=ctx)
     links.propagate(link, tx_train_f, seed=1)
@@ -69,8 +69,9 @@ def test_learned_dbp_on_wdm_link(ctx):
     rx_test = links.centre_channel(link, tx_test_f)
     q2_plain, ms2 = links.plain_dbp_q(link, rx_test, tx_test, 2)
     q50, ms50 = links.plain_dbp_q(link, rx_test, tx_test, 50)
-    r = links.learned_dbp(link, rx_train, tx_train, rx_test, tx_test, steps_per_span=2, taps=31, mf_taps=31,
-                          iters=200, lr=5e-4, cnn_iters=100)
+    # 40 km steps at 2 samples/symbol need ~63 taps (31 taps alone cap Q near 20 dB)
+    r = links.learned_dbp(link, rx_train, tx_train, rx_test, tx_test, steps_per_span=2, taps=63, mf_taps=63,
+                          iters=200, lr=3e-4, cnn_iters=100)
     # the split-step initialisation reproduces plain 2-step DBP
     assert abs(np.mean(r["q_init"]) - np.mean(q2_plain)) < 0.5
     assert r["loss_last"] < r["loss_first"]
