@@ -98,7 +98,7 @@ SIGNATURES = {
     "focss_ldbp_get_params": (I, [P, P, P, I]),
     "focss_ldbp_forward": (I, [P, P, P]),
     "focss_ldbp_loss_grad": (I, [P, P, P, P]),
-    "focss_ldbp_adam_step": (I, [P, D, D, D, D]),
+    "focss_ldbp_adam_step": (I, [P, D, D, D, D, D]),
     "focss_cnn_create": (I, [P, I, I, I, I, D, C.POINTER(P)]),
     "focss_cnn_destroy": (I, [P]),
     "focss_cnn_num_params": (I, [P]),

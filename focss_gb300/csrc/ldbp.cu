@@ -152,17 +152,19 @@ __global__ void mse_decimate_kernel(const float2* __restrict__ y, const float2* 
 }
 
 // Adam on n real parameters (complex parameters as interleaved pairs; the
-// real gradient of a complex z = a + ib is (2 Re g, 2 Im g)).
+// real gradient of a complex z = a + ib is (2 Re g, 2 Im g)).  Parameters in
+// [alt_lo, alt_hi) (the nonlinear gains) use the learning rate lr_alt.
 __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1,
                             float* __restrict__ m2, int n, float lr, float b1, float b2, float eps, float c1,
-                            float c2, float gscale) {
+                            float c2, float gscale, int alt_lo, int alt_hi, float lr_alt) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float gi = g[i] * gscale;
         const float a = b1 * m1[i] + (1.f - b1) * gi;
         const float v = b2 * m2[i] + (1.f - b2) * gi * gi;
         m1[i] = a;
         m2[i] = v;
-        p[i] -= lr * (a * c1) / (sqrtf(v * c2) + eps);
+        const float r = (i >= alt_lo && i < alt_hi) ? lr_alt : lr;
+        p[i] -= r * (a * c1) / (sqrtf(v * c2) + eps);
     }
 }
 
@@ -400,16 +402,18 @@ FOCSS_API focss_status focss_ldbp_loss_grad(focss_ldbp* m, const focss_field* in
     return ldbp_err(m->ctx, e, "ldbp loss/grad");
 }
 
-FOCSS_API focss_status focss_ldbp_adam_step(focss_ldbp* m, double lr, double beta1, double beta2, double eps) {
+FOCSS_API focss_status focss_ldbp_adam_step(focss_ldbp* m, double lr, double lr_gain, double beta1, double beta2,
+                                            double eps) {
     if (!m) return FOCSS_ERR_INVALID_ARG;
     m->adam_t += 1;
     const float c1 = (float)(1.0 / (1.0 - std::pow(beta1, m->adam_t)));
     const float c2 = (float)(1.0 / (1.0 - std::pow(beta2, m->adam_t)));
     // complex gradients g = dL/dconj(z) -> real gradient 2 g; xi gradients are already real:
     // the factor 2 is applied uniformly (Adam is invariant to gradient scale).
-    fg::adam_kernel<<<gridn(m->n_params), 256, 0, m->ctx->stream>>>(m->params, m->grads, m->m1, m->m2, m->n_params,
-                                                                    (float)lr, (float)beta1, (float)beta2, (float)eps,
-                                                                    c1, c2, 1.f);
+    const int xi_lo = m->spans * m->steps * m->taps * 2;
+    fg::adam_kernel<<<gridn(m->n_params), 256, 0, m->ctx->stream>>>(
+        m->params, m->grads, m->m1, m->m2, m->n_params, (float)lr, (float)beta1, (float)beta2, (float)eps, c1, c2,
+        1.f, xi_lo, xi_lo + m->spans * m->steps, (float)lr_gain);
     count_launch();
     return ldbp_err(m->ctx, cudaGetLastError(), "ldbp adam");
 }

@@ -117,6 +117,7 @@ class LearnedDBP:
         h = np.tile(full, (self.layers, 1))
         h[0] = half
         xi = np.full(self.layers, -kappa * gamma * hstep)
+        self.gain_scale = abs(kappa * gamma * hstep)
         mf = taps_from_response(np.asarray(mf_response) *
                                 dispersion_response(0.5 * hstep, alpha, beta2, dt, self.samples), self.mf_taps)
         self.set_params(h, xi, mf)
@@ -133,8 +134,19 @@ class LearnedDBP:
         check(lib().focss_ldbp_loss_grad(self.h, field.h, tx.h, C.byref(loss)), self.ctx.h)
         return loss.value
 
-    def adam_step(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
-        check(lib().focss_ldbp_adam_step(self.h, lr, beta1, beta2, eps), self.ctx.h)
+    def adam_step(self, lr=1e-3, lr_gain=None, beta1=0.9, beta2=0.999, eps=1e-8):
+        """Adam; the nonlinear gains move with lr_gain (default: lr times the
+        magnitude of the initial gains, so both parameter groups move by the
+        same relative amount per step)."""
+        if lr_gain is None:
+            lr_gain = lr * getattr(self, "gain_scale", 1.0)
+        check(lib().focss_ldbp_adam_step(self.h, lr, lr_gain, beta1, beta2, eps), self.ctx.h)
+
+    def rotate_output(self, angle):
+        """Multiply the matched filter by exp(i angle) (absorbs a constant
+        phase, e.g. the phase-shift equalizer angle of the training data)."""
+        (h, xi, hmf), _ = self.get_params()
+        self.set_params(h, xi, hmf * np.exp(1j * angle))
 
     def fit(self, field: Field, tx: Field, iters=100, lr=1e-3, log=None):
         hist = []

@@ -116,6 +116,12 @@ def learned_dbp(link: Link, rx_train: Field, tx_train: Field, rx_test: Field, tx
     model.init_from_dbp(fib.alpha, fib.beta2, fib.gamma, fib.kappa, link.span_m, rx_train.domain.time_step,
                         rrc_response(ns, n2 // ns, link.roll_off, ctx=ctx))
     pse = dsp.PhaseShiftEqualizer(angle_steps)
+    # The reference equalizes the DBP output's constant phase (mostly the mean
+    # cross-phase modulation of the neighbour channels) with the phase-shift
+    # equalizer; fold the training set's angle into the matched filter so
+    # that training starts from the equalized DBP.
+    ang = pse.estimate(tx_train, model.forward(rx_train))
+    model.rotate_output(float(np.angle(np.mean(np.exp(1j * ang)))))
     q_init = dsp.q2_factor(tx_test, pse.train_equalize(tx_test, model.forward(rx_test)), cut)
     t0 = time.perf_counter()
     hist = model.fit(rx_train, tx_train, iters=iters, lr=lr)

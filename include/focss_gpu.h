@@ -285,7 +285,10 @@ FOCSS_API focss_status focss_ldbp_get_params(focss_ldbp* model, float* params, f
 FOCSS_API focss_status focss_ldbp_forward(focss_ldbp* model, const focss_field* in, focss_field* symbols);
 FOCSS_API focss_status focss_ldbp_loss_grad(focss_ldbp* model, const focss_field* in, const focss_field* tx,
                                             double* loss);
-FOCSS_API focss_status focss_ldbp_adam_step(focss_ldbp* model, double lr, double beta1, double beta2, double eps);
+/* Adam step; `lr` for the filter taps, `lr_gain` for the nonlinear gains
+ * (their scale, kappa*gamma*h ~ 10^1 /W, differs from the taps' ~ 10^-1). */
+FOCSS_API focss_status focss_ldbp_adam_step(focss_ldbp* model, double lr, double lr_gain, double beta1,
+                                            double beta2, double eps);
 
 /* No reference counterpart: the convolutional correction stage after the
  * learned DBP.  z = y + s (d_re + i d_im) with d = a 4-layer 1D CNN
