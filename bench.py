@@ -365,6 +365,8 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "clocks": clk,
     }
+    if not args.no_dbp:
+        line["dbp"] = dbp_section(fg, ctx)
     if world == 1 and rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, t = cpu_sample(threads, 12)
@@ -376,6 +378,34 @@ def run_ours(args):
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def dbp_section(fg, ctx, power_dbm=2.0, batch=8):
+    """Q (dB) per DBP GPU time, learned vs plain, on the same link: the centre
+    channel at `power_dbm` per channel, 2 samples/symbol, independent train
+    and test sets of `batch` realizations each (fresh symbols and ASE)."""
+    from focss_gb300 import links
+    link = links.Link(spans=W["spans"], span_m=W["span_m"], noise_figure_db=W["noise_figure_db"],
+                      max_phase=W["max_phase_shift"], max_step=W["max_step_m"], channels=W["channels"],
+                      spacing=W["spacing_hz"], osf=W["samples_per_symbol"], roll_off=W["roll_off"])
+    ns = W["symbols_per_channel"]
+    a, ta = links.wdm_transmitter(link, ns, batch, power_dbm, seed=101, ctx=ctx)
+    b, tb = links.wdm_transmitter(link, ns, batch, power_dbm, seed=202, ctx=ctx)
+    links.propagate(link, a, seed=11)
+    links.propagate(link, b, seed=22)
+    ra, rb = links.centre_channel(link, a), links.centre_channel(link, b)
+    out = {"power_dbm_per_channel": power_dbm, "test_realizations": batch, "symbols_per_realization": ns,
+           "samples_per_symbol": 2, "plain": {}}
+    for k in (1, 2, 4, 100):
+        q, ms = links.plain_dbp_q(link, rb, tb, k)
+        out["plain"]["%d_steps_per_span" % k] = {"q_db": float(np.mean(q)), "ms": ms}
+    r = links.learned_dbp(link, ra, ta, rb, tb, steps_per_span=2, taps=63, mf_taps=63, iters=300, lr=3e-4,
+                          cnn_iters=300, cnn_lr=1e-3)
+    out["learned_2_steps_per_span"] = {"q_db": float(np.mean(r["q_learned"])), "ms": r["ms_learned"],
+                                       "q_db_at_init": float(np.mean(r["q_init"])), "train_s": r["train_s"]}
+    out["learned_2_steps_per_span_cnn"] = {"q_db": float(np.mean(r["q_learned_cnn"])), "ms": r["ms_learned_cnn"],
+                                           "train_s": r["cnn_train_s"]}
+    return out
 
 
 def run_ncu_case(args):
@@ -403,6 +433,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-dbp", action="store_true", help="skip the learned-vs-plain DBP section")
     args = ap.parse_args()
     if args.ncu_case:
         return run_ncu_case(args)
