@@ -1,0 +1,663 @@
+/* focss_gpu.hpp -- C++ facade over the C ABI in focss_gpu.h.
+ *
+ * Mirrors the reference's C++ API for the split-step path with the same class
+ * and function names in namespace focss:
+ *   Domain, Field                    src/focss/field.h:20-162
+ *   Fiber                            src/focss/module/fiber.h:5-21
+ *   SSFM                             src/focss/solver/ssfm.h:8-54
+ *   Amplifier                        src/focss/module/amplifier.h:7-22
+ *   q2/evm2, dB helpers              src/focss/functions.h
+ *   pulse::rrc, rrc_shaping/sampling, decisions, BER/SER, WDM helpers
+ *                                    src/focss/processing/modulation.h:8-45
+ *   PhaseShiftEqualizer, ScalarEqualizer
+ *                                    src/focss/equalizer/linear.h
+ * so that callers such as src/tasks/systems.cpp compile against it unchanged
+ * (include/focss_compat/ maps the reference's header names onto this file).
+ *
+ * Differences from the reference, all forced by device residency:
+ *  - A Field lives in GPU memory (complex64).  Element access (operator[],
+ *    operator()) goes through a host mirror that is filled on demand and
+ *    written back before the next device operation; a reference returned by
+ *    the non-const accessors is valid until that operation.
+ *  - A Field may hold a batch of independent realizations (extra `batch`
+ *    argument, default 1); every operation applies to all of them.  Scalar
+ *    results (powers, Q, BER, angles) refer to realization 0; the *_each
+ *    variants return one value per realization.
+ *  - Errors throw focss::gpu_error (the reference only asserts).
+ *  - ASE noise comes from a counter-based generator: the process-wide seed
+ *    (reseed_global_urng / set_global_seed) plus a call counter, so every
+ *    add_noise call draws fresh noise as the reference's global engine does.
+ *  - rrc_shaping / rrc_sampling keep the reference's fixed roll-off 0.01
+ *    (modulation.cpp:85); overloads take the roll-off explicitly.
+ * Header only; link with libfocss_gpu.so.
+ */
+#ifndef FOCSS_GPU_HPP_
+#define FOCSS_GPU_HPP_
+
+#include <atomic>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstdlib>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "focss_gpu.h"
+
+namespace focss {
+
+typedef double real_t;
+typedef std::complex<real_t> complex_t;
+template <typename T>
+using Vector = std::vector<T>;
+typedef Vector<real_t> RealVector;
+typedef Vector<complex_t> ComplexVector;
+
+const real_t math_pi = 3.14159265358979323846264338;
+const real_t planck = 6.62607004081818181818181e-34;  // [m^2 kg / s]
+const real_t light_speed = 299792458;                 // [m / s]
+const complex_t i_unit = complex_t(0, 1);
+
+/* Error raised for any non-OK status of the C ABI. */
+class gpu_error : public std::runtime_error {
+  public:
+    gpu_error(int status, const std::string& what) : std::runtime_error(what), status_(status) {}
+    int status() const { return status_; }
+
+  private:
+    int status_;
+};
+
+namespace detail {
+inline void check(focss_status s, const focss_ctx* ctx = nullptr) {
+    if (s == FOCSS_OK) return;
+    std::string msg = std::string("focss: ") + focss_status_string(s);
+    if (ctx) {
+        const char* e = focss_ctx_last_error(ctx);
+        if (e && *e) msg += std::string(": ") + e;
+    }
+    throw gpu_error(s, msg);
+}
+struct ContextHolder {
+    focss_ctx* ctx = nullptr;
+    ~ContextHolder() {
+        if (ctx) focss_ctx_destroy(ctx);
+    }
+};
+inline std::atomic<std::uint64_t>& urng_seed() {
+    static std::atomic<std::uint64_t> s{0x5eed0f0c55ull};
+    return s;
+}
+inline std::atomic<std::uint64_t>& urng_counter() {
+    static std::atomic<std::uint64_t> c{0};
+    return c;
+}
+}  // namespace detail
+
+/* The calling thread's device context (one stream per host thread).  The
+ * device is FOCSS_DEVICE from the environment, else 0. */
+inline focss_ctx* gpu_context() {
+    static thread_local detail::ContextHolder h;
+    if (!h.ctx) {
+        int dev = 0;
+        if (const char* e = std::getenv("FOCSS_DEVICE")) dev = std::atoi(e);
+        detail::check(focss_ctx_create(dev, &h.ctx));
+    }
+    return h.ctx;
+}
+inline void gpu_sync() { detail::check(focss_ctx_sync(gpu_context()), gpu_context()); }
+
+/* ------------------------------------------------------------- functions */
+/* src/focss/functions.cpp:11-25: the ASE generator's seed. */
+inline void set_global_seed(std::uint64_t seed) {
+    detail::urng_seed() = seed;
+    detail::urng_counter() = 0;
+}
+inline void reseed_global_urng() {
+    std::random_device rd;
+    set_global_seed(((std::uint64_t)rd() << 32) ^ (std::uint64_t)rd());
+}
+inline void setup() { reseed_global_urng(); }
+
+/* src/focss/functions.cpp:82-105 */
+inline double db_to_linear(const double& db_value) { return std::pow(10, db_value / 10); }
+inline double dbm_to_watts(const double& dbm_power) { return 1e-3 * std::pow(10, dbm_power / 10); }
+inline double db_to_natural(const double& db_value) { return db_value * std::log(10) / 10; }
+inline double disp_to_beta2(const double& dispersion, const double& wavelength) {
+    return -wavelength * wavelength * dispersion / (2 * math_pi * light_speed);
+}
+inline double sinc(const double& x) { return x == 0 ? 1 : std::sin(math_pi * x) / math_pi / x; }
+inline complex_t i_exp(const double& x) { return complex_t(std::cos(x), std::sin(x)); }
+
+/* ---------------------------------------------------------------- Domain */
+struct Domain {
+    int modes;
+    int samples;
+    real_t time_step;
+    real_t center_frequency;
+    inline int size() const { return modes * samples; }
+    inline bool operator==(const Domain& o) const {
+        return modes == o.modes && samples == o.samples && time_step == o.time_step &&
+               center_frequency == o.center_frequency;
+    }
+};
+
+/* ----------------------------------------------------------------- Field */
+class Field {
+  public:
+    Field() : h_(nullptr), dom_{0, 0, 0, 0}, batch_(0), where_(DEVICE) {}
+    explicit Field(const Domain& domain, int batch = 1) : dom_(domain), batch_(batch), where_(DEVICE) {
+        create();
+    }
+    /* data: batch * modes * samples values, realization-major then mode-major. */
+    Field(const Domain& domain, const ComplexVector& data) : dom_(domain), where_(DEVICE) {
+        const size_t n = (size_t)domain.size();
+        if (n == 0 || data.size() % n) throw gpu_error(FOCSS_ERR_INVALID_ARG, "focss: data size is not a multiple of the domain size");
+        batch_ = (int)(data.size() / n);
+        create();
+        host_ = data;
+        where_ = HOST;
+    }
+    Field(const Field& o) : dom_(o.dom_), batch_(o.batch_), where_(DEVICE) {
+        h_ = nullptr;
+        if (!o.h_) return;
+        create();
+        o.push();
+        detail::check(focss_field_copy(h_, o.h_), gpu_context());
+    }
+    Field(Field&& o) noexcept : h_(o.h_), dom_(o.dom_), batch_(o.batch_), host_(std::move(o.host_)), where_(o.where_) {
+        o.h_ = nullptr;
+        o.batch_ = 0;
+    }
+    Field& operator=(const Field& o) {
+        if (this == &o) return *this;
+        Field t(o);
+        swap(t);
+        return *this;
+    }
+    Field& operator=(Field&& o) noexcept {
+        swap(o);
+        return *this;
+    }
+    ~Field() {
+        if (h_) focss_field_destroy(h_);
+    }
+    void swap(Field& o) noexcept {
+        std::swap(h_, o.h_);
+        std::swap(dom_, o.dom_);
+        std::swap(batch_, o.batch_);
+        host_.swap(o.host_);
+        std::swap(where_, o.where_);
+    }
+
+    /* ---- element access through the host mirror (field.cpp:135-159) */
+    complex_t operator[](const int& index) const { return pull()[(size_t)index]; }
+    complex_t& operator[](const int& index) { return pull_mut()[(size_t)index]; }
+    complex_t operator()(const int& mode, const int& sample) const {
+        return pull()[(size_t)mode * dom_.samples + sample];
+    }
+    complex_t& operator()(const int& mode, const int& sample) {
+        return pull_mut()[(size_t)mode * dom_.samples + sample];
+    }
+    ComplexVector operator()(const int& mode) const {
+        const ComplexVector& h = pull();
+        return ComplexVector(h.begin() + (size_t)mode * dom_.samples, h.begin() + (size_t)(mode + 1) * dom_.samples);
+    }
+    /* All realizations, realization-major. */
+    const ComplexVector& data() const { return pull(); }
+
+    /* ---- powers (field.cpp:164-195); realization 0, *_each per realization */
+    real_t power(const int& sample) const {
+        const ComplexVector& h = pull();
+        real_t p = 0;
+        for (int m = 0; m < dom_.modes; ++m) p += std::norm(h[(size_t)m * dom_.samples + sample]);
+        return p;
+    }
+    RealVector peak_power_each() const {
+        RealVector pk((size_t)batch_);
+        detail::check(focss_field_power(handle(), nullptr, pk.data()), gpu_context());
+        return pk;
+    }
+    RealVector average_power_each() const {
+        RealVector av((size_t)batch_);
+        detail::check(focss_field_power(handle(), av.data(), nullptr), gpu_context());
+        return av;
+    }
+    real_t peak_power() const { return peak_power_each()[0]; }
+    real_t average_power() const { return average_power_each()[0]; }
+    Field& peak_normalize(const real_t& p = 1) { return (*this) *= std::sqrt(p / peak_power()); }
+    Field& average_normalize(const real_t& p = 1) { return (*this) *= std::sqrt(p / average_power()); }
+
+    /* ---- shape and grids (field.cpp:199-266) */
+    int size() const { return dom_.size(); }
+    int modes() const { return dom_.modes; }
+    int samples() const { return dom_.samples; }
+    int batch() const { return batch_; }
+    real_t duration() const { return dom_.samples * dom_.time_step; }
+    real_t bandwidth() const { return 1.0 / dom_.time_step; }
+    real_t time_step() const { return dom_.time_step; }
+    real_t sampling_rate() const { return 1.0 / dom_.time_step; }
+    real_t center_frequency() const { return dom_.center_frequency; }
+    real_t dt() const { return dom_.time_step; }
+    real_t df() const { return 1.0 / (dom_.time_step * dom_.samples); }
+    real_t dw() const { return 2.0 * math_pi / (dom_.time_step * dom_.samples); }
+    real_t t(const int& sample) const { return static_cast<real_t>(sample) * dt(); }
+    real_t f(const int& sample) const { return dom_.center_frequency + (sample - dom_.samples / 2) * df(); }
+    real_t w(const int& sample) const { return 2 * math_pi * f(sample); }
+    Domain domain() const { return dom_; }
+    RealVector time_grid() const {
+        RealVector g((size_t)dom_.samples);
+        for (int s = 0; s < dom_.samples; ++s) g[(size_t)s] = t(s);
+        return g;
+    }
+    RealVector frequency_grid() const {
+        RealVector g((size_t)dom_.samples);
+        for (int s = 0; s < dom_.samples; ++s) g[(size_t)s] = f(s);
+        return g;
+    }
+    RealVector temporal_power() const {
+        RealVector p((size_t)dom_.samples);
+        for (int s = 0; s < dom_.samples; ++s) p[(size_t)s] = power(s);
+        return p;
+    }
+
+    /* ---- resampling (field.cpp:272-320) */
+    Field upsample(const int& factor) const {
+        Field out(Domain{dom_.modes, dom_.samples * factor, dom_.time_step / factor, dom_.center_frequency}, batch_);
+        detail::check(focss_upsample(gpu_context(), handle(), factor, out.h_), gpu_context());
+        return out;
+    }
+    Field downsample(const int& factor) const {
+        Field out(Domain{dom_.modes, dom_.samples / factor, dom_.time_step * factor, dom_.center_frequency}, batch_);
+        detail::check(focss_downsample(gpu_context(), handle(), factor, out.h_), gpu_context());
+        return out;
+    }
+    Field decimate(const int& factor) const {
+        Field out(Domain{dom_.modes, dom_.samples / factor, dom_.time_step * factor, dom_.center_frequency}, batch_);
+        detail::check(focss_decimate(gpu_context(), handle(), factor, out.h_), gpu_context());
+        return out;
+    }
+
+    /* ---- Fourier methods (field.cpp:343-372) */
+    Field& fft_inplace() {
+        detail::check(focss_field_fft(mut()), gpu_context());
+        return *this;
+    }
+    Field& ifft_inplace() {
+        detail::check(focss_field_ifft(mut()), gpu_context());
+        return *this;
+    }
+    Field fft() const { return Field(*this).fft_inplace(); }
+    Field ifft() const { return Field(*this).ifft_inplace(); }
+    Field& filter_inplace(const ComplexVector& impulse_response) {
+        detail::check(focss_filter(gpu_context(), mut(), reinterpret_cast<const double*>(impulse_response.data()),
+                                   (int)impulse_response.size()),
+                      gpu_context());
+        return *this;
+    }
+    Field filter(const ComplexVector& impulse_response) const { return Field(*this).filter_inplace(impulse_response); }
+
+    /* ---- scalar arithmetic (field.cpp:376-400) */
+    Field& operator*=(const real_t& a) { return (*this) *= complex_t(a, 0); }
+    Field& operator*=(const complex_t& a) {
+        detail::check(focss_field_scale(mut(), a.real(), a.imag()), gpu_context());
+        return *this;
+    }
+    Field& operator/=(const real_t& a) { return (*this) *= complex_t(1.0 / a, 0); }
+    Field& operator/=(const complex_t& a) { return (*this) *= (complex_t(1, 0) / a); }
+    friend Field operator*(const Field& f, const real_t& a) { return Field(f) *= a; }
+    friend Field operator*(const Field& f, const complex_t& a) { return Field(f) *= a; }
+    friend Field operator*(const real_t& a, const Field& f) { return Field(f) *= a; }
+    friend Field operator*(const complex_t& a, const Field& f) { return Field(f) *= a; }
+    friend Field operator/(const Field& f, const real_t& a) { return Field(f) /= a; }
+    friend Field operator/(const Field& f, const complex_t& a) { return Field(f) /= a; }
+
+    /* ---- batch helpers */
+    /* `count` realizations of `src` from src_first into this field from dst_first. */
+    void copy_realizations(int dst_first, const Field& src, int src_first, int count) {
+        detail::check(focss_field_copy_realizations(mut(), dst_first, src.handle(), src_first, count), gpu_context());
+    }
+
+    /* Device handle with host edits written back (read access). */
+    focss_field* handle() const {
+        push();
+        return h_;
+    }
+    /* Device handle for an operation that modifies the field. */
+    focss_field* mut() {
+        push();
+        where_ = DEVICE;
+        return h_;
+    }
+
+  private:
+    enum Where { DEVICE, HOST, BOTH };
+    void create() {
+        focss_domain d{dom_.modes, dom_.samples, dom_.time_step, dom_.center_frequency};
+        detail::check(focss_field_create(gpu_context(), &d, batch_, &h_), gpu_context());
+    }
+    size_t count() const { return (size_t)batch_ * (size_t)dom_.size(); }
+    void push() const {
+        if (where_ != HOST) return;
+        detail::check(focss_field_upload(h_, reinterpret_cast<const double*>(host_.data()), count()), gpu_context());
+        where_ = BOTH;
+    }
+    const ComplexVector& pull() const {
+        if (where_ == DEVICE) {
+            host_.resize(count());
+            detail::check(focss_field_download(h_, reinterpret_cast<double*>(host_.data()), count()), gpu_context());
+            where_ = BOTH;
+        }
+        return host_;
+    }
+    ComplexVector& pull_mut() {
+        pull();
+        where_ = HOST;
+        return host_;
+    }
+
+    focss_field* h_;
+    Domain dom_;
+    int batch_;
+    mutable ComplexVector host_;
+    mutable Where where_;
+};
+
+/* ----------------------------------------------------------------- Fiber */
+/* src/focss/module/fiber.cpp:4-45 */
+struct Fiber {
+    double alpha;
+    double beta2;
+    double gamma;
+    double length;
+    double wavelength;
+    double kappa;
+
+    Fiber linear() const {
+        Fiber f = *this;
+        f.gamma = 0;
+        return f;
+    }
+    Fiber nonlinear() const {
+        Fiber f = *this;
+        f.alpha = 0;
+        f.beta2 = 0;
+        return f;
+    }
+    Fiber dispersive() const {
+        Fiber f = *this;
+        f.alpha = 0;
+        f.gamma = 0;
+        return f;
+    }
+    Fiber operator-() const {
+        Fiber f = *this;
+        f.alpha = -alpha;
+        f.beta2 = -beta2;
+        f.gamma = -gamma;
+        return f;
+    }
+    Fiber operator*(const double& length_factor) const {
+        Fiber f = *this;
+        if (length_factor >= 0) {
+            f.length *= length_factor;
+        } else {
+            f.alpha = -alpha;
+            f.beta2 = -beta2;
+            f.gamma = -gamma;
+            f.length *= -length_factor;
+        }
+        return f;
+    }
+    focss_fiber c() const { return focss_fiber{alpha, beta2, gamma, length, wavelength, kappa}; }
+};
+
+/* ------------------------------------------------------------------ SSFM */
+/* src/focss/solver/ssfm.h:8-54.  The reference leaves the grid and limits
+ * uninitialised unless set (ssfm.cpp:17-22); here they default to UNIFORM,
+ * one step, 1e-3 rad and 1 km. */
+class SSFM {
+  public:
+    typedef const int Grid;
+    static constexpr int UNIFORM = FOCSS_UNIFORM;
+    static constexpr int LOGARITHMIC = FOCSS_LOGARITHMIC;
+    static constexpr int ADAPTIVE = FOCSS_ADAPTIVE;
+    typedef const double Direction;
+    static constexpr double FORWARD = FOCSS_FORWARD;
+    static constexpr double BACKWARD = FOCSS_BACKWARD;
+
+    SSFM() : fiber_{0, 0, 0, 0, 1.55e-6, 1}, opts_{FOCSS_UNIFORM, 1, 1e-3, 1e3} {}
+    SSFM(const Fiber& fiber) : fiber_(fiber), opts_{FOCSS_UNIFORM, 1, 1e-3, 1e3} {}
+    SSFM(const Fiber& fiber, const int& total_steps) : fiber_(fiber), opts_{FOCSS_UNIFORM, total_steps, 1e-3, 1e3} {}
+
+    void set_fiber(const Fiber& fiber) { fiber_ = fiber; }
+    void set_grid(const int& grid) { opts_.grid = grid; }
+    void set_total_steps(const int& total_steps) { opts_.total_steps = total_steps; }
+    void set_maximum_phase_shift(const double& v) { opts_.maximum_phase_shift = v; }
+    void set_maximum_step_size(const double& v) { opts_.maximum_step_size = v; }
+
+    /* Runs every realization of `field`; last_steps() gives the step counts. */
+    void run(Field& field, const double& direction = FORWARD) {
+        steps_.assign((size_t)field.batch(), 0);
+        focss_fiber f = fiber_.c();
+        detail::check(focss_ssfm_run(gpu_context(), field.mut(), &f, &opts_, direction, steps_.data()), gpu_context());
+    }
+    const Vector<int>& last_steps() const { return steps_; }
+
+  private:
+    Fiber fiber_;
+    focss_ssfm_opts opts_;
+    Vector<int> steps_;
+};
+
+/* ------------------------------------------------------------- Amplifier */
+/* src/focss/module/amplifier.cpp:8-47 */
+class Amplifier {
+  public:
+    Amplifier() : gain_(1), noise_factor_(0) {}
+    Amplifier(const double& gain) : gain_(gain), noise_factor_(0) {}
+    Amplifier(const double& gain, const double& noise_factor) : gain_(gain), noise_factor_(noise_factor) {}
+
+    void amplify(Field& field) const { apply(field, FOCSS_AMP_AMPLIFY); }
+    void add_noise(Field& field) const { apply(field, FOCSS_AMP_ADD_NOISE); }
+    void give_power(Field& field) const { apply(field, FOCSS_AMP_GIVE_POWER); }
+    void drop_power(Field& field) const { apply(field, FOCSS_AMP_DROP_POWER); }
+
+  private:
+    void apply(Field& field, int op) const {
+        const std::uint64_t counter = detail::urng_counter().fetch_add(1);
+        detail::check(focss_amplifier_apply(gpu_context(), field.mut(), gain_, noise_factor_, detail::urng_seed().load(),
+                                            counter, op),
+                      gpu_context());
+    }
+    double gain_;
+    double noise_factor_;
+};
+
+/* -------------------------------------------------------------- metrics */
+/* src/focss/functions.cpp:27-80 (FP64 sums on the device). */
+inline double q2_factor(const Field& tx, const Field& rx, const int& cut) {
+    Vector<double> q((size_t)tx.batch());
+    detail::check(focss_q2_factor(gpu_context(), tx.handle(), rx.handle(), cut, q.data()), gpu_context());
+    return q[0];
+}
+inline double q2_factor(const Field& tx, const Field& rx) { return q2_factor(tx, rx, -1); }
+inline double evm2_factor(const Field& tx, const Field& rx, const int& cut) {
+    return std::pow(10.0, -q2_factor(tx, rx, cut) / 10.0);
+}
+inline double evm2_factor(const Field& tx, const Field& rx) { return evm2_factor(tx, rx, -1); }
+inline Vector<double> q2_factor_each(const Field& tx, const Field& rx, int cut = -1) {
+    Vector<double> q((size_t)tx.batch());
+    detail::check(focss_q2_factor(gpu_context(), tx.handle(), rx.handle(), cut, q.data()), gpu_context());
+    return q;
+}
+
+/* ------------------------------------------------------------ modulation */
+namespace pulse {
+/* src/focss/processing/modulation.cpp:47-74, computed on the device in FP64. */
+inline ComplexVector rrc(const int& n_symbols, const int& oversampling, const double& roll_off) {
+    ComplexVector taps((size_t)n_symbols * oversampling);
+    detail::check(focss_rrc_pulse(gpu_context(), n_symbols, oversampling, roll_off, reinterpret_cast<double*>(taps.data())),
+                  gpu_context());
+    return taps;
+}
+}  // namespace pulse
+
+const double rrc_roll_off = 0.01;  // modulation.cpp:85
+
+/* Gray 16QAM points of codes (modulation.cpp:9-17); codes in field order. */
+inline Field qam16_symbols(const Vector<int>& codes, const Domain& domain) {
+    const int batch = domain.size() ? (int)(codes.size() / (size_t)domain.size()) : 0;
+    Field out(domain, batch);
+    Vector<std::int32_t> c(codes.begin(), codes.end());
+    detail::check(focss_qam16_map(gpu_context(), c.data(), c.size(), out.mut()), gpu_context());
+    return out;
+}
+
+/* modulation.cpp:86-90 / :92-96 */
+inline Field rrc_shaping(const Field& symbols, const int& osf, const double& gain, const double& roll_off) {
+    const Domain d = symbols.domain();
+    Field out(Domain{d.modes, d.samples * osf, d.time_step / osf, d.center_frequency}, symbols.batch());
+    detail::check(focss_rrc_shaping(gpu_context(), symbols.handle(), osf, roll_off, gain, out.mut()), gpu_context());
+    return out;
+}
+inline Field rrc_shaping(const Field& symbols, const int& osf, const double& gain = 1) {
+    return rrc_shaping(symbols, osf, gain, rrc_roll_off);
+}
+inline Field rrc_sampling(const Field& signal, const int& osf, const double& gain, const double& roll_off) {
+    const Domain d = signal.domain();
+    Field out(Domain{d.modes, d.samples / osf, d.time_step * osf, d.center_frequency}, signal.batch());
+    detail::check(focss_rrc_sampling(gpu_context(), signal.handle(), osf, roll_off, gain, out.mut()), gpu_context());
+    return out;
+}
+inline Field rrc_sampling(const Field& signal, const int& osf, const double& gain = 1) {
+    return rrc_sampling(signal, osf, gain, rrc_roll_off);
+}
+
+/* modulation.cpp:112-120, :148-156 */
+inline Field hard_decision_16qam(const Field& signal) {
+    Field out(signal.domain(), signal.batch());
+    detail::check(focss_hard_decision(gpu_context(), signal.handle(), out.mut()), gpu_context());
+    return out;
+}
+inline Vector<int> hd_sequence_16qam(const Field& signal) {
+    Vector<std::int32_t> c((size_t)signal.batch() * signal.size());
+    detail::check(focss_hd_codes(gpu_context(), signal.handle(), c.data()), gpu_context());
+    return Vector<int>(c.begin(), c.end());
+}
+
+/* modulation.cpp:158-223 */
+inline double bit_error_rate_16qam(const Field& tx, const Field& rx, const int& cut) {
+    Vector<double> v((size_t)tx.batch());
+    detail::check(focss_bit_error_rate(gpu_context(), tx.handle(), rx.handle(), cut, v.data()), gpu_context());
+    return v[0];
+}
+inline double bit_error_rate_16qam(const Field& tx, const Field& rx) { return bit_error_rate_16qam(tx, rx, -1); }
+inline double symbol_error_rate_16qam(const Field& tx, const Field& rx, const int& cut) {
+    Vector<double> v((size_t)tx.batch());
+    detail::check(focss_symbol_error_rate(gpu_context(), tx.handle(), rx.handle(), cut, v.data()), gpu_context());
+    return v[0];
+}
+
+/* modulation.cpp:225-277 */
+inline Field frequency_shift(const Field& field, const double& frequency) {
+    Field out(field);
+    detail::check(focss_frequency_shift(gpu_context(), out.mut(), frequency), gpu_context());
+    return out;
+}
+inline Field bandpass_filter(const Field& field, const double& frequency) {
+    Field out(field);
+    detail::check(focss_bandpass(gpu_context(), out.mut(), frequency), gpu_context());
+    return out;
+}
+inline Field wdm_select(const Field& field, const int& channel_index, const double& channel_bandwidth) {
+    Field out(field.domain(), field.batch());
+    detail::check(focss_wdm_select(gpu_context(), field.handle(), channel_index, channel_bandwidth, out.mut()),
+                  gpu_context());
+    return out;
+}
+inline Field wdm_mux(const Vector<Field>& channels, const double& channel_bandwidth) {
+    if (channels.empty()) throw gpu_error(FOCSS_ERR_INVALID_ARG, "focss: wdm_mux of no channels");
+    const Domain d = channels[0].domain();
+    Field stacked(d, (int)channels.size());
+    for (size_t c = 0; c < channels.size(); ++c) stacked.copy_realizations((int)c, channels[c], 0, 1);
+    Field out(d, 1);
+    detail::check(focss_wdm_mux(gpu_context(), stacked.handle(), channel_bandwidth, out.mut()), gpu_context());
+    return out;
+}
+inline Vector<Field> wdm_demux(const Field& field, const int& n_channels, const double& channel_bandwidth) {
+    Vector<Field> out;
+    for (int ch = 0; ch < n_channels; ++ch) out.push_back(wdm_select(field, ch - n_channels / 2, channel_bandwidth));
+    return out;
+}
+
+/* ------------------------------------------------------------ equalizers */
+/* src/focss/equalizer/phase_shift_equalizer.cpp:1-46 */
+class PhaseShiftEqualizer {
+  public:
+    PhaseShiftEqualizer() : angle_steps_(3600) {}
+    explicit PhaseShiftEqualizer(const int& angle_steps) : angle_steps_(angle_steps) {}
+    void set_angle_steps(const int& angle_steps) { angle_steps_ = angle_steps; }
+    void train(const Field& desired, const Field& actual) { angles_ = estimate(desired, actual); }
+    Field equalize(const Field& original) const {
+        Field out(original);
+        Vector<double> a = angles_;
+        a.resize((size_t)original.batch(), angles_.empty() ? 0.0 : angles_.back());
+        detail::check(focss_field_rotate(gpu_context(), out.mut(), a.data()), gpu_context());
+        return out;
+    }
+    Field train_equalize(const Field& desired, const Field& actual) const {
+        Field out(actual);
+        Vector<double> a = estimate(desired, actual);
+        detail::check(focss_field_rotate(gpu_context(), out.mut(), a.data()), gpu_context());
+        return out;
+    }
+    double get_angle() const { return angles_.empty() ? 0.0 : angles_[0]; }
+    const Vector<double>& get_angles() const { return angles_; }
+
+  private:
+    Vector<double> estimate(const Field& desired, const Field& actual) const {
+        Vector<double> a((size_t)actual.batch());
+        detail::check(focss_pse_estimate(gpu_context(), desired.handle(), actual.handle(), angle_steps_, a.data()),
+                      gpu_context());
+        return a;
+    }
+    int angle_steps_;
+    Vector<double> angles_;
+};
+
+/* src/focss/equalizer/scalar_equalizer.cpp:1-33 */
+class ScalarEqualizer {
+  public:
+    ScalarEqualizer() {}
+    void train(const Field& desired, const Field& actual) { scalars_ = estimate(desired, actual); }
+    Field equalize(const Field& original) const {
+        Field out(original);
+        Vector<double> s = scalars_;
+        s.resize(2 * (size_t)original.batch(), 0.0);
+        detail::check(focss_field_scale_each(gpu_context(), out.mut(), s.data()), gpu_context());
+        return out;
+    }
+    Field train_equalize(const Field& desired, const Field& actual) const {
+        Field out(actual);
+        Vector<double> s = estimate(desired, actual);
+        detail::check(focss_field_scale_each(gpu_context(), out.mut(), s.data()), gpu_context());
+        return out;
+    }
+    complex_t get_scalar() const { return scalars_.size() >= 2 ? complex_t(scalars_[0], scalars_[1]) : complex_t(1, 0); }
+
+  private:
+    Vector<double> estimate(const Field& desired, const Field& actual) const {
+        Vector<double> s(2 * (size_t)actual.batch());
+        detail::check(focss_scalar_estimate(gpu_context(), desired.handle(), actual.handle(), s.data()), gpu_context());
+        return s;
+    }
+    Vector<double> scalars_;
+};
+
+}  // namespace focss
+
+#endif  // FOCSS_GPU_HPP_
