@@ -375,6 +375,8 @@ def run_ours(args):
     }
     if not args.no_dbp:
         line["dbp"] = dbp_section(fg, ctx)
+    if not args.no_sweep:
+        line["sweep"] = sweep_section(fg, ctx, stream)
     if world == 1 and rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         n_steps = CPU_BASELINE_STEPS
@@ -418,6 +420,120 @@ def dbp_section(fg, ctx, power_dbm=2.0, batch=8):
     return out
 
 
+SWEEP = dict(
+    workload="sweep256_16qam_32GBd_2^12-2^16sym_8sps_15x80km_ssmf_ase_dbp_1-16stps",
+    realizations=256, log2_symbols=[12, 16], samples_per_symbol=8, dbp_samples_per_symbol=2,
+    powers_dbm=[-4.0, 4.0], spans=15, span_m=80e3, noise_figure_db=5.0, roll_off=0.1,
+    forward="ADAPTIVE, max 0.005 rad/step, max 1 km", dbp_steps_per_span=[1, 2, 4, 8, 16], seed=3,
+)
+
+
+def _stream_ms(torch, stream, fn):
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    out = fn()
+    e1.record(stream)
+    e1.synchronize()
+    return out, e0.elapsed_time(e1)
+
+
+def sweep_section(fg, ctx, stream):
+    """Batched sweep of independent single-channel realizations of uneven
+    lengths: 2^U 16QAM symbols, U uniform in {12..16}, launch powers uniform
+    in -4..+4 dBm, 8 samples/symbol, 15 x 80 km SSMF with ASE.  All lengths
+    are one span-loop graph launch for the forward propagation and one for
+    DBP at 1/2/4/8/16 steps per span (25 fields); the FFT split of every
+    length is picked by the autotuner first."""
+    import torch
+    from focss_gb300 import dsp
+    alpha, beta2, gamma = fiber_params()
+    sw = SWEEP
+    rng = np.random.default_rng(sw["seed"])
+    R = sw["realizations"]
+    U = rng.integers(sw["log2_symbols"][0], sw["log2_symbols"][1] + 1, R)
+    P = rng.uniform(sw["powers_dbm"][0], sw["powers_dbm"][1], R)
+    fib = fg.Fiber(alpha, beta2, gamma, sw["span_m"])
+    G = 10 ** (W["alpha_db_per_km"] * sw["span_m"] / 1e3 / 10)
+    NF = 10 ** (sw["noise_figure_db"] / 10)
+    osf, dosf, spans = sw["samples_per_symbol"], sw["dbp_samples_per_symbol"], sw["spans"]
+    lengths = sorted(set(int(u) for u in U))
+    tx, pristine, pw = [], [], []
+    for u in lengths:
+        idx = np.nonzero(U == u)[0]
+        ns = 1 << u
+        codes = rng.integers(0, 16, (len(idx), 1, ns))
+        sym = dsp.qam16_map(codes, fg.Domain(1, ns, 1 / 32e9, F0), batch=len(idx), ctx=ctx)
+        dsp.scale_each(sym, np.sqrt(1e-3 * 10 ** (P[idx] / 10)))
+        tx.append(sym)
+        pristine.append(dsp.rrc_shaping(sym, osf, sw["roll_off"]))
+        pw.append(P[idx])
+    tuned = {}
+    for f in pristine:
+        tuned[f.domain.samples] = fg.autotune(f.domain.samples, f.batch, ctx=ctx)[0]
+    ssfm = fg.SSFM(fib)
+    ssfm.set_grid(fg.SSFM.ADAPTIVE)
+    ssfm.set_maximum_phase_shift(W["max_phase_shift"])
+    ssfm.set_maximum_step_size(W["max_step_m"])
+    work = [f.copy() for f in pristine]
+
+    def forward(seed):
+        for w, f in zip(work, pristine):
+            w.assign(f)
+        return fg.span_loop(work, fib, ssfm, spans, after=fg.Amplifier.AMPLIFY,
+                            amplifier=fg.Amplifier(G, NF, seed=seed))
+
+    n0 = fg.launch_count()
+    forward(300)  # records the graph
+    n1 = fg.launch_count()
+    steps, fwd_ms = _stream_ms(torch, stream, lambda: forward(301))
+    fwd_launches = fg.launch_count() - n1
+    fwd_ss = float(sum(int(st.sum()) * f.domain.samples for st, f in zip(steps, work)))
+
+    rx = [dsp.decimate(w, osf // dosf) for w in work]
+    ks = sw["dbp_steps_per_span"]
+    dbp = [r.copy() for k in ks for r in rx]
+    ssfms = [fg.SSFM(fib, k) for k in ks for _ in rx]
+
+    def backward():
+        for d, r in zip(dbp, [r for _ in ks for r in rx]):
+            d.assign(r)
+        return fg.span_loop(dbp, fib, ssfms, spans, direction=fg.SSFM.BACKWARD, amplifier=fg.Amplifier(G),
+                            before=fg.Amplifier.DROP_POWER)
+
+    backward()  # records
+    n2 = fg.launch_count()
+    _, dbp_ms = _stream_ms(torch, stream, backward)
+    dbp_launches = fg.launch_count() - n2
+    dbp_ss = float(sum(k * spans * r.batch * r.domain.samples for k in ks for r in rx))
+    # the same DBP work through the host-driven span loop, for comparison
+    host = [r.copy() for k in ks for r in rx]
+
+    def backward_host():
+        for d, r, s in zip(host, [r for _ in ks for r in rx], ssfms):
+            d.assign(r)
+            fg.backward_propagation(d, fib, s, G, spans)
+
+    _, host_ms = _stream_ms(torch, stream, backward_host)
+    q = {}
+    pse = dsp.PhaseShiftEqualizer(720)
+    for i, k in enumerate(ks):
+        qs = []
+        for j, t in enumerate(tx):
+            y = dsp.rrc_sampling(dbp[i * len(rx) + j], dosf, sw["roll_off"])
+            qs.append(dsp.q2_factor(t, pse.train_equalize(t, y), 100))
+        q["%d_steps_per_span" % k] = float(np.mean(np.concatenate(qs)))
+    return {
+        "config": sw, "lengths_samples": {str(f.domain.samples): f.batch for f in pristine},
+        "autotuned_log2_n1": {str(k): v for k, v in tuned.items()},
+        "forward": {"graph_launches": 1, "kernels": int(fwd_launches), "ms": fwd_ms,
+                    "sample_steps": fwd_ss, "gsample_steps_per_s": fwd_ss / fwd_ms / 1e6,
+                    "first_call_kernels": int(n1 - n0)},
+        "dbp": {"graph_launches": 1, "fields": len(dbp), "kernels": int(dbp_launches), "ms": dbp_ms,
+                "sample_steps": dbp_ss, "gsample_steps_per_s": dbp_ss / dbp_ms / 1e6,
+                "host_driven_ms": host_ms, "q_db_mean": q},
+    }
+
+
 def run_ncu_case(args):
     """Small case for ncu captures: UNIFORM split steps on 40 realizations of
     the N=2^19 WDM field (168 MB, above the L2 size), 4 steps."""
@@ -444,6 +560,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-dbp", action="store_true", help="skip the learned-vs-plain DBP section")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the uneven-length batched sweep section")
     args = ap.parse_args()
     if args.ncu_case:
         return run_ncu_case(args)

@@ -38,6 +38,10 @@ class CSsfmOpts(C.Structure):
     _fields_ = [("grid", I), ("total_steps", I), ("maximum_phase_shift", D), ("maximum_step_size", D)]
 
 
+class CAmp(C.Structure):
+    _fields_ = [("gain", D), ("noise_factor", D), ("seed", U64), ("counter0", U64), ("before", I), ("after", I)]
+
+
 # name -> (restype, argtypes); every symbol the header declares is listed here
 # (tests check this table against include/*.h).
 SIGNATURES = {
@@ -67,6 +71,10 @@ SIGNATURES = {
     "focss_forward_propagation": (I, [P, P, C.POINTER(CFiber), C.POINTER(CSsfmOpts), D, D, U64, U64, I]),
     "focss_backward_propagation": (I, [P, P, C.POINTER(CFiber), C.POINTER(CSsfmOpts), D, I]),
     "focss_cd_compensation": (I, [P, P, C.POINTER(CFiber), I]),
+    "focss_span_loop": (I, [P, I, C.POINTER(P), C.POINTER(CFiber), C.POINTER(CSsfmOpts), C.POINTER(CAmp), I, D,
+                            P]),
+    "focss_autotune": (I, [P, I, I, C.POINTER(I), C.POINTER(D)]),
+    "focss_set_fft_split": (I, [P, I, I]),
     "focss_qam16_map": (I, [P, P, SZ, P]),
     "focss_upsample": (I, [P, P, I, P]),
     "focss_downsample": (I, [P, P, I, P]),

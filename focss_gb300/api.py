@@ -14,7 +14,7 @@ from dataclasses import dataclass, replace
 
 import numpy as np
 
-from ._lib import CDomain, CFiber, CSsfmOpts, FocssError, alive, check, lib
+from ._lib import CAmp, CDomain, CFiber, CSsfmOpts, FocssError, alive, check, lib
 
 # src/focss/definitions.h:13-15
 MATH_PI = 3.14159265358979323846264338
@@ -316,6 +316,55 @@ def backward_propagation(field: Field, fiber: Fiber, ssfm: SSFM, gain: float, sp
     fb, op = fiber.c(), ssfm.opts()
     check(lib().focss_backward_propagation(field.ctx.h, field.h, C.byref(fb), C.byref(op), gain, spans),
           field.ctx.h)
+
+
+AMP_NONE = -1
+
+
+def span_loop(fields, fiber: Fiber, ssfms, spans: int, direction: float = SSFM.FORWARD,
+              amplifier: Amplifier | None = None, before: int = AMP_NONE, after: int = AMP_NONE,
+              counter0: int = 0):
+    """Span loops of forward/backward_propagation (src/tasks/systems.cpp:26-91)
+    for several fields at once, as one CUDA-graph launch (focss_span_loop):
+    per span, amplifier op `before`, SSFM with ssfms[i] on fields[i], op
+    `after`.  `ssfms` is one SSFM or one per field.  Returns the steps per
+    realization summed over spans, one array per field."""
+    fields = list(fields)
+    if isinstance(ssfms, SSFM):
+        ssfms = [ssfms] * len(fields)
+    if len(ssfms) != len(fields):
+        raise FocssError(1, "span_loop: one SSFM per field")
+    ctx = fields[0].ctx
+    handles = (C.c_void_p * len(fields))(*[f.h.value if isinstance(f.h, C.c_void_p) else f.h for f in fields])
+    opts = (CSsfmOpts * len(fields))(*[s.opts() for s in ssfms])
+    amp = amplifier or Amplifier()
+    ca = CAmp(amp.gain, amp.noise_factor, amp.seed, counter0, before, after)
+    total = sum(f.batch for f in fields)
+    steps = np.zeros(total, np.int32)
+    fb = fiber.c()
+    check(lib().focss_span_loop(ctx.h, len(fields), handles, C.byref(fb), opts, C.byref(ca), spans, direction,
+                                steps.ctypes.data_as(C.c_void_p)), ctx.h)
+    out, o = [], 0
+    for f in fields:
+        out.append(steps[o:o + f.batch].copy())
+        o += f.batch
+    return out
+
+
+def autotune(samples: int, batch: int, ctx: Context | None = None):
+    """Time every admissible FFT split of length `samples` on `batch`
+    realizations and keep the fastest for this context's split-step runs.
+    Returns (log2 N1, ms per step)."""
+    ctx = ctx or Context.default()
+    l1, ms = C.c_int(), C.c_double()
+    check(lib().focss_autotune(ctx.h, samples, batch, C.byref(l1), C.byref(ms)), ctx.h)
+    return l1.value, ms.value
+
+
+def set_fft_split(samples: int, log2_n1: int, ctx: Context | None = None):
+    """Pin the split of length-`samples` split-step runs (0 = balanced default)."""
+    ctx = ctx or Context.default()
+    check(lib().focss_set_fft_split(ctx.h, samples, log2_n1), ctx.h)
 
 
 def cd_compensation(field: Field, fiber: Fiber, spans: int):

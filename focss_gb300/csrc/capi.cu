@@ -28,7 +28,26 @@ focss_status cuda_check(Ctx* ctx, cudaError_t e, const char* what) {
 }
 
 focss_status get_plan(Ctx* ctx, int N, const Plan** out) {
-    auto it = ctx->plans.find(N);
+    int lg = 0;
+    while ((1 << lg) < N) ++lg;
+    return get_plan_split(ctx, N, lg / 2, out);
+}
+
+int default_split(int N) {
+    int lg = 0;
+    while ((1 << lg) < N) ++lg;
+    return lg / 2;
+}
+
+bool split_supported(int N, int log2N1) {
+    int lg = 0;
+    while ((1 << lg) < N) ++lg;
+    return fft_size_supported(N) && log2N1 >= 4 && log2N1 <= 10 && lg - log2N1 >= 4 && lg - log2N1 <= 10;
+}
+
+focss_status get_plan_split(Ctx* ctx, int N, int log2N1, const Plan** out) {
+    const long long key = ((long long)log2N1 << 32) | (unsigned)N;
+    auto it = ctx->plans.find(key);
     if (it != ctx->plans.end()) {
         *out = &it->second;
         return FOCSS_OK;
@@ -36,12 +55,15 @@ focss_status get_plan(Ctx* ctx, int N, const Plan** out) {
     if (!fft_size_supported(N))
         return set_error(ctx, FOCSS_ERR_UNSUPPORTED,
                          "field length " + std::to_string(N) + " is not a power of two in [2^8, 2^20]");
+    if (!split_supported(N, log2N1))
+        return set_error(ctx, FOCSS_ERR_UNSUPPORTED, "FFT split 2^" + std::to_string(log2N1) + " of length " +
+                                                         std::to_string(N) + " is outside [2^4, 2^10] x [2^4, 2^10]");
     Plan p;
     int lg = 0;
     while ((1 << lg) < N) ++lg;
     p.N = N;
-    p.log2N1 = lg / 2;
-    p.log2N2 = lg - lg / 2;
+    p.log2N1 = log2N1;
+    p.log2N2 = lg - log2N1;
     p.N1 = 1 << p.log2N1;
     p.N2 = 1 << p.log2N2;
     // Twiddle tables from FP64 as double-float pairs {re_hi, im_hi, re_lo, im_lo}
@@ -74,7 +96,7 @@ focss_status get_plan(Ctx* ctx, int N, const Plan** out) {
         cudaFree(p.tw);
         return cuda_check(ctx, e, "twiddle upload");
     }
-    auto res = ctx->plans.emplace(N, p);
+    auto res = ctx->plans.emplace(key, p);
     *out = &res.first->second;
     return FOCSS_OK;
 }
@@ -122,12 +144,43 @@ void* scratch_buffer(Ctx* ctx, int slot, size_t bytes) {
 }
 
 static long long g_launches = 0;
-void count_launch(long long n) { __atomic_fetch_add(&g_launches, n, __ATOMIC_RELAXED); }
+// Launches recorded into a graph are counted when the graph runs, not here.
+thread_local int g_capturing = 0;
+void count_launch(long long n) {
+    if (!g_capturing) __atomic_fetch_add(&g_launches, n, __ATOMIC_RELAXED);
+}
+void count_launch_graph(long long n) { __atomic_fetch_add(&g_launches, n, __ATOMIC_RELAXED); }
+void set_capturing(bool on) { g_capturing += on ? 1 : -1; }
 
 }  // namespace fg
 
+namespace fg {
+// Amplifier::amplify / add_noise / give_power / drop_power
+// (src/focss/module/amplifier.cpp:15-42) as A <- scale*A + sigma*(z0 + i z1).
+bool amplifier_coeffs(int op, double gain, double noise_factor, double f0, double dt, double* scale,
+                      double* sigma) {
+    const double kPlanck = 6.62607004081818181818181e-34;  // src/focss/definitions.h:14
+    bool noise = false;
+    switch (op) {
+        case FOCSS_AMP_AMPLIFY: *scale = std::sqrt(gain); noise = noise_factor != 0; break;     // :15-18
+        case FOCSS_AMP_ADD_NOISE: *scale = 1.0; noise = true; break;                            // :20-28
+        case FOCSS_AMP_GIVE_POWER: *scale = gain > 1 ? std::sqrt(gain) : std::sqrt(1 / gain); break;  // :30-35
+        case FOCSS_AMP_DROP_POWER: *scale = gain < 1 ? std::sqrt(gain) : std::sqrt(1 / gain); break;  // :37-42
+        default: return false;
+    }
+    *sigma = 0.0;
+    if (noise) {
+        // amplifier.cpp:21-27: variance = h f0 NF (G-1)/2 * (1/dt); sigma per quadrature = sqrt(var/2)
+        double variance = kPlanck * f0;
+        variance *= noise_factor * (gain - 1) / 2;
+        variance *= 1.0 / dt;
+        *sigma = std::sqrt(variance / 2);
+    }
+    return true;
+}
+}  // namespace fg
+
 namespace {
-const double kPlanck = 6.62607004081818181818181e-34;  // src/focss/definitions.h:14
 
 bool same_shape(const Field* a, const Field* b) {
     return a->modes == b->modes && a->samples == b->samples && a->batch == b->batch;
@@ -184,6 +237,7 @@ FOCSS_API focss_status focss_ctx_destroy(focss_ctx* c) {
     for (void* p : c->scratch) cudaFree(p);
     for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
     for (auto& kv : c->tables) cudaFree(kv.second);
+    fg::free_loop_graphs(c);
     cudaFree(c->d_state);
     cudaFree(c->d_counters);
     cudaFree(c->d_red);
@@ -358,23 +412,9 @@ FOCSS_API focss_status focss_amplifier_apply(focss_ctx* c, focss_field* f, doubl
                                              uint64_t seed, uint64_t counter, int op) {
     if (!c || !f) return FOCSS_ERR_INVALID_ARG;
     if (!(gain > 0)) return fg::set_error(c, FOCSS_ERR_INVALID_ARG, "amplifier: gain must be > 0");
-    double scale = 1.0;
-    bool noise = false;
-    switch (op) {
-        case FOCSS_AMP_AMPLIFY: scale = std::sqrt(gain); noise = noise_factor != 0; break;     // :15-18
-        case FOCSS_AMP_ADD_NOISE: scale = 1.0; noise = true; break;                            // :20-28
-        case FOCSS_AMP_GIVE_POWER: scale = gain > 1 ? std::sqrt(gain) : std::sqrt(1 / gain); break;  // :30-35
-        case FOCSS_AMP_DROP_POWER: scale = gain < 1 ? std::sqrt(gain) : std::sqrt(1 / gain); break;  // :37-42
-        default: return fg::set_error(c, FOCSS_ERR_INVALID_ARG, "amplifier: unknown op");
-    }
-    double sigma = 0.0;
-    if (noise) {
-        // amplifier.cpp:21-27: variance = h f0 NF (G-1)/2 * (1/dt); sigma per quadrature = sqrt(var/2)
-        double variance = kPlanck * f->f0;
-        variance *= noise_factor * (gain - 1) / 2;
-        variance *= 1.0 / f->dt;
-        sigma = std::sqrt(variance / 2);
-    }
+    double scale = 1.0, sigma = 0.0;
+    if (!fg::amplifier_coeffs(op, gain, noise_factor, f->f0, f->dt, &scale, &sigma))
+        return fg::set_error(c, FOCSS_ERR_INVALID_ARG, "amplifier: unknown op");
     return fg::cuda_check(c,
                           fg::launch_amplifier(f->d, f->modes, f->samples, f->batch, (float)scale, (float)sigma,
                                                seed, counter, c->stream),

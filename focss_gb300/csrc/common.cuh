@@ -108,4 +108,23 @@ __device__ __forceinline__ float2 gaussian_pair(uint32_t x0, uint32_t x1) {
     return make_float2(r * c, r * s);
 }
 
+// One sample of Amplifier::amplify / add_noise (src/focss/module/amplifier.cpp:15-28):
+// scale*a + sigma*(z0 + i z1), (z0, z1) Box-Muller on Philox4x32-10 with
+// counter {sample, mode + modes*realization, c_lo, c_hi} (element i of a
+// realization-major, mode-major buffer of `samples` per mode).
+__device__ __forceinline__ float2 amplifier_sample(float2 a, size_t i, int samples, float scale, float sigma,
+                                                   uint2 key, uint32_t c_lo, uint32_t c_hi) {
+    a.x *= scale;
+    a.y *= scale;
+    if (sigma != 0.0f) {
+        const uint32_t sample = (uint32_t)(i % (size_t)samples);
+        const uint32_t stream = (uint32_t)(i / (size_t)samples);
+        const uint4 r = philox4x32_10(make_uint4(sample, stream, c_lo, c_hi), key);
+        const float2 z = gaussian_pair(r.x, r.y);
+        a.x = fmaf(sigma, z.x, a.x);
+        a.y = fmaf(sigma, z.y, a.y);
+    }
+    return a;
+}
+
 }  // namespace fg

@@ -29,20 +29,8 @@ cudaError_t launch_scale(float2* d, size_t n, float2 s, cudaStream_t st) {
 // counter {sample, mode + modes*realization, counter_lo, counter_hi}.
 __global__ void amplifier_kernel(float2* __restrict__ d, int modes, int samples, size_t n, float scale,
                                  float sigma, uint2 key, uint32_t c_lo, uint32_t c_hi) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        float2 a = d[i];
-        a.x *= scale;
-        a.y *= scale;
-        if (sigma != 0.0f) {
-            const uint32_t sample = (uint32_t)(i % (size_t)samples);
-            const uint32_t stream = (uint32_t)(i / (size_t)samples);  // mode + modes*b
-            const uint4 r = philox4x32_10(make_uint4(sample, stream, c_lo, c_hi), key);
-            const float2 z = gaussian_pair(r.x, r.y);
-            a.x = fmaf(sigma, z.x, a.x);
-            a.y = fmaf(sigma, z.y, a.y);
-        }
-        d[i] = a;
-    }
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        d[i] = amplifier_sample(d[i], i, samples, scale, sigma, key, c_lo, c_hi);
     (void)modes;
 }
 

@@ -61,6 +61,7 @@ struct PassArgs {
     SsfmState* state;       // null: plain transform driven by `op`
     SsfmParams prm;
     int N, N1, N2, log2N2;
+    int batch;              // realizations (set by the launch helpers)
     int op;
     float scale;
     int bp_cut;
@@ -71,10 +72,12 @@ struct Plan {
     float4* tw = nullptr;   // device tables (layout above)
 };
 
+struct LoopGraph;  // span_loop.cu
+
 struct Ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
-    std::map<int, Plan> plans;
+    std::map<long long, Plan> plans;  // key (log2 N1 << 32) | N
     std::string last_error;
     SsfmState* d_state = nullptr;
     int state_cap = 0;
@@ -91,10 +94,22 @@ struct Ctx {
     std::vector<cudaEvent_t> prof_events;
     double prof_ms[2] = {0, 0};          // column, row
     long long prof_launches[2] = {0, 0};
+    // split-step FFT split (log2 N1) per length picked by the autotuner or
+    // pinned by the caller; lengths absent here use the balanced split
+    std::map<int, int> ssfm_split;
+    // instantiated span-loop graphs keyed by shape and parameters, and the
+    // streams/events their capture uses (span_loop.cu)
+    std::map<std::string, LoopGraph*> loops;
+    std::vector<cudaStream_t> side_streams;
+    std::vector<cudaEvent_t> side_events;
 };
 
-// Process-wide launch counter (focss_launch_count).
+// Process-wide launch counter (focss_launch_count).  While a graph is being
+// captured on this thread, launches are not counted; count_launch_graph adds
+// the kernels a graph ran.
 void count_launch(long long n = 1);
+void count_launch_graph(long long n);
+void set_capturing(bool on);
 
 struct Field {
     Ctx* ctx = nullptr;
@@ -107,7 +122,10 @@ struct Field {
 // ---- helpers implemented in capi.cu
 focss_status set_error(Ctx* ctx, focss_status st, const std::string& msg);
 focss_status cuda_check(Ctx* ctx, cudaError_t e, const char* what);
-focss_status get_plan(Ctx* ctx, int N, const Plan** out);
+focss_status get_plan(Ctx* ctx, int N, const Plan** out);  // balanced split
+focss_status get_plan_split(Ctx* ctx, int N, int log2N1, const Plan** out);
+int default_split(int N);
+bool split_supported(int N, int log2N1);
 focss_status ensure_state(Ctx* ctx, int batch);
 focss_status ensure_red(Ctx* ctx, size_t doubles);
 void* scratch_buffer(Ctx* ctx, int slot, size_t bytes);
@@ -118,6 +136,21 @@ cudaError_t launch_col(const Plan& p, PassArgs a, int batch, cudaStream_t s);
 cudaError_t launch_row(const Plan& p, PassArgs a, int batch, cudaStream_t s);
 focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ssfm_opts& o, double dir,
                       int* steps_out);
+// Argument checks of ssfm_run and the pass arguments of one run (state and
+// finished-realization counter supplied by the caller).
+focss_status ssfm_validate(Ctx* ctx, const Field* f, const focss_fiber& fib, const focss_ssfm_opts& o);
+PassArgs ssfm_args(const Field* f, const focss_fiber& fib, const focss_ssfm_opts& o, double dir, SsfmState* state,
+                   int* n_done);
+// The plan ssfm_run uses for length N (autotuned or pinned split, else balanced).
+focss_status ssfm_plan(Ctx* ctx, int N, const Plan** out);
+
+// Amplifier operation `op` (FOCSS_AMP_*) as A <- scale*A + sigma*(z0 + i z1);
+// false for an unknown op (capi.cu).
+bool amplifier_coeffs(int op, double gain, double noise_factor, double f0, double dt, double* scale,
+                      double* sigma);
+
+// ---- span_loop.cu
+void free_loop_graphs(Ctx* ctx);
 // Plain transforms on a field buffer of `batch` x N (modes folded into batch).
 focss_status fft_forward(Ctx* ctx, float2* data, int N, int batch);   // natural order, x 1/N
 focss_status fft_inverse(Ctx* ctx, float2* data, int N, int batch);   // natural order, unnormalized

@@ -20,6 +20,7 @@
 // a = beta2/2*hl*dw^2/(2*pi) (turns per k'^2) held as a 64-bit fixed-point
 // turn fraction; a*k'^2 mod 1 is then an exact wrapping 64-bit integer
 // product, so the FP32 sincospi argument is already range-reduced to [-1, 1).
+#include <algorithm>
 #include <cmath>
 
 #include "ssfm_kernels.cuh"
@@ -81,24 +82,30 @@ bool fft_size_supported(int N) {
     return lg >= 8 && lg <= 20;
 }
 
+// Opt the kernel in to `smem` bytes of dynamic shared memory (once per size).
+cudaError_t prepare(Launch& l, size_t smem) {
+    if (l.attr_set && smem <= l.smem) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute((const void*)l.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    l.attr_set = true;
+    l.smem = smem;
+    return cudaSuccess;
+}
+
 cudaError_t launch_col(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
     static Launch cache[16];
     Launch& l = cache[p.log2N1];
     if (!l.fn) l = col_launch_for(p.log2N1);
     if (!l.fn) return cudaErrorInvalidValue;
     const size_t smem = sizeof(float4) * (2 * (size_t)p.N1 + p.N2) + sizeof(float2) * (size_t)p.N1 * l.per_block;
-    if (!l.attr_set || smem > l.smem) {
-        cudaError_t e = cudaFuncSetAttribute((const void*)l.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
-        if (e != cudaSuccess) return e;
-        l.attr_set = true;
-        l.smem = smem;
-    }
+    cudaError_t e = prepare(l, smem);
+    if (e != cudaSuccess) return e;
     a.N = p.N;
     a.N1 = p.N1;
     a.N2 = p.N2;
     a.log2N2 = p.log2N2;
     a.tw = p.tw;
+    a.batch = batch;
     dim3 grid(p.N2 / l.per_block, batch);
     l.fn<<<grid, l.threads, smem, s>>>(a);
     count_launch();
@@ -114,18 +121,14 @@ cudaError_t launch_row(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
     const int Q = p.N2 / P;
     int R = l.per_block;
     const size_t smem = sizeof(float4) * ((size_t)p.N2 + 512) + sizeof(float2) * (size_t)R * Q * (P + 1);
-    if (!l.attr_set || smem > l.smem) {
-        cudaError_t e = cudaFuncSetAttribute((const void*)l.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
-        if (e != cudaSuccess) return e;
-        l.attr_set = true;
-        l.smem = smem;
-    }
+    cudaError_t e = prepare(l, smem);
+    if (e != cudaSuccess) return e;
     a.N = p.N;
     a.N1 = p.N1;
     a.N2 = p.N2;
     a.log2N2 = p.log2N2;
     a.tw = p.tw;
+    a.batch = batch;
     if (p.N1 % R != 0) return cudaErrorInvalidValue;
     dim3 grid(p.N1 / R, batch);
     l.fn<<<grid, l.threads, smem, s>>>(a);
@@ -162,14 +165,12 @@ void prof_collect(Ctx* ctx) {
 }
 }  // namespace
 
-focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ssfm_opts& o, double dir,
-                      int* steps_out) {
+focss_status ssfm_validate(Ctx* ctx, const Field* f, const focss_fiber& fib, const focss_ssfm_opts& o) {
     if (f->modes != 1)
         return set_error(ctx, FOCSS_ERR_UNSUPPORTED, "ssfm_run: only single-mode fields are implemented");
-    const int N = f->samples;
-    const Plan* p = nullptr;
-    focss_status st = get_plan(ctx, N, &p);
-    if (st != FOCSS_OK) return st;
+    if (!fft_size_supported(f->samples))
+        return set_error(ctx, FOCSS_ERR_UNSUPPORTED,
+                         "field length " + std::to_string(f->samples) + " is not a power of two in [2^8, 2^20]");
     if (o.grid == FOCSS_UNIFORM && o.total_steps <= 0)
         return set_error(ctx, FOCSS_ERR_INVALID_ARG, "ssfm_run: total_steps must be > 0 for UNIFORM");
     if (o.grid != FOCSS_UNIFORM && (!(o.maximum_step_size > 0) || !(o.maximum_phase_shift > 0)))
@@ -179,17 +180,15 @@ focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ss
         return set_error(ctx, FOCSS_ERR_INVALID_ARG, "ssfm_run: LOGARITHMIC grid needs alpha != 0");
     if (!(fib.length > 0)) return set_error(ctx, FOCSS_ERR_INVALID_ARG, "ssfm_run: fiber length must be > 0");
     if (o.grid < 0 || o.grid > 2) return set_error(ctx, FOCSS_ERR_INVALID_ARG, "ssfm_run: unknown grid");
-    st = ensure_state(ctx, f->batch);
-    if (st != FOCSS_OK) return st;
-    cudaStream_t s = ctx->stream;
-    st = cuda_check(ctx, cudaMemsetAsync(ctx->d_state, 0, sizeof(SsfmState) * f->batch, s), "memset state");
-    if (st != FOCSS_OK) return st;
-    st = cuda_check(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(int) * 4, s), "memset counters");
-    if (st != FOCSS_OK) return st;
+    return FOCSS_OK;
+}
 
+PassArgs ssfm_args(const Field* f, const focss_fiber& fib, const focss_ssfm_opts& o, double dir, SsfmState* state,
+                   int* n_done) {
+    const int N = f->samples;
     PassArgs a{};
     a.data = f->d;
-    a.state = ctx->d_state;
+    a.state = state;
     a.prm.alpha = fib.alpha;
     a.prm.beta2 = fib.beta2;
     a.prm.gamma = fib.gamma;
@@ -202,7 +201,30 @@ focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ss
     a.prm.grid = o.grid;
     a.prm.total_steps = o.total_steps;
     a.prm.samples = N;
-    a.prm.n_done = ctx->d_counters;
+    a.prm.n_done = n_done;
+    return a;
+}
+
+focss_status ssfm_plan(Ctx* ctx, int N, const Plan** out) {
+    auto it = ctx->ssfm_split.find(N);
+    return get_plan_split(ctx, N, it != ctx->ssfm_split.end() ? it->second : default_split(N), out);
+}
+
+focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ssfm_opts& o, double dir,
+                      int* steps_out) {
+    focss_status st = ssfm_validate(ctx, f, fib, o);
+    if (st != FOCSS_OK) return st;
+    const Plan* p = nullptr;
+    st = ssfm_plan(ctx, f->samples, &p);
+    if (st != FOCSS_OK) return st;
+    st = ensure_state(ctx, f->batch);
+    if (st != FOCSS_OK) return st;
+    cudaStream_t s = ctx->stream;
+    st = cuda_check(ctx, cudaMemsetAsync(ctx->d_state, 0, sizeof(SsfmState) * f->batch, s), "memset state");
+    if (st != FOCSS_OK) return st;
+    st = cuda_check(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(int) * 4, s), "memset counters");
+    if (st != FOCSS_OK) return st;
+    const PassArgs a = ssfm_args(f, fib, o, dir, ctx->d_state, ctx->d_counters);
 
     // Upper bound on column passes: UNIFORM is exact; the others are polled.
     long long cap;

@@ -171,6 +171,46 @@ FOCSS_API focss_status focss_backward_propagation(focss_ctx* ctx, focss_field* f
 FOCSS_API focss_status focss_cd_compensation(focss_ctx* ctx, focss_field* field,
                                              const focss_fiber* fiber, int spans);
 
+/* ------------------------------------------ graph-captured span loops */
+#define FOCSS_AMP_NONE (-1)
+typedef struct focss_amp {
+    double gain;          /* linear span gain G (Amplifier(gain, noise_factor))      */
+    double noise_factor;  /* linear noise factor; 0 = no ASE                         */
+    uint64_t seed;        /* ASE key; field i of a focss_span_loop call uses seed+i  */
+    uint64_t counter0;    /* ASE counter of span 0; span s uses counter0 + s         */
+    int before;           /* FOCSS_AMP_* applied before each span's SSFM, or _NONE   */
+    int after;            /* FOCSS_AMP_* applied after each span's SSFM, or _NONE    */
+} focss_amp;
+
+/* The span loops of forward_propagation / backward_propagation
+ * (src/tasks/systems.cpp:26-61, 73-91) for n_fields fields at once: for each
+ * span, amp->before, SSFM::run(field, direction) with opts[i] (one entry per
+ * field), amp->after.  Fields may differ in length and batch; they run as
+ * concurrent branches of ONE CUDA graph launch.  UNIFORM grids are fixed
+ * sequences of passes; ADAPTIVE and LOGARITHMIC spans run as a device-side
+ * loop (a conditional WHILE graph node) that a kernel ends once every
+ * realization of the field has finished the span, capped at 2^17 passes per
+ * span (FOCSS_ERR_NOT_CONVERGED beyond).  The graph is recorded on the first
+ * call for a given set of fields, shapes and parameters and replayed after
+ * that; seed and counter0 are read from device memory, so changing them does
+ * not re-record.  steps_out (may be NULL) receives, per realization, the steps
+ * summed over all spans, fields concatenated in order.  Returns after the
+ * propagation finished.  No reference counterpart for the multi-field form. */
+FOCSS_API focss_status focss_span_loop(focss_ctx* ctx, int n_fields, focss_field* const* fields,
+                                       const focss_fiber* fiber, const focss_ssfm_opts* opts,
+                                       const focss_amp* amp, int spans, double direction, int* steps_out);
+
+/* Split-step FFT autotuner (no reference counterpart).  The two-pass FFT of
+ * length N = N1*N2 can use any split with N1, N2 in [2^4, 2^10]; this times
+ * every admissible split on a scratch batch of `batch` realizations (a few
+ * UNIFORM steps each, CUDA events) and keeps the fastest for this context's
+ * split-step runs of length `samples`.  log2_n1 / ms_per_step (may be NULL)
+ * receive the choice and its time per step for the whole batch. */
+FOCSS_API focss_status focss_autotune(focss_ctx* ctx, int samples, int batch, int* log2_n1, double* ms_per_step);
+/* Pin the split used for split-step runs of length `samples` (log2_n1 = 0
+ * restores the balanced default). */
+FOCSS_API focss_status focss_set_fft_split(focss_ctx* ctx, int samples, int log2_n1);
+
 /* --------------------------------------------------- TX / resampling DSP */
 /* Output fields must be created by the caller with the shape the reference
  * would produce (same modes and batch; samples as stated).  Inputs are not
