@@ -20,8 +20,8 @@ __device__ __forceinline__ float cnorm(float2 a) { return fmaf(a.x, a.x, a.y * a
 
 // (cos phi, sin phi).  |phi| <= 1/4 (every step of an adaptive grid, whose
 // nonlinear phase is bounded by construction): Taylor polynomials to degree
-// 8/9 (truncation < 3e-13), about one FP32 rounding; larger phases fall back
-// to sincosf.
+// 8/9 (truncation < 3e-13), about one FP32 rounding; larger phases take the
+// reduced path below.
 __device__ __forceinline__ float2 phase_rotation(float phi) {
     if (fabsf(phi) <= 0.25f) {
         const float p2 = phi * phi;
@@ -30,9 +30,21 @@ __device__ __forceinline__ float2 phase_rotation(float phi) {
                              1.0f);
         return make_float2(c, s);
     }
-    float s, c;
-    sincosf(phi, &s, &c);
-    return make_float2(c, s);
+    // Larger phases: Cody-Waite reduction by q quarter turns (pi/2 as a
+    // two-float constant), Taylor series on |r| <= pi/4 (truncation below
+    // 3e-9), exact quarter-turn placement.  Straight-line code with no local
+    // memory, so it stays cheap to inline in unrolled loops.
+    const float q = rintf(phi * 0.63661977236758134f);
+    float r = fmaf(-q, 1.57079637050628662f, phi);
+    r = fmaf(q, 4.37113900018624284e-8f, r);
+    const float r2 = r * r;
+    const float sr = r * fmaf(r2, fmaf(r2, fmaf(r2, fmaf(r2, 1.0f / 362880.0f, -1.0f / 5040.0f), 1.0f / 120.0f),
+                                        -1.0f / 6.0f), 1.0f);
+    const float cr = fmaf(r2, fmaf(r2, fmaf(r2, fmaf(r2, fmaf(r2, -1.0f / 3628800.0f, 1.0f / 40320.0f),
+                                                         -1.0f / 720.0f), 1.0f / 24.0f), -0.5f), 1.0f);
+    const int k = (int)q & 3;
+    const float c = (k & 1) ? -sr : cr, s = (k & 1) ? cr : sr;
+    return (k & 2) ? make_float2(-c, -s) : make_float2(c, s);
 }
 
 // Block-wide reductions (blockDim.x multiple of 32, <= 1024).

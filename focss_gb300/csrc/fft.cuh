@@ -150,6 +150,38 @@ struct ColLayout {
 // XOR swizzle of a table index inside groups of 8 entries (16-byte entries:
 // 8 per 128-byte shared-memory wavefront), so strided reads spread over banks.
 __host__ __device__ __forceinline__ int swz8(int e) { return e ^ (((e >> 3) ^ (e >> 6)) & 7); }
+// The same for 8-byte entries (16 per wavefront).
+__host__ __device__ __forceinline__ int swz16(int e) { return e ^ ((e >> 4) & 15); }
+
+// ---------------------------------------------------------------------------
+// Rotations by lifting (three shears, A. W. Paeth, "A fast algorithm for
+// general raster rotation", Graphics Interface 1986): with ts = {tan(theta/2),
+// sin(theta)} in FP32,
+//     x -= t y;  y += s x;  x -= t y
+// rotates (x, y) by theta in three FMAs, and the same shears undone in reverse
+// order invert it exactly up to the data's own roundings, whatever the
+// rounding of t and s.  A forward transform whose inverse is its exact mirror
+// therefore adds no error that repeats identically from step to step (the
+// rounding of a plain FP32 twiddle does), which is what the column pass needs:
+// it applies the inverse transform, a Kerr phase close to identity and the
+// forward transform.  |theta| <= pi/2 keeps |t| <= 1.
+__device__ __forceinline__ float2 lift_rot(float2 v, float2 ts) {
+    float x = fmaf(-ts.x, v.y, v.x);
+    const float y = fmaf(ts.y, x, v.y);
+    x = fmaf(-ts.x, y, x);
+    return make_float2(x, y);
+}
+__device__ __forceinline__ float2 lift_rot_inv(float2 v, float2 ts) {
+    float x = fmaf(ts.x, v.y, v.x);
+    const float y = fmaf(-ts.y, x, v.y);
+    x = fmaf(ts.x, y, x);
+    return make_float2(x, y);
+}
+// v * (-i)^q (exact).
+__device__ __forceinline__ float2 quarter_turns(float2 v, int q) {
+    const float2 r = (q & 1) ? make_float2(v.y, -v.x) : v;
+    return (q & 2) ? make_float2(-r.x, -r.y) : r;
+}
 
 // Group-wide sub-FFT (see file comment).  twPQ[u*P + t] = exp(-2 pi i t u / L)
 // as double-float {re_hi, im_hi, re_lo, im_lo}: the P threads of a group read

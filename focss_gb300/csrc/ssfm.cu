@@ -97,7 +97,8 @@ cudaError_t launch_col(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
     Launch& l = cache[p.log2N1];
     if (!l.fn) l = col_launch_for(p.log2N1);
     if (!l.fn) return cudaErrorInvalidValue;
-    const size_t smem = sizeof(float4) * (2 * (size_t)p.N1 + p.N2) + sizeof(float2) * (size_t)p.N1 * l.per_block;
+    const size_t smem = sizeof(float4) * (size_t)p.N1 + sizeof(float2) * ((size_t)p.N1 / 4 + p.N2) +
+                        sizeof(float2) * (size_t)p.N1 * l.per_block;
     cudaError_t e = prepare(l, smem);
     if (e != cudaSuccess) return e;
     a.N = p.N;

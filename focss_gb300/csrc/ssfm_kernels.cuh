@@ -136,10 +136,10 @@ template <int N1, int C>
 __global__ void __launch_bounds__(C* PQ<N1>::P, 2) col_kernel(const PassArgs a) {
     constexpr int P = PQ<N1>::P, Q = PQ<N1>::Q;
     extern __shared__ float4 smem4[];
-    float4* s_fc = smem4;                           // column sub-FFT twiddles, (u,t) order
-    float4* s_hi = s_fc + N1;                       // six-step W_N1^h
-    float4* s_lo = s_hi + N1;                       // six-step W_N^l, swizzled
-    float2* sx = reinterpret_cast<float2*>(s_lo + a.N2);  // N1*C exchange
+    float4* s_fc = smem4;                                  // column sub-FFT twiddles, (u,t) order
+    float2* s_hi = reinterpret_cast<float2*>(s_fc + N1);   // six-step lifting pairs, W_N1^h, h < N1/4
+    float2* s_lo = s_hi + N1 / 4;                          // six-step lifting pairs, W_N^l, swizzled
+    float2* sx = s_lo + a.N2;                              // N1*C exchange
     __shared__ float red[64];
 
     const int b = blockIdx.y;
@@ -150,11 +150,11 @@ __global__ void __launch_bounds__(C* PQ<N1>::P, 2) col_kernel(const PassArgs a) 
         if (op == COL_IDLE) return;
     }
     const int N2 = a.N2;
-    for (int i = threadIdx.x; i < N1; i += blockDim.x) {
-        s_fc[i] = a.tw[i];
-        s_hi[i] = a.tw[N1 + N2 + i];
-    }
-    for (int i = threadIdx.x; i < N2; i += blockDim.x) s_lo[i] = a.tw[2 * N1 + N2 + i];
+    const float2* tw_hi = reinterpret_cast<const float2*>(a.tw + N1 + N2);
+    const float2* tw_lo = reinterpret_cast<const float2*>(a.tw + 2 * N1 + N2);
+    for (int i = threadIdx.x; i < N1; i += blockDim.x) s_fc[i] = a.tw[i];
+    for (int i = threadIdx.x; i < N1 / 4; i += blockDim.x) s_hi[i] = tw_hi[i];
+    for (int i = threadIdx.x; i < N2; i += blockDim.x) s_lo[i] = tw_lo[i];
 
     const int c = threadIdx.x % C, t = threadIdx.x / C;
     const int n2 = blockIdx.x * C + c;
@@ -165,24 +165,29 @@ __global__ void __launch_bounds__(C* PQ<N1>::P, 2) col_kernel(const PassArgs a) 
     __syncthreads();
 
     const ColLayout<P, C> lay{c};
-    const int mask = N2 - 1, sh = a.log2N2;
+    // Six-step twiddle W_N^e, e = n2*k1 = q*N/4 + h*N2 + l:  (-i)^q W_N1^h W_N^l,
+    // the last two as lifting rotations (|angles| < pi/2) whose inverses
+    // mirror them exactly.
+    const int mask = N2 - 1, sh = a.log2N2, qsh = a.log2N2 + ilog2c(N1) - 2, mmask = (1 << qsh) - 1;
     float pk = 0.0f, sm = 0.0f;
     if (op != COL_FWD) {
-        // inverse six-step twiddle W_N^{-n2 k1} = conj(W_N1^{e>>sh} W_N^{e&mask}), e = n2*k1
 #pragma unroll
         for (int j = 0; j < Q; ++j) {
-            const int e = n2 * (t + P * j);
-            v[j] = cmulc_df(cmulc_df(v[j], s_hi[e >> sh]), s_lo[swz8(e & mask)]);
+            const int e = n2 * (t + P * j), m = e & mmask;
+            v[j] = lift_rot_inv(lift_rot_inv(quarter_turns(v[j], -(e >> qsh) & 3), s_hi[m >> sh]),
+                                s_lo[swz16(m & mask)]);
         }
         fft_pq<P, Q, true, true>(v, sx, lay, t, s_fc);
     }
     if (op == COL_KERR) {
-        // src/focss/solver/ssfm.cpp:160-164: A *= exp(i kappa gamma h |A|^2)
+        // src/focss/solver/ssfm.cpp:160-164: A *= exp(i kappa gamma h |A|^2); the
+        // peak is taken from |A|^2 before the rotation (which preserves it).
         const float coef = (float)(a.prm.kappa * a.prm.gamma * st->h);
 #pragma unroll
         for (int j = 0; j < Q; ++j) {
-            v[j] = cmul(v[j], phase_rotation(coef * cnorm(v[j])));
-            pk = fmaxf(pk, cnorm(v[j]));
+            const float p = cnorm(v[j]);
+            v[j] = cmul(v[j], phase_rotation(coef * p));
+            pk = fmaxf(pk, p);
         }
     } else if (op == COL_FWD && st) {
 #pragma unroll
@@ -196,8 +201,8 @@ __global__ void __launch_bounds__(C* PQ<N1>::P, 2) col_kernel(const PassArgs a) 
         fft_pq<P, Q, false, true>(v, sx, lay, t, s_fc);
 #pragma unroll
         for (int j = 0; j < Q; ++j) {
-            const int e = n2 * (t + P * j);
-            v[j] = cmul_df(cmul_df(v[j], s_hi[e >> sh]), s_lo[swz8(e & mask)]);
+            const int e = n2 * (t + P * j), m = e & mmask;
+            v[j] = quarter_turns(lift_rot(lift_rot(v[j], s_lo[swz16(m & mask)]), s_hi[m >> sh]), e >> qsh);
         }
     }
 #pragma unroll
