@@ -213,6 +213,138 @@ __device__ __forceinline__ void fft_pq(float2 (&v)[Q], float2* __restrict__ sm, 
 }
 
 // ---------------------------------------------------------------------------
+// Mirrored sub-FFTs for the column pass: in-register DFT twiddles as lifting
+// rotations (quarter turns exact, residual |angle| <= pi/4 in three FMAs), and
+// an inverse that undoes the forward operation by operation in reverse order
+// (see lift_rot).  The inter-stage table twiddles stay double-float.
+
+// {tan(theta/2), sin(theta)} for theta = -pi*r/32, r = 0..8 (forward sign).
+__host__ __device__ __forceinline__ constexpr float2 lift_pi32(int r) {
+    constexpr float2 t[9] = {{0.0f, 0.0f},
+                             {-0.049126848578453064f, -0.0980171412229538f},
+                             {-0.09849140048027039f, -0.19509032368659973f},
+                             {-0.1483359932899475f, -0.290284663438797f},
+                             {-0.1989123672246933f, -0.3826834261417389f},
+                             {-0.25048696994781494f, -0.4713967442512512f},
+                             {-0.3033466935157776f, -0.5555702447891235f},
+                             {-0.3578057289123535f, -0.6343932747840881f},
+                             {-0.4142135679721832f, -0.7071067690849304f}};
+    return r >= 0 ? t[r] : float2{-t[-r].x, -t[-r].y};
+}
+
+// a * exp(-i pi idx/32) = (-i)^q * rot(-pi r/32), idx = 16 q + r, |r| <= 8.
+__device__ __forceinline__ float2 twlift(float2 a, int idx) {
+    idx &= 63;
+    const int q = (idx + 8) >> 4, r = idx - 16 * q;
+    if (r != 0) a = lift_rot(a, lift_pi32(r));
+    return quarter_turns(a, q & 3);
+}
+// Exact inverse of twlift.
+__device__ __forceinline__ float2 twlift_inv(float2 a, int idx) {
+    idx &= 63;
+    const int q = (idx + 8) >> 4, r = idx - 16 * q;
+    a = quarter_turns(a, -q & 3);
+    return r != 0 ? lift_rot_inv(a, lift_pi32(r)) : a;
+}
+
+template <int R>
+__device__ __forceinline__ void bitrev_swap(float2 (&v)[R]) {
+    constexpr int bits = ilog2c(R);
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        const int r = bitrev(i, bits);
+        if (i < r) {
+            const float2 tmp = v[i];
+            v[i] = v[r];
+            v[r] = tmp;
+        }
+    }
+}
+
+// Forward in-register DFT (radix-2 DIF, natural order in and out).
+template <int R>
+__device__ __forceinline__ void dft_lift(float2 (&v)[R]) {
+#pragma unroll
+    for (int half = R / 2; half >= 1; half >>= 1) {
+#pragma unroll
+        for (int base = 0; base < R; base += 2 * half) {
+#pragma unroll
+            for (int j = 0; j < half; ++j) {
+                const float2 a = v[base + j], b = v[base + j + half];
+                v[base + j] = cadd(a, b);
+                v[base + j + half] = twlift(csub(a, b), j * (32 / half));
+            }
+        }
+    }
+    bitrev_swap<R>(v);
+}
+// Its mirror: R times the inverse DFT.
+template <int R>
+__device__ __forceinline__ void dft_lift_inv(float2 (&v)[R]) {
+    bitrev_swap<R>(v);
+#pragma unroll
+    for (int half = 1; half < R; half <<= 1) {
+#pragma unroll
+        for (int base = 0; base < R; base += 2 * half) {
+#pragma unroll
+            for (int j = 0; j < half; ++j) {
+                const float2 s = v[base + j], d = twlift_inv(v[base + j + half], j * (32 / half));
+                v[base + j] = cadd(s, d);
+                v[base + j + half] = csub(s, d);
+            }
+        }
+    }
+}
+
+// fft_pq with the mirrored pieces (same layouts; forward and L times inverse).
+template <int P, int Q, bool BLOCK_SYNC, class Lay>
+__device__ __forceinline__ void fft_pq_lift(float2 (&v)[Q], float2* __restrict__ sm, const Lay lay, int t,
+                                            const float4* __restrict__ twPQ) {
+    static_assert(Q % P == 0, "Q must be a multiple of P");
+    constexpr int M = Q / P;
+    dft_lift<Q>(v);
+#pragma unroll
+    for (int u = 1; u < Q; ++u) v[u] = cmul_df(v[u], twPQ[u * P + t]);
+#pragma unroll
+    for (int u = 0; u < Q; ++u) sm[lay(u, t)] = v[u];
+    if (BLOCK_SYNC) __syncthreads(); else __syncwarp();
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+        float2 w[P];
+        const int u = t + P * i;
+#pragma unroll
+        for (int s = 0; s < P; ++s) w[s] = sm[lay(u, s)];
+        dft_lift<P>(w);
+#pragma unroll
+        for (int s = 0; s < P; ++s) v[i + M * s] = w[s];
+    }
+    if (BLOCK_SYNC) __syncthreads(); else __syncwarp();
+}
+template <int P, int Q, bool BLOCK_SYNC, class Lay>
+__device__ __forceinline__ void fft_pq_lift_inv(float2 (&v)[Q], float2* __restrict__ sm, const Lay lay, int t,
+                                                const float4* __restrict__ twPQ) {
+    static_assert(Q % P == 0, "Q must be a multiple of P");
+    constexpr int M = Q / P;
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+        float2 w[P];
+#pragma unroll
+        for (int s = 0; s < P; ++s) w[s] = v[i + M * s];
+        dft_lift_inv<P>(w);
+        const int u = t + P * i;
+#pragma unroll
+        for (int s = 0; s < P; ++s) sm[lay(u, s)] = w[s];
+    }
+    if (BLOCK_SYNC) __syncthreads(); else __syncwarp();
+#pragma unroll
+    for (int u = 0; u < Q; ++u) v[u] = sm[lay(u, t)];
+    if (BLOCK_SYNC) __syncthreads(); else __syncwarp();
+#pragma unroll
+    for (int u = 1; u < Q; ++u) v[u] = cmulc_df(v[u], twPQ[u * P + t]);
+    dft_lift_inv<Q>(v);
+}
+
+// ---------------------------------------------------------------------------
 // exp(2 pi i x) for a 64-bit fixed-point turn fraction x = X / 2^64, returned
 // as a double-float rotation {re_hi, im_hi, re_lo, im_lo} accurate to ~1e-12.
 // x = j/512 + r with |r| <= 1/1024: T[j] = exp(2 pi i j/512) from a

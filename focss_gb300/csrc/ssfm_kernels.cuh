@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(C* PQ<N1>::P, 2) col_kernel(const PassArgs a) 
             v[j] = lift_rot_inv(lift_rot_inv(quarter_turns(v[j], -(e >> qsh) & 3), s_hi[m >> sh]),
                                 s_lo[swz16(m & mask)]);
         }
-        fft_pq<P, Q, true, true>(v, sx, lay, t, s_fc);
+        fft_pq_lift_inv<P, Q, true>(v, sx, lay, t, s_fc);
     }
     if (op == COL_KERR) {
         // src/focss/solver/ssfm.cpp:160-164: A *= exp(i kappa gamma h |A|^2); the
@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(C* PQ<N1>::P, 2) col_kernel(const PassArgs a) 
         }
     }
     if (op == COL_FWD || op == COL_KERR) {
-        fft_pq<P, Q, false, true>(v, sx, lay, t, s_fc);
+        fft_pq_lift<P, Q, true>(v, sx, lay, t, s_fc);
 #pragma unroll
         for (int j = 0; j < Q; ++j) {
             const int e = n2 * (t + P * j), m = e & mmask;
