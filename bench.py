@@ -238,6 +238,7 @@ def run_ours(args):
 
     host = batch_inputs()
     B = host.shape[0]
+    split = fg.autotune(N, B, ctx=ctx)[0]
     dom = fg.Domain(1, N, DT, F0)
     pristine = fg.Field(dom, data=host, batch=B, ctx=ctx)
     field = fg.Field(dom, batch=B, ctx=ctx)
@@ -365,6 +366,7 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": t_max / max(1, args.steps), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": dict(W, batch=B, samples=N, l2="batch of 235 MB complex64 exceeds the 129 MB L2",
+                       fft_split="%d x %d (autotuned)" % (1 << split, N >> split),
                        parallelism="replicas" if world > 1 else "single GPU",
                        sample_steps_per_step=sample_steps / max(1, args.steps)),
         "roofline": roofline,
@@ -377,6 +379,8 @@ def run_ours(args):
         line["dbp"] = dbp_section(fg, ctx)
     if not args.no_sweep:
         line["sweep"] = sweep_section(fg, ctx, stream)
+    if not args.no_ppe:
+        line["ppe"] = ppe_section(fg, ctx, stream)
     if world == 1 and rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         n_steps = CPU_BASELINE_STEPS
@@ -411,12 +415,15 @@ def dbp_section(fg, ctx, power_dbm=2.0, batch=8):
     for k in (1, 2, 4, 100):
         q, ms = links.plain_dbp_q(link, rb, tb, k)
         out["plain"]["%d_steps_per_span" % k] = {"q_db": float(np.mean(q)), "ms": ms}
-    r = links.learned_dbp(link, ra, ta, rb, tb, steps_per_span=2, taps=63, mf_taps=63, iters=300, lr=3e-4,
-                          cnn_iters=300, cnn_lr=1e-3)
-    out["learned_2_steps_per_span"] = {"q_db": float(np.mean(r["q_learned"])), "ms": r["ms_learned"],
-                                       "q_db_at_init": float(np.mean(r["q_init"])), "train_s": r["train_s"]}
-    out["learned_2_steps_per_span_cnn"] = {"q_db": float(np.mean(r["q_learned_cnn"])), "ms": r["ms_learned_cnn"],
-                                           "train_s": r["cnn_train_s"]}
+    for k in (2, 4):
+        r = links.learned_dbp(link, ra, ta, rb, tb, steps_per_span=k, taps=63, mf_taps=255, iters=500, lr=3e-4,
+                              cnn_iters=300, cnn_lr=1e-3)
+        out["learned_%d_steps_per_span" % k] = {
+            "q_db": float(np.mean(r["q_learned"])), "ms": r["ms_learned"],
+            "q_db_at_init": float(np.mean(r["q_init"])), "train_s": r["train_s"],
+            "loss_first": r["loss_first"], "loss_last": r["loss_last"]}
+        out["learned_%d_steps_per_span_cnn" % k] = {
+            "q_db": float(np.mean(r["q_learned_cnn"])), "ms": r["ms_learned_cnn"], "train_s": r["cnn_train_s"]}
     return out
 
 
@@ -534,6 +541,80 @@ def sweep_section(fg, ctx, stream):
     }
 
 
+PPE = dict(
+    workload="ppe_16qam_32GBd_2^20sym_20x80km_ssmf_3dBm",
+    symbols=2 ** 20, realizations=4, samples_per_symbol=4, power_dbm=3.0, spans=20, span_m=80e3,
+    noise_figure_db=5.0, roll_off=0.1, forward="ADAPTIVE, max 0.005 rad/step, max 1 km",
+    sino_radius=32, prune=1e-3, train_symbols=2 ** 16, angle_steps=720, cut=100, seed=4,
+)
+
+
+def ppe_section(fg, ctx, stream):
+    """Perturbation (triplet) equalizer against 1- and 100-step/span DBP on
+    one single-channel link: 2^20 received 16QAM symbols (4 realizations of
+    2^18), 32 GBaud, 20 x 80 km SSMF with ASE at 3 dBm.  The coefficients
+    come from the SINO::train restatement on an independent training
+    realization (diamond |m|+|n| <= R, pruned below 1e-3 of the largest);
+    the equalizer runs on the CDC + matched-filter symbols."""
+    import torch
+    from focss_gb300 import dsp, sino
+    alpha, beta2, gamma = fiber_params()
+    c = PPE
+    fib = fg.Fiber(alpha, beta2, gamma, c["span_m"])
+    G = 10 ** (W["alpha_db_per_km"] * c["span_m"] / 1e3 / 10)
+    NF = 10 ** (c["noise_figure_db"] / 10)
+    osf, spans, ro = c["samples_per_symbol"], c["spans"], c["roll_off"]
+    p = np.sqrt(1e-3 * 10 ** (c["power_dbm"] / 10))
+    rng = np.random.default_rng(c["seed"])
+    ssfm = fg.SSFM(fib)
+    ssfm.set_grid(fg.SSFM.ADAPTIVE)
+    ssfm.set_maximum_phase_shift(W["max_phase_shift"])
+    ssfm.set_maximum_step_size(W["max_step_m"])
+
+    def link(ns, batch, seed):
+        codes = rng.integers(0, 16, (batch, 1, ns))
+        sym = dsp.qam16_map(codes, fg.Domain(1, ns, 1 / 32e9, F0), batch=batch, ctx=ctx)
+        sym *= p
+        sig = dsp.rrc_shaping(sym, osf, ro)
+        fg.span_loop([sig], fib, ssfm, spans, after=fg.Amplifier.AMPLIFY, amplifier=fg.Amplifier(G, NF, seed=seed))
+        return sym, sig
+
+    pse = dsp.PhaseShiftEqualizer(c["angle_steps"])
+
+    def cdc_symbols(sig):
+        f = sig.copy()
+        fg.cd_compensation(f, fib, spans)
+        return dsp.rrc_sampling(f, osf, ro)
+
+    # training realization and coefficient fit (host least squares)
+    tx_t, sig_t = link(c["train_symbols"], 1, 41)
+    y_t = pse.train_equalize(tx_t, cdc_symbols(sig_t))
+    t0 = time.perf_counter()
+    model = sino.SINO(c["sino_radius"], 0.0, sino.SinoType.ORDINARY).train(tx_t, y_t, solver="normal")
+    fit_s = time.perf_counter() - t0
+    m, n, cf = model.terms(c["prune"])
+
+    # test set: 2^20 symbols
+    ns = c["symbols"] // c["realizations"]
+    tx, sig = link(ns, c["realizations"], 42)
+    y = pse.train_equalize(tx, cdc_symbols(sig))
+    q_cdc = float(np.mean(dsp.q2_factor(tx, y, c["cut"])))
+    model.equalize(y, tx, c["prune"])  # warm-up
+    eq, ppe_ms = _stream_ms(torch, stream, lambda: model.equalize(y, tx, c["prune"]))
+    q_ppe = float(np.mean(dsp.q2_factor(tx, pse.train_equalize(tx, eq), c["cut"])))
+    out = {"config": c, "terms": int(m.size), "fit_s": fit_s, "q_db_cdc": q_cdc,
+           "ppe": {"q_db": q_ppe, "ms": ppe_ms, "msymbols_per_s": c["symbols"] / ppe_ms / 1e3,
+                   "gflops": 8.0 * m.size * c["symbols"] / ppe_ms / 1e6}}
+    rx2 = dsp.decimate(sig, osf // 2)
+    for k in (1, 100):
+        f = rx2.copy()
+        ctx.sync()
+        _, ms = _stream_ms(torch, stream, lambda: fg.backward_propagation(f, fib, fg.SSFM(fib, k), G, spans))
+        yk = pse.train_equalize(tx, dsp.rrc_sampling(f, 2, ro))
+        out["dbp_%d_steps_per_span" % k] = {"q_db": float(np.mean(dsp.q2_factor(tx, yk, c["cut"]))), "ms": ms}
+    return out
+
+
 def run_ncu_case(args):
     """Small case for ncu captures: UNIFORM split steps on 40 realizations of
     the N=2^19 WDM field (168 MB, above the L2 size), 4 steps."""
@@ -543,6 +624,8 @@ def run_ncu_case(args):
     fib = fg.Fiber(alpha, beta2, gamma, W["span_m"])
     x = (synth_wdm() * np.sqrt(1e-3)).astype(np.complex64)
     B = args.ncu_batch
+    if args.split:
+        fg.set_fft_split(N, args.split, ctx=ctx)
     f = fg.Field(fg.Domain(1, N, DT, F0), data=np.broadcast_to(x, (B, 1, N)), batch=B, ctx=ctx)
     fg.SSFM(fib, 4).run(f)
     ctx.sync()
@@ -554,6 +637,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ncu-case", action="store_true", help="small fixed case for ncu captures")
     ap.add_argument("--ncu-batch", type=int, default=40)
+    ap.add_argument("--split", type=int, default=0, help="ncu case: log2 N1 of the FFT split (0: balanced)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
@@ -561,6 +645,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-dbp", action="store_true", help="skip the learned-vs-plain DBP section")
     ap.add_argument("--no-sweep", action="store_true", help="skip the uneven-length batched sweep section")
+    ap.add_argument("--no-ppe", action="store_true", help="skip the perturbation-equalizer section")
     args = ap.parse_args()
     if args.ncu_case:
         return run_ncu_case(args)
