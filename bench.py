@@ -616,26 +616,69 @@ def ppe_section(fg, ctx, stream):
 
 
 def run_ncu_case(args):
-    """Small case for ncu captures: UNIFORM split steps on 40 realizations of
-    the N=2^19 WDM field (168 MB, above the L2 size), 4 steps."""
+    """Small fixed cases for ncu captures (one kernel family each):
+    ssfm  UNIFORM split steps on `--ncu-batch` realizations of the N=2^19 WDM
+          field (40 -> 168 MB, above the L2 size), 4 steps, then one EDFA;
+    ppe   triplet equalizer on 2^20 symbols (4 x 2^18), 2113 diamond terms
+          |m|+|n| <= 32 with decaying random coefficients;
+    ldbp  learned-DBP forward + backward, 20 spans x 2 steps, 63/255 taps,
+          8 x 2^16 samples;
+    cnn   correction-CNN forward + backward, 8 x 2^15 symbols."""
     import focss_gb300 as fg
+    from focss_gb300 import dsp
     ctx = fg.Context(0)
     alpha, beta2, gamma = fiber_params()
     fib = fg.Fiber(alpha, beta2, gamma, W["span_m"])
-    x = (synth_wdm() * np.sqrt(1e-3)).astype(np.complex64)
-    B = args.ncu_batch
-    if args.split:
-        fg.set_fft_split(N, args.split, ctx=ctx)
-    f = fg.Field(fg.Domain(1, N, DT, F0), data=np.broadcast_to(x, (B, 1, N)), batch=B, ctx=ctx)
-    fg.SSFM(fib, 4).run(f)
+    rng = np.random.default_rng(5)
+    kind = args.ncu_case
+    if kind == "ssfm":
+        x = (synth_wdm() * np.sqrt(1e-3)).astype(np.complex64)
+        B = args.ncu_batch
+        if args.split:
+            fg.set_fft_split(N, args.split, ctx=ctx)
+        f = fg.Field(fg.Domain(1, N, DT, F0), data=np.broadcast_to(x, (B, 1, N)), batch=B, ctx=ctx)
+        fg.SSFM(fib, 4).run(f)
+        fg.Amplifier(10 ** 1.6, 10 ** 0.5, seed=1).amplify(f)
+    elif kind == "ppe":
+        from focss_gb300 import sino
+        R, ns, B = 32, 2 ** 18, 4
+        y = dsp.qam16_map(rng.integers(0, 16, (B, 1, ns)), fg.Domain(1, ns, 1 / 32e9, F0), batch=B, ctx=ctx)
+        mm, nn = np.meshgrid(np.arange(-R, R + 1), np.arange(-R, R + 1), indexing="ij")
+        Wc = (rng.standard_normal(mm.shape) + 1j * rng.standard_normal(mm.shape)) * np.exp(-(abs(mm) + abs(nn)) / 8.0)
+        m, n, c = sino.diamond_terms(Wc * 1e-2, R, 1e-3)
+        for _ in range(2):
+            sino.triplet_apply(y, R, m, n, c)
+    elif kind == "ldbp":
+        from focss_gb300.ldbp import LearnedDBP, rrc_response
+        n2, B = 2 ** 16, 8
+        dt2 = 1 / 64e9
+        x = (rng.standard_normal((B, 1, n2)) + 1j * rng.standard_normal((B, 1, n2))) * 1e-2
+        rx = fg.Field(fg.Domain(1, n2, dt2, F0), data=x, batch=B, ctx=ctx)
+        tx = dsp.qam16_map(rng.integers(0, 16, (B, 1, n2 // 2)), fg.Domain(1, n2 // 2, 1 / 32e9, F0), batch=B,
+                           ctx=ctx)
+        model = LearnedDBP(20, 2, 63, 255, n2, B, 10 ** -0.8, ctx=ctx)
+        model.init_from_dbp(alpha, beta2, gamma, 1.0, W["span_m"], dt2, rrc_response(n2 // 2, 2, 0.1, ctx=ctx))
+        model.forward(rx)
+        model.loss_grad(rx, tx)
+    elif kind == "cnn":
+        from focss_gb300.cnn import CorrectionCNN, he_init
+        ns, B = 2 ** 15, 8
+        y = dsp.qam16_map(rng.integers(0, 16, (B, 1, ns)), fg.Domain(1, ns, 1 / 32e9, F0), batch=B, ctx=ctx)
+        net = CorrectionCNN(ns, B, 1.0, ctx=ctx)
+        net.set_params(he_init(rng))
+        net.forward(y)
+        net.loss_grad(y, y)
+    else:
+        raise SystemExit("unknown ncu case %r" % kind)
     ctx.sync()
-    print("ncu case done: %d x N=%d, 4 uniform steps" % (B, N))
+    print("ncu case %s done" % kind)
     return 0
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ncu-case", action="store_true", help="small fixed case for ncu captures")
+    ap.add_argument("--ncu-case", nargs="?", const="ssfm", default=None,
+                    help="small fixed case for ncu captures: ssfm (default), ppe, ldbp, cnn")
     ap.add_argument("--ncu-batch", type=int, default=40)
     ap.add_argument("--split", type=int, default=0, help="ncu case: log2 N1 of the FFT split (0: balanced)")
     ap.add_argument("--gpus", type=int, default=1)
