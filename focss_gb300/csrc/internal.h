@@ -64,6 +64,7 @@ struct PassArgs {
     SsfmParams prm;
     int N, N1, N2, log2N2;
     int batch;              // realizations (set by the launch helpers)
+    int modes;              // modes per realization of an SSFM run (0 or 1: single mode)
     int op;
     float scale;
     int bp_cut;

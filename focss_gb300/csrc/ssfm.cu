@@ -97,8 +97,9 @@ cudaError_t launch_col(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
     Launch& l = cache[p.log2N1];
     if (!l.fn) l = col_launch_for(p.log2N1);
     if (!l.fn) return cudaErrorInvalidValue;
+    const int modes = a.modes > 1 ? a.modes : 1;
     const size_t smem = sizeof(float4) * (size_t)p.N1 + sizeof(float2) * ((size_t)p.N1 / 4 + p.N2) +
-                        sizeof(float2) * (size_t)p.N1 * l.per_block;
+                        sizeof(float2) * (size_t)p.N1 * l.per_block * modes;
     cudaError_t e = prepare(l, smem);
     if (e != cudaSuccess) return e;
     a.N = p.N;
@@ -108,7 +109,7 @@ cudaError_t launch_col(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
     a.tw = p.tw;
     a.batch = batch;
     dim3 grid(p.N2 / l.per_block, batch);
-    l.fn<<<grid, l.threads, smem, s>>>(a);
+    l.fn<<<grid, l.threads * modes, smem, s>>>(a);
     count_launch();
     return cudaGetLastError();
 }
@@ -131,7 +132,7 @@ cudaError_t launch_row(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
     a.tw = p.tw;
     a.batch = batch;
     if (p.N1 % R != 0) return cudaErrorInvalidValue;
-    dim3 grid(p.N1 / R, batch);
+    dim3 grid(p.N1 / R, batch * (a.modes > 1 ? a.modes : 1));
     l.fn<<<grid, l.threads, smem, s>>>(a);
     count_launch();
     return cudaGetLastError();
@@ -167,8 +168,8 @@ void prof_collect(Ctx* ctx) {
 }  // namespace
 
 focss_status ssfm_validate(Ctx* ctx, const Field* f, const focss_fiber& fib, const focss_ssfm_opts& o) {
-    if (f->modes != 1)
-        return set_error(ctx, FOCSS_ERR_UNSUPPORTED, "ssfm_run: only single-mode fields are implemented");
+    if (f->modes != 1 && f->modes != 2)
+        return set_error(ctx, FOCSS_ERR_UNSUPPORTED, "ssfm_run: fields of 1 or 2 modes are implemented");
     if (!fft_size_supported(f->samples))
         return set_error(ctx, FOCSS_ERR_UNSUPPORTED,
                          "field length " + std::to_string(f->samples) + " is not a power of two in [2^8, 2^20]");
@@ -203,6 +204,7 @@ PassArgs ssfm_args(const Field* f, const focss_fiber& fib, const focss_ssfm_opts
     a.prm.total_steps = o.total_steps;
     a.prm.samples = N;
     a.prm.n_done = n_done;
+    a.modes = f->modes;
     return a;
 }
 

@@ -132,14 +132,19 @@ __device__ __noinline__ static void ssfm_advance(SsfmState& s, const SsfmParams&
 }
 
 // ---------------------------------------------------------------- column pass
+// A CTA holds the same C columns of every mode of one realization (a.modes
+// groups of C*P threads; 1 or 2 modes), so the Kerr phase can use the power
+// summed over modes (Field::power, src/focss/field.cpp:164-171).  The launch
+// bound (2 groups, 1 CTA) keeps the same 128-register budget as 1 group x 2 CTAs.
 template <int N1, int C>
-__global__ void __launch_bounds__(C* PQ<N1>::P, 2) col_kernel(const PassArgs a) {
+__global__ void __launch_bounds__(2 * C * PQ<N1>::P, 1) col_kernel(const PassArgs a) {
     constexpr int P = PQ<N1>::P, Q = PQ<N1>::Q;
     extern __shared__ float4 smem4[];
     float4* s_fc = smem4;                                  // column sub-FFT twiddles, (u,t) order
     float2* s_hi = reinterpret_cast<float2*>(s_fc + N1);   // six-step lifting pairs, W_N1^h, h < N1/4
     float2* s_lo = s_hi + N1 / 4;                          // six-step lifting pairs, W_N^l, swizzled
-    float2* sx = s_lo + a.N2;                              // N1*C exchange
+    const int mo = threadIdx.x / (C * P);                  // mode of this thread group
+    float2* sx = s_lo + a.N2 + (size_t)mo * N1 * C;        // N1*C exchange per mode
     __shared__ float red[64];
 
     const int b = blockIdx.y;
@@ -156,9 +161,10 @@ __global__ void __launch_bounds__(C* PQ<N1>::P, 2) col_kernel(const PassArgs a) 
     for (int i = threadIdx.x; i < N1 / 4; i += blockDim.x) s_hi[i] = tw_hi[i];
     for (int i = threadIdx.x; i < N2; i += blockDim.x) s_lo[i] = tw_lo[i];
 
-    const int c = threadIdx.x % C, t = threadIdx.x / C;
+    const int modes = a.modes > 1 ? a.modes : 1;
+    const int c = threadIdx.x % C, t = (threadIdx.x / C) % P;
     const int n2 = blockIdx.x * C + c;
-    float2* base = a.data + (size_t)b * a.N + n2;
+    float2* base = a.data + ((size_t)b * modes + mo) * a.N + n2;
     float2 v[Q];
 #pragma unroll
     for (int j = 0; j < Q; ++j) v[j] = base[(size_t)(t + P * j) * N2];
@@ -183,18 +189,53 @@ __global__ void __launch_bounds__(C* PQ<N1>::P, 2) col_kernel(const PassArgs a) 
         // src/focss/solver/ssfm.cpp:160-164: A *= exp(i kappa gamma h |A|^2); the
         // peak is taken from |A|^2 before the rotation (which preserves it).
         const float coef = (float)(a.prm.kappa * a.prm.gamma * st->h);
+        if (modes == 1) {
 #pragma unroll
-        for (int j = 0; j < Q; ++j) {
-            const float p = cnorm(v[j]);
-            v[j] = cmul(v[j], phase_rotation(coef * p));
-            pk = fmaxf(pk, p);
+            for (int j = 0; j < Q; ++j) {
+                const float p = cnorm(v[j]);
+                v[j] = cmul(v[j], phase_rotation(coef * p));
+                pk = fmaxf(pk, p);
+            }
+        } else {
+            // |A_0|^2 + |A_1|^2 through the (now free) exchange buffers
+            float* pw = reinterpret_cast<float*>(s_lo + a.N2);
+            const int stride = N1 * C;
+#pragma unroll
+            for (int j = 0; j < Q; ++j) pw[mo * stride + (t + P * j) * C + c] = cnorm(v[j]);
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < Q; ++j) {
+                const int i = (t + P * j) * C + c;
+                const float p = pw[i] + pw[stride + i];
+                v[j] = cmul(v[j], phase_rotation(coef * p));
+                pk = fmaxf(pk, p);
+            }
+            __syncthreads();  // the forward transform reuses the buffers
         }
     } else if (op == COL_FWD && st) {
+        if (modes == 1) {
 #pragma unroll
-        for (int j = 0; j < Q; ++j) {
-            const float p = cnorm(v[j]);
-            pk = fmaxf(pk, p);
-            sm += p;
+            for (int j = 0; j < Q; ++j) {
+                const float p = cnorm(v[j]);
+                pk = fmaxf(pk, p);
+                sm += p;
+            }
+        } else {
+            float* pw = reinterpret_cast<float*>(s_lo + a.N2);
+            const int stride = N1 * C;
+#pragma unroll
+            for (int j = 0; j < Q; ++j) {
+                const float p = cnorm(v[j]);
+                pw[mo * stride + (t + P * j) * C + c] = p;
+                sm += p;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < Q; ++j) {
+                const int i = (t + P * j) * C + c;
+                pk = fmaxf(pk, pw[i] + pw[stride + i]);
+            }
+            __syncthreads();
         }
     }
     if (op == COL_FWD || op == COL_KERR) {
@@ -240,8 +281,8 @@ __global__ void __launch_bounds__(R* PQ<N2>::P, 2) row_kernel(const PassArgs a) 
     float4* s_T = s_tw + N2;                                 // exp(2 pi i j/512)
     float2* sx = reinterpret_cast<float2*>(s_T + 512);       // R * Q * (P+1)
 
-    const int b = blockIdx.y;
-    const SsfmState* st = a.state ? a.state + b : nullptr;
+    const int b = blockIdx.y;  // realization * modes + mode
+    const SsfmState* st = a.state ? a.state + b / (a.modes > 1 ? a.modes : 1) : nullptr;
     unsigned long long dhi = 0ull, dlo = 0ull;
     float g = a.scale;
     if (st) {
