@@ -85,15 +85,6 @@ focss_status get_plan_split(Ctx* ctx, int N, int log2N1, const Plan** out) {
     };
     fill_pq(h.data(), p.N1);
     fill_pq(h.data() + p.N1, p.N2);
-    // six-step factors as lifting pairs {tan(theta/2), sin(theta)} (float2, packed)
-    auto lift = [&](long long e, long long L) {
-        const double th = -two_pi * (double)e / (double)L;
-        return make_float2((float)std::tan(0.5 * th), (float)std::sin(th));
-    };
-    float2* hi2 = reinterpret_cast<float2*>(h.data() + p.N1 + p.N2);
-    float2* lo2 = reinterpret_cast<float2*>(h.data() + 2 * p.N1 + p.N2);
-    for (int e = 0; e < p.N1 / 4; ++e) hi2[e] = lift(e, p.N1);
-    for (int e = 0; e < p.N2; ++e) lo2[swz16(e)] = lift(e, N);
     for (int j = 0; j < 512; ++j)
         h[2 * p.N1 + 2 * p.N2 + j] = df(std::cos(two_pi * j / 512), std::sin(two_pi * j / 512));
     cudaError_t e = cudaMalloc(&p.tw, sizeof(float4) * h.size());

@@ -177,6 +177,18 @@ __device__ __forceinline__ float2 lift_rot_inv(float2 v, float2 ts) {
     x = fmaf(ts.x, y, x);
     return make_float2(x, y);
 }
+// W_N^e = exp(-2 pi i e/N) = (-i)^q rot(theta), q = round(4e/N), |theta| <= pi/4,
+// for 0 <= e < N = 2^log2N: {tan(theta/2), sin(theta), q (int bits), 0}.  The
+// residual turn fraction is exact, so the pair is a deterministic function of
+// (e, N): a rotation applied in one launch is undone exactly in another.
+__device__ __forceinline__ float4 sixstep_factor(int e, int log2N) {
+    const int q = ((e << 2) + (1 << (log2N - 1))) >> log2N;
+    const float r = (float)(e - (q << (log2N - 2))) * __int_as_float((127 - log2N) << 23);
+    float sp, cp;
+    sincospif(r, &sp, &cp);  // sin, cos of pi*r;  theta = -2 pi r
+    return make_float4(-sp / cp, -2.0f * sp * cp, __int_as_float(q & 3), 0.0f);
+}
+
 // v * (-i)^q (exact).
 __device__ __forceinline__ float2 quarter_turns(float2 v, int q) {
     const float2 r = (q & 1) ? make_float2(v.y, -v.x) : v;

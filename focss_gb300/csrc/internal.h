@@ -51,10 +51,9 @@ struct SsfmParams {
 // device buffer (offsets in entries):
 //   0            column sub-FFT table, entry u*P+t = W_N1^{t u}   (N1 entries)
 //   N1           row sub-FFT table,    entry u*P+t = W_N2^{t u}   (N2 entries)
-//   N1+N2        six-step high factor  W_N1^h, h < N1/4, as float2 lifting
-//                pairs {tan(theta/2), sin(theta)} packed two per entry
-//   2N1+N2       six-step low factor   W_N^l, l < N2, float2 lifting pairs
-//                at swz16(l), packed two per entry
+//   N1+N2        reserved (N1 entries; the column pass computes its six-step
+//                factors on the device, sixstep_factor in fft.cuh)
+//   2N1+N2       reserved (N2 entries)
 //   2N1+2N2      exp(+2 pi i j/512), j < 512                      (512 entries)
 struct PassArgs {
     float2* data;           // batch x N complex64

@@ -64,13 +64,6 @@ __device__ __forceinline__ float4 df_rotation(double turns_times_2) {
     return make_float4(ch, sh, (float)(c - (double)ch), (float)(s - (double)sh));
 }
 
-// Lifting pair {tan(theta/2), sin(theta)} of theta = pi * turns_times_2.
-__device__ __forceinline__ float2 lift_pair(double turns_times_2) {
-    double sh, ch;
-    sincospi(0.5 * turns_times_2, &sh, &ch);
-    return make_float2((float)(sh / ch), (float)sinpi(turns_times_2));
-}
-
 __host__ __device__ __forceinline__ int group_p(int L) { return L <= 32 ? 4 : L <= 128 ? 8 : L <= 512 ? 16 : 32; }
 
 // The plan tables of internal.h, computed on the device in FP64.
@@ -83,12 +76,8 @@ __global__ void noalloc_tables_kernel(float4* __restrict__ tw, int N, int N1, in
             const int P = group_p(L);
             const long long e = (long long)(k % P) * (k / P) % L;
             tw[i] = df_rotation(-2.0 * (double)e / L);
-        } else if (i < 2 * N1 + N2) {
-            const int h = i - N1 - N2;
-            if (h < N1 / 4) reinterpret_cast<float2*>(tw + N1 + N2)[h] = lift_pair(-2.0 * (double)h / N1);
         } else if (i < 2 * N1 + 2 * N2) {
-            const int l = i - 2 * N1 - N2;
-            reinterpret_cast<float2*>(tw + 2 * N1 + N2)[swz16(l)] = lift_pair(-2.0 * (double)l / N);
+            tw[i] = make_float4(0.f, 0.f, 0.f, 0.f);  // reserved
         } else {
             const int j = i - 2 * N1 - 2 * N2;
             tw[i] = df_rotation(2.0 * (double)j / 512);

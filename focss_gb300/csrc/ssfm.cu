@@ -98,7 +98,9 @@ cudaError_t launch_col(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
     if (!l.fn) l = col_launch_for(p.log2N1);
     if (!l.fn) return cudaErrorInvalidValue;
     const int modes = a.modes > 1 ? a.modes : 1;
-    const size_t smem = sizeof(float4) * (size_t)p.N1 + sizeof(float2) * ((size_t)p.N1 / 4 + p.N2) +
+    // s_fc (N1) + six-step table (Q x C, Q = N1/P) + exchange (N1 x C per mode)
+    const int P = l.threads / l.per_block;
+    const size_t smem = sizeof(float4) * ((size_t)p.N1 + (size_t)(p.N1 / P) * l.per_block) +
                         sizeof(float2) * (size_t)p.N1 * l.per_block * modes;
     cudaError_t e = prepare(l, smem);
     if (e != cudaSuccess) return e;

@@ -141,10 +141,10 @@ __global__ void __launch_bounds__(2 * C * PQ<N1>::P, 1) col_kernel(const PassArg
     constexpr int P = PQ<N1>::P, Q = PQ<N1>::Q;
     extern __shared__ float4 smem4[];
     float4* s_fc = smem4;                                  // column sub-FFT twiddles, (u,t) order
-    float2* s_hi = reinterpret_cast<float2*>(s_fc + N1);   // six-step lifting pairs, W_N1^h, h < N1/4
-    float2* s_lo = s_hi + N1 / 4;                          // six-step lifting pairs, W_N^l, swizzled
+    float4* s_B = s_fc + N1;                               // six-step factors W_N^{n2 P j}, [j][c]
+    float2* s_x0 = reinterpret_cast<float2*>(s_B + Q * C); // exchange buffers, N1*C per mode
     const int mo = threadIdx.x / (C * P);                  // mode of this thread group
-    float2* sx = s_lo + a.N2 + (size_t)mo * N1 * C;        // N1*C exchange per mode
+    float2* sx = s_x0 + (size_t)mo * N1 * C;
     __shared__ float red[64];
 
     const int b = blockIdx.y;
@@ -155,15 +155,21 @@ __global__ void __launch_bounds__(2 * C * PQ<N1>::P, 1) col_kernel(const PassArg
         if (op == COL_IDLE) return;
     }
     const int N2 = a.N2;
-    const float2* tw_hi = reinterpret_cast<const float2*>(a.tw + N1 + N2);
-    const float2* tw_lo = reinterpret_cast<const float2*>(a.tw + 2 * N1 + N2);
+    // Six-step twiddle of column n2, row k1 = t + P j:  W_N^{n2 k1} =
+    // W_N^{n2 t} (per thread) x W_N^{n2 P j} (per CTA table over j and the C
+    // columns), each a quarter turn times a lifting rotation whose inverse
+    // mirrors it exactly.
+    const int log2N = a.log2N2 + ilog2c(N1);
     for (int i = threadIdx.x; i < N1; i += blockDim.x) s_fc[i] = a.tw[i];
-    for (int i = threadIdx.x; i < N1 / 4; i += blockDim.x) s_hi[i] = tw_hi[i];
-    for (int i = threadIdx.x; i < N2; i += blockDim.x) s_lo[i] = tw_lo[i];
+    for (int i = threadIdx.x; i < Q * C; i += blockDim.x)
+        s_B[i] = sixstep_factor((blockIdx.x * C + i % C) * P * (i / C), log2N);
 
     const int modes = a.modes > 1 ? a.modes : 1;
     const int c = threadIdx.x % C, t = (threadIdx.x / C) % P;
     const int n2 = blockIdx.x * C + c;
+    const float4 fa = sixstep_factor(n2 * t, log2N);
+    const float2 tsA = make_float2(fa.x, fa.y);
+    const int qA = __float_as_int(fa.z);
     float2* base = a.data + ((size_t)b * modes + mo) * a.N + n2;
     float2 v[Q];
 #pragma unroll
@@ -171,17 +177,14 @@ __global__ void __launch_bounds__(2 * C * PQ<N1>::P, 1) col_kernel(const PassArg
     __syncthreads();
 
     const ColLayout<P, C> lay{c};
-    // Six-step twiddle W_N^e, e = n2*k1 = q*N/4 + h*N2 + l:  (-i)^q W_N1^h W_N^l,
-    // the last two as lifting rotations (|angles| < pi/2) whose inverses
-    // mirror them exactly.
-    const int mask = N2 - 1, sh = a.log2N2, qsh = a.log2N2 + ilog2c(N1) - 2, mmask = (1 << qsh) - 1;
     float pk = 0.0f, sm = 0.0f;
     if (op != COL_FWD) {
 #pragma unroll
         for (int j = 0; j < Q; ++j) {
-            const int e = n2 * (t + P * j), m = e & mmask;
-            v[j] = lift_rot_inv(lift_rot_inv(quarter_turns(v[j], -(e >> qsh) & 3), s_hi[m >> sh]),
-                                s_lo[swz16(m & mask)]);
+            const float4 fb = s_B[j * C + c];
+            v[j] = lift_rot_inv(lift_rot_inv(quarter_turns(v[j], -(qA + __float_as_int(fb.z)) & 3),
+                                             make_float2(fb.x, fb.y)),
+                                tsA);
         }
         fft_pq_lift_inv<P, Q, true>(v, sx, lay, t, s_fc);
     }
@@ -198,7 +201,7 @@ __global__ void __launch_bounds__(2 * C * PQ<N1>::P, 1) col_kernel(const PassArg
             }
         } else {
             // |A_0|^2 + |A_1|^2 through the (now free) exchange buffers
-            float* pw = reinterpret_cast<float*>(s_lo + a.N2);
+            float* pw = reinterpret_cast<float*>(s_x0);
             const int stride = N1 * C;
 #pragma unroll
             for (int j = 0; j < Q; ++j) pw[mo * stride + (t + P * j) * C + c] = cnorm(v[j]);
@@ -221,7 +224,7 @@ __global__ void __launch_bounds__(2 * C * PQ<N1>::P, 1) col_kernel(const PassArg
                 sm += p;
             }
         } else {
-            float* pw = reinterpret_cast<float*>(s_lo + a.N2);
+            float* pw = reinterpret_cast<float*>(s_x0);
             const int stride = N1 * C;
 #pragma unroll
             for (int j = 0; j < Q; ++j) {
@@ -242,8 +245,8 @@ __global__ void __launch_bounds__(2 * C * PQ<N1>::P, 1) col_kernel(const PassArg
         fft_pq_lift<P, Q, true>(v, sx, lay, t, s_fc);
 #pragma unroll
         for (int j = 0; j < Q; ++j) {
-            const int e = n2 * (t + P * j), m = e & mmask;
-            v[j] = quarter_turns(lift_rot(lift_rot(v[j], s_lo[swz16(m & mask)]), s_hi[m >> sh]), e >> qsh);
+            const float4 fb = s_B[j * C + c];
+            v[j] = quarter_turns(lift_rot(lift_rot(v[j], tsA), make_float2(fb.x, fb.y)), qA + __float_as_int(fb.z));
         }
     }
 #pragma unroll
