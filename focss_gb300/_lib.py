@@ -88,6 +88,7 @@ SIGNATURES = {
     "focss_wdm_select": (I, [P, P, I, D, P]),
     "focss_wdm_mux": (I, [P, P, D, P]),
     "focss_hard_decision": (I, [P, P, P]),
+    "focss_soft_decision": (I, [P, P, D, P]),
     "focss_hd_codes": (I, [P, P, P]),
     "focss_error_counts": (I, [P, P, P, I, P, P]),
     "focss_bit_error_rate": (I, [P, P, P, I, P]),

@@ -213,6 +213,27 @@ __global__ void hard_decision_kernel(const float2* __restrict__ in, float2* __re
     }
 }
 
+// soft_decision_16qam (modulation.cpp:122-146): per quadrature the hard
+// decision, unless the normalized received value lies within
+// sqrt(10)*uncertainty of a decision boundary (0, +-2/sqrt(10)); then it is kept.
+__global__ void soft_decision_kernel(const float2* __restrict__ in, float2* __restrict__ out, int modes, int samples,
+                                     size_t per, int batch, const double* __restrict__ psum, double uncertainty) {
+    const double s10 = 1.0 / sqrt(10.0);
+    const double pivot = 2.0 / sqrt(10.0), thr = sqrt(10.0) * uncertainty;
+    const size_t n = per * batch;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int b = (int)(i / per);
+        const double power = psum[b] / samples / modes;
+        const double sp = sqrt(power);
+        const double re = (double)in[i].x / sp, im = (double)in[i].y / sp;
+        const unsigned c = demod16(re, im);
+        double gr = c_gray_re[c] * s10, gi = c_gray_im[c] * s10;
+        if (fabs(re) < thr || fabs(re - pivot) < thr || fabs(re + pivot) < thr) gr = re;
+        if (fabs(im) < thr || fabs(im - pivot) < thr || fabs(im + pivot) < thr) gi = im;
+        out[i] = make_float2((float)(sp * gr), (float)(sp * gi));
+    }
+}
+
 // hd_sequence_16qam (modulation.cpp:148-156): scale = sqrt(modes / average_power).
 __global__ void hd_codes_kernel(const float2* __restrict__ in, int32_t* __restrict__ codes, int modes, int samples,
                                 size_t per, int batch, const double* __restrict__ psum) {
@@ -605,6 +626,18 @@ FOCSS_API focss_status focss_hard_decision(focss_ctx* c, const focss_field* in, 
     const size_t per = (size_t)in->modes * in->samples;
     FG_LAUNCH(fg::hard_decision_kernel<<<fg::grid_for(in->n(), 256), 256, 0, c->stream>>>(in->d, out->d, in->modes, in->samples, per, in->batch, c->d_red));
     return fg::cuda_check(c, cudaGetLastError(), "hard_decision");
+}
+
+FOCSS_API focss_status focss_soft_decision(focss_ctx* c, const focss_field* in, double uncertainty,
+                                           focss_field* out) {
+    if (!c || !in || !out || !(uncertainty >= 0)) return FOCSS_ERR_INVALID_ARG;
+    focss_status st = fg::check_same(c, in, out);
+    if (st == FOCSS_OK) st = fg::ensure_red(c, (size_t)in->batch);
+    if (st == FOCSS_OK) st = fg::power_sums(c, in, c->d_red);
+    if (st != FOCSS_OK) return st;
+    const size_t per = (size_t)in->modes * in->samples;
+    FG_LAUNCH(fg::soft_decision_kernel<<<fg::grid_for(in->n(), 256), 256, 0, c->stream>>>(in->d, out->d, in->modes, in->samples, per, in->batch, c->d_red, uncertainty));
+    return fg::cuda_check(c, cudaGetLastError(), "soft_decision");
 }
 
 FOCSS_API focss_status focss_hd_codes(focss_ctx* c, const focss_field* in, int32_t* codes) {

@@ -114,6 +114,13 @@ def hard_decision_16qam(f: Field) -> Field:
     return out
 
 
+def soft_decision_16qam(f: Field, uncertainty: float) -> Field:
+    """soft_decision_16qam (src/focss/processing/modulation.cpp:122-146)."""
+    out = _like(f)
+    check(lib().focss_soft_decision(f.ctx.h, f.h, float(uncertainty), out.h), f.ctx.h)
+    return out
+
+
 def hd_sequence_16qam(f: Field):
     codes = np.zeros(f.shape, np.int32)
     check(lib().focss_hd_codes(f.ctx.h, f.h, _vp(codes)), f.ctx.h)

@@ -257,6 +257,12 @@ FOCSS_API focss_status focss_wdm_mux(focss_ctx* ctx, const focss_field* channels
 
 /* hard_decision_16qam (src/focss/processing/modulation.cpp:112-120). */
 FOCSS_API focss_status focss_hard_decision(focss_ctx* ctx, const focss_field* in, focss_field* out);
+/* soft_decision_16qam (src/focss/processing/modulation.cpp:122-146): the
+ * hard decision per quadrature, except where the received value normalized by
+ * sqrt(average power / modes) lies within sqrt(10)*uncertainty of a decision
+ * boundary (0, +-2/sqrt(10)); there the received value is kept. */
+FOCSS_API focss_status focss_soft_decision(focss_ctx* ctx, const focss_field* in, double uncertainty,
+                                          focss_field* out);
 /* hd_sequence_16qam (src/focss/processing/modulation.cpp:148-156): codes is a
  * host int32 array of batch*modes*samples. */
 FOCSS_API focss_status focss_hd_codes(focss_ctx* ctx, const focss_field* in, int32_t* codes);

@@ -543,6 +543,11 @@ inline Field hard_decision_16qam(const Field& signal) {
     detail::check(focss_hard_decision(gpu_context(), signal.handle(), out.mut()), gpu_context());
     return out;
 }
+inline Field soft_decision_16qam(const Field& signal, const double& uncertainty) {
+    Field out(signal.domain(), signal.batch());
+    detail::check(focss_soft_decision(gpu_context(), signal.handle(), uncertainty, out.mut()), gpu_context());
+    return out;
+}
 inline Vector<int> hd_sequence_16qam(const Field& signal) {
     Vector<std::int32_t> c((size_t)signal.batch() * signal.size());
     detail::check(focss_hd_codes(gpu_context(), signal.handle(), c.data()), gpu_context());

@@ -60,6 +60,7 @@ def lib():
             "ofc_demodulate16": (C.c_uint32, [D, D]),
             "ofc_hd_sequence": (None, [I, I, P, P]),
             "ofc_hard_decision": (None, [I, I, P, P]),
+            "ofc_soft_decision": (None, [I, I, P, D, P]),
             "ofc_error_counts": (None, [I, I, P, P, I, P, P]),
             "ofc_bit_error_rate": (D, [I, I, P, P, I]),
             "ofc_symbol_error_rate": (D, [I, I, P, P, I]),
@@ -268,6 +269,13 @@ def hard_decision(a):
     m, n = _shape(a)
     out = np.zeros(a.shape, np.complex128)
     lib().ofc_hard_decision(m, n, _ptr(a), _ptr(out))
+    return out
+
+def soft_decision(a, uncertainty):
+    a = _c128(a)
+    m, n = _shape(a)
+    out = np.zeros_like(a)
+    lib().ofc_soft_decision(m, n, _ptr(a), uncertainty, _ptr(out))
     return out
 
 

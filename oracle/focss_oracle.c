@@ -580,6 +580,27 @@ void ofc_hard_decision(int modes, int samples, const double* a, double* out) {
     }
 }
 
+void ofc_soft_decision(int modes, int samples, const double* a, double uncertainty, double* out) {
+    /* modulation.cpp:122-146: hard decision per quadrature unless the received
+     * value lies within sqrt(10)*uncertainty of a decision boundary (0, +-2/sqrt(10)),
+     * in which case the received value is kept */
+    double t[32];
+    ofc_gray16(t);
+    double power = ofc_average_power(modes, samples, a) / modes;
+    double sp = sqrt(power);
+    double pivot = 2.0 / sqrt(10);
+    double threshold = sqrt(10) * uncertainty;
+    for (size_t i = 0; i < (size_t)modes * samples; ++i) {
+        double re = a[2 * i] / sp, im = a[2 * i + 1] / sp;
+        uint32_t c = ofc_demodulate16(re, im);
+        double gr = t[2 * c], gi = t[2 * c + 1];
+        if (fabs(re) < threshold || fabs(re - pivot) < threshold || fabs(re + pivot) < threshold) gr = re;
+        if (fabs(im) < threshold || fabs(im - pivot) < threshold || fabs(im + pivot) < threshold) gi = im;
+        out[2 * i] = sp * gr;
+        out[2 * i + 1] = sp * gi;
+    }
+}
+
 static int popcount4(uint32_t d) {
     int n = 0;
     while (d) {

@@ -56,6 +56,7 @@ def lib():
             "ref_rrc_sampling_rolloff": (None, [I, I, D, P, I, D, D, P]),
             "ref_demodulate16": (U, [D, D]),
             "ref_hard_decision": (None, [I, I, P, P]),
+            "ref_soft_decision": (None, [I, I, P, D, P]),
             "ref_ber": (D, [I, I, P, P, I]),
             "ref_ser": (D, [I, I, P, P, I]),
             "ref_q2": (D, [I, I, P, P, I]),
@@ -180,6 +181,11 @@ def demodulate16(z): return int(lib().ref_demodulate16(float(np.real(z)), float(
 def hard_decision(a):
     a = _c(a); m, n = _shape(a); o = np.zeros(a.shape, np.complex128)
     lib().ref_hard_decision(m, n, _p(a), _p(o)); return o
+
+
+def soft_decision(a, uncertainty):
+    a = _c(a); m, n = _shape(a); o = np.zeros(a.shape, np.complex128)
+    lib().ref_soft_decision(m, n, _p(a), uncertainty, _p(o)); return o
 
 
 def ber(tx, rx, cut=-1):

@@ -167,6 +167,9 @@ unsigned ref_demodulate16(double re, double im) { return demodulate_16qam(comple
 void ref_hard_decision(int modes, int samples, const double* data, double* out) {
     store(hard_decision_16qam(make_field(modes, samples, 1.0, 0, data)), out);
 }
+void ref_soft_decision(int modes, int samples, const double* data, double uncertainty, double* out) {
+    store(soft_decision_16qam(make_field(modes, samples, 1.0, 0, data), uncertainty), out);
+}
 
 double ref_ber(int modes, int samples, const double* tx, const double* rx, int cut) {
     Field t = make_field(modes, samples, 1.0, 0, tx);

@@ -109,6 +109,8 @@ def main():
     noisy = noisy * 1.7 * np.exp(0.3j)
     g["rx_noisy"] = noisy
     g["hd_out"] = ref.hard_decision(noisy)
+    g["sd_out_005"] = ref.soft_decision(noisy, 0.05)
+    g["sd_out_002"] = ref.soft_decision(noisy, 0.02)
     g["demod_codes"] = np.array([ref.demodulate16(z / np.sqrt(np.mean(np.abs(noisy) ** 2))) for z in noisy],
                                 np.int32)
     rx_eq = noisy / 1.7 * np.exp(-0.3j)

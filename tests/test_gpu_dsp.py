@@ -72,6 +72,8 @@ def test_decisions_and_metrics(ctx, golden):
     sym, noisy, rx = golden["qam_symbols"], golden["rx_noisy"], golden["rx_eq"]
     n = fld(noisy, 1.0, ctx)
     assert rel_l2(dsp.hard_decision_16qam(n).numpy()[0, 0], golden["hd_out"]) < 1e-7
+    for u, key in ((0.05, "sd_out_005"), (0.02, "sd_out_002")):
+        assert rel_l2(dsp.soft_decision_16qam(n, u).numpy()[0, 0], golden[key]) < 1e-7
     np.testing.assert_array_equal(dsp.hd_sequence_16qam(n)[0, 0], golden["demod_codes"])
     t, r = fld(sym, 1.0, ctx), fld(rx, 1.0, ctx)
     assert dsp.bit_error_rate_16qam(t, r, -1)[0] == golden["ber_nocut"][0]

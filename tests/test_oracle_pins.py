@@ -84,6 +84,8 @@ def test_decisions_and_metrics(golden, oracle_cpu):
     cpu = oracle_cpu
     sym, noisy, rx = golden["qam_symbols"], golden["rx_noisy"], golden["rx_eq"]
     assert rel_l2(cpu.hard_decision(noisy), golden["hd_out"]) < 1e-15
+    assert rel_l2(cpu.soft_decision(noisy, 0.05), golden["sd_out_005"]) < 1e-15
+    assert rel_l2(cpu.soft_decision(noisy, 0.02), golden["sd_out_002"]) < 1e-15
     np.testing.assert_array_equal(cpu.hd_sequence(noisy), golden["demod_codes"])
     assert cpu.bit_error_rate(sym, rx, 0) == golden["ber_nocut"][0]
     assert cpu.bit_error_rate(sym, rx, 7) == golden["ber_cut7"][0]
