@@ -11,6 +11,8 @@
  *                                    src/focss/processing/modulation.h:8-45
  *   PhaseShiftEqualizer, ScalarEqualizer
  *                                    src/focss/equalizer/linear.h
+ *   save/load_transmission           src/focss/functions.cpp:174-221
+ *   save_field / load_field          src/tasks/wdm_run.cpp:55-77, wdm_scoring.cpp:79-103
  * so that callers such as src/tasks/systems.cpp compile against it unchanged
  * (include/focss_compat/ maps the reference's header names onto this file).
  *
@@ -39,6 +41,9 @@
 #include <complex>
 #include <cstdint>
 #include <cstdlib>
+#include <fstream>
+#include <istream>
+#include <ostream>
 #include <random>
 #include <stdexcept>
 #include <string>
@@ -596,6 +601,86 @@ inline Field wdm_mux(const Vector<Field>& channels, const double& channel_bandwi
 inline Vector<Field> wdm_demux(const Field& field, const int& n_channels, const double& channel_bandwidth) {
     Vector<Field> out;
     for (int ch = 0; ch < n_channels; ++ch) out.push_back(wdm_select(field, ch - n_channels / 2, channel_bandwidth));
+    return out;
+}
+
+/* ------------------------------------------------------------- dataset I/O */
+/* Transmission CSV of src/focss/functions.cpp:174-221: per sample the tx
+ * modes then the rx modes as re,im pairs (realization 0 of each field). */
+inline void save_transmission(std::ostream& output, const Field& tx, const Field& rx) {
+    if (tx.modes() != rx.modes() || tx.samples() != rx.samples())
+        throw gpu_error(FOCSS_ERR_INVALID_ARG, "focss: save_transmission of fields of different shapes");
+    const int M = tx.modes();
+    for (int i = 0; i < tx.samples(); ++i) {
+        for (int m = 0; m < M; ++m) output << tx(m, i).real() << ',' << tx(m, i).imag() << ',';
+        for (int m = 0; m < M; ++m) {
+            output << rx(m, i).real() << ',' << rx(m, i).imag();
+            output << (m + 1 < M ? ',' : '\n');
+        }
+    }
+}
+inline void load_transmission(std::istream& input, Field* tx, Field* rx) {
+    if (tx->modes() != rx->modes() || tx->samples() != rx->samples())
+        throw gpu_error(FOCSS_ERR_INVALID_ARG, "focss: load_transmission into fields of different shapes");
+    double re, im;
+    char delimiter = ',';
+    for (int i = 0; i < tx->samples(); ++i) {
+        for (int m = 0; m < tx->modes(); ++m) {
+            if (m) input >> delimiter;
+            input >> re >> delimiter >> im;
+            (*tx)(m, i) = complex_t(re, im);
+        }
+        for (int m = 0; m < rx->modes(); ++m) {
+            input >> delimiter >> re >> delimiter >> im;
+            (*rx)(m, i) = complex_t(re, im);
+        }
+    }
+}
+inline void save_transmission(const std::string& filename, const Field& tx, const Field& rx) {
+    std::ofstream file(filename);
+    file.precision(15);
+    save_transmission(file, tx, rx);
+}
+inline void load_transmission(const std::string& filename, Field* tx, Field* rx) {
+    std::ifstream file(filename);
+    load_transmission(file, tx, rx);
+}
+
+/* Field binary of src/tasks/wdm_run.cpp:55-77 (written) and
+ * src/tasks/wdm_scoring.cpp:79-103 (read): ints n_ch, n_samples, n_modes,
+ * flags = 0, then sample-major, channel, mode complex<double> values. */
+inline void save_field(const Vector<Field>& data, const std::string& set, const std::string& tag,
+                       const int& index) {
+    std::ofstream file(set + "/" + tag + "/" + std::to_string(index) + ".bin", std::ios::binary);
+    const int hdr[4] = {(int)data.size(), data.empty() ? 0 : data[0].samples(), data.empty() ? 0 : data[0].modes(), 0};
+    file.write(reinterpret_cast<const char*>(hdr), sizeof hdr);
+    for (int s = 0; s < hdr[1]; ++s)
+        for (int ch = 0; ch < hdr[0]; ++ch)
+            for (int m = 0; m < hdr[2]; ++m) {
+                const complex_t v = data[(size_t)ch](m, s);
+                file.write(reinterpret_cast<const char*>(&v), sizeof v);
+            }
+}
+/* The channels back as fields of `domain` (modes and samples from the file). */
+inline Vector<Field> load_field(const std::string& set, const std::string& tag, const int& index,
+                                Domain domain) {
+    std::ifstream file(set + "/" + tag + "/" + std::to_string(index) + ".bin", std::ios::binary);
+    int hdr[4] = {0, 0, 0, 0};
+    file.read(reinterpret_cast<char*>(hdr), sizeof hdr);
+    if (!file) throw gpu_error(FOCSS_ERR_INVALID_ARG, "focss: cannot read field file header");
+    domain.samples = hdr[1];
+    domain.modes = hdr[2];
+    Vector<ComplexVector> ch((size_t)hdr[0], ComplexVector((size_t)hdr[1] * hdr[2]));
+    for (int s = 0; s < hdr[1]; ++s)
+        for (int c = 0; c < hdr[0]; ++c)
+            for (int m = 0; m < hdr[2]; ++m) {
+                complex_t v;
+                file.read(reinterpret_cast<char*>(&v), sizeof v);
+                ch[(size_t)c][(size_t)m * hdr[1] + s] = v;
+            }
+    if (!file) throw gpu_error(FOCSS_ERR_INVALID_ARG, "focss: truncated field file");
+    Vector<Field> out;
+    for (auto& d : ch) out.emplace_back(domain, d);
     return out;
 }
 

@@ -57,6 +57,8 @@ def lib():
             "ref_demodulate16": (U, [D, D]),
             "ref_hard_decision": (None, [I, I, P, P]),
             "ref_soft_decision": (None, [I, I, P, D, P]),
+            "ref_save_transmission": (None, [I, I, P, P, C.c_char_p]),
+            "ref_load_transmission": (None, [I, I, C.c_char_p, P, P]),
             "ref_ber": (D, [I, I, P, P, I]),
             "ref_ser": (D, [I, I, P, P, I]),
             "ref_q2": (D, [I, I, P, P, I]),
@@ -230,3 +232,17 @@ def wdm_mux(channels, dt, bw):
 
 def soliton(dark, points, z):
     o = np.zeros(points, np.complex128); lib().ref_soliton(1 if dark else 0, points, z, _p(o)); return o
+
+
+def save_transmission(path, tx, rx):
+    """The reference's own save_transmission (functions.cpp:174-208) on (modes, samples) arrays."""
+    tx, rx = _c(tx), _c(rx)
+    m, n = _shape(tx)
+    lib().ref_save_transmission(m, n, _p(tx), _p(rx), str(path).encode())
+
+
+def load_transmission(path, modes, samples):
+    tx = np.zeros((modes, samples), np.complex128)
+    rx = np.zeros((modes, samples), np.complex128)
+    lib().ref_load_transmission(modes, samples, str(path).encode(), _p(tx), _p(rx))
+    return tx, rx

@@ -8,6 +8,7 @@
  * committed under tests/golden/.  The product never links it.
  */
 #include <cstring>
+#include <string>
 #include <random>
 
 #include "focss/definitions.h"
@@ -167,6 +168,17 @@ unsigned ref_demodulate16(double re, double im) { return demodulate_16qam(comple
 void ref_hard_decision(int modes, int samples, const double* data, double* out) {
     store(hard_decision_16qam(make_field(modes, samples, 1.0, 0, data)), out);
 }
+void ref_save_transmission(int modes, int samples, const double* tx, const double* rx, const char* path) {
+    save_transmission(std::string(path), make_field(modes, samples, 1.0, 0, tx), make_field(modes, samples, 1.0, 0, rx));
+}
+
+void ref_load_transmission(int modes, int samples, const char* path, double* tx, double* rx) {
+    Field t(Domain{modes, samples, 1.0, 0}), r(Domain{modes, samples, 1.0, 0});
+    load_transmission(std::string(path), &t, &r);
+    store(t, tx);
+    store(r, rx);
+}
+
 void ref_soft_decision(int modes, int samples, const double* data, double uncertainty, double* out) {
     store(soft_decision_16qam(make_field(modes, samples, 1.0, 0, data), uncertainty), out);
 }

@@ -144,6 +144,13 @@ def main():
     g["sech_1024_z0"] = ref.soliton(False, 1024, 0.0)
     g["sech_1024_z1"] = ref.soliton(False, 1024, 1.0)
 
+    # --- dataset file written by the reference's own save_transmission (functions.cpp:174-208)
+    io_rng = np.random.default_rng(31)
+    scale = 10.0 ** io_rng.integers(-7, 2, (2, 40))
+    g["io_tx"] = (io_rng.standard_normal((2, 40)) + 1j * io_rng.standard_normal((2, 40))) * scale
+    g["io_rx"] = (io_rng.standard_normal((2, 40)) + 1j * io_rng.standard_normal((2, 40))) * scale
+    ref.save_transmission(os.path.join(OUT, "transmission_ref.csv"), g["io_tx"], g["io_rx"])
+
     np.savez_compressed(os.path.join(OUT, "reference_golden.npz"), **g)
     print("wrote", len(g), "arrays")
 
