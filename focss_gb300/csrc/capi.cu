@@ -78,13 +78,13 @@ focss_status get_plan_split(Ctx* ctx, int N, int log2N1, const Plan** out) {
     auto w = [&](long long e, long long L) { return df(std::cos(two_pi * e / L), -std::sin(two_pi * e / L)); };
     // Threads per group of a length-L sub-FFT (must match PQ<L>::P in fft.cuh).
     auto groupP = [](int L) { return L <= 32 ? 4 : L <= 128 ? 8 : L <= 512 ? 16 : 32; };
-    auto fill_pq = [&](float4* dst, int L) {
-        const int P = groupP(L), Q = L / P;
+    auto fill_pq = [&](float4* dst, int L, int P) {
+        const int Q = L / P;
         for (int u = 0; u < Q; ++u)
             for (int t = 0; t < P; ++t) dst[u * P + t] = w((long long)t * u % L, L);
     };
-    fill_pq(h.data(), p.N1);
-    fill_pq(h.data() + p.N1, p.N2);
+    fill_pq(h.data(), p.N1, col_group_p(p.N1));
+    fill_pq(h.data() + p.N1, p.N2, groupP(p.N2));
     for (int j = 0; j < 512; ++j)
         h[2 * p.N1 + 2 * p.N2 + j] = df(std::cos(two_pi * j / 512), std::sin(two_pi * j / 512));
     cudaError_t e = cudaMalloc(&p.tw, sizeof(float4) * h.size());

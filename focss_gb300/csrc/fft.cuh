@@ -357,6 +357,80 @@ __device__ __forceinline__ void fft_pq_lift_inv(float2 (&v)[Q], float2* __restri
 }
 
 // ---------------------------------------------------------------------------
+// Column sub-FFT with half the registers: L = 2 Q^2 on P = 2Q threads of Q
+// elements (L = 32, 128, 512).  Thread t holds x[t + P j]; after an in-register
+// Q-point DFT over j, the twiddle W_L^{t u} and one exchange, lane pair
+// (u = t >> 1, h = t & 1) holds the even (h = 0) or odd (h = 1) half of the
+// P-point DFT over t for row u, transforms it in registers and finishes with
+// one radix-2 butterfly across the pair (__shfl_xor, the partner lane differs
+// by `pair_xor`).  Output: thread t holds X[k1], k1 = (t>>1) + Q k + Q^2 (t&1).
+// The inverse mirrors the forward operation by operation (lifting rotations).
+template <int Q, bool BLOCK_SYNC, class Lay>
+__device__ __forceinline__ void fft_p2q_lift(float2 (&v)[Q], float2* __restrict__ sm, const Lay lay, int t,
+                                             const float4* __restrict__ twPQ, int pair_xor) {
+    constexpr int P = 2 * Q;
+    dft_lift<Q>(v);
+#pragma unroll
+    for (int u = 1; u < Q; ++u) v[u] = cmul_df(v[u], twPQ[u * P + t]);
+#pragma unroll
+    for (int u = 0; u < Q; ++u) sm[lay(u, t)] = v[u];
+    if (BLOCK_SYNC) __syncthreads(); else __syncwarp();
+    const int u = t >> 1, h = t & 1;
+#pragma unroll
+    for (int s = 0; s < Q; ++s) v[s] = sm[lay(u, h + 2 * s)];
+    if (BLOCK_SYNC) __syncthreads(); else __syncwarp();
+    dft_lift<Q>(v);
+    const float sg = h ? -1.0f : 1.0f;
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        // h = 0: Z = Y0 + W Y1;  h = 1: Z = Y0 - W Y1, W = W_P^k
+        const float2 tw = twlift(v[k], k * (32 / Q));
+        const float2 mine = h ? tw : v[k];
+        const float ox = __shfl_xor_sync(0xffffffffu, mine.x, pair_xor);
+        const float oy = __shfl_xor_sync(0xffffffffu, mine.y, pair_xor);
+        v[k] = make_float2(fmaf(sg, mine.x, ox), fmaf(sg, mine.y, oy));
+    }
+}
+template <int Q, bool BLOCK_SYNC, class Lay>
+__device__ __forceinline__ void fft_p2q_lift_inv(float2 (&v)[Q], float2* __restrict__ sm, const Lay lay, int t,
+                                                 const float4* __restrict__ twPQ, int pair_xor) {
+    constexpr int P = 2 * Q;
+    const int u = t >> 1, h = t & 1;
+    const float sg = h ? -1.0f : 1.0f;
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        // h = 0: 2 Y0 = Z0 + Z1;  h = 1: 2 Y1 = W^-1 (Z0 - Z1)
+        const float ox = __shfl_xor_sync(0xffffffffu, v[k].x, pair_xor);
+        const float oy = __shfl_xor_sync(0xffffffffu, v[k].y, pair_xor);
+        const float2 sd = make_float2(fmaf(sg, v[k].x, ox), fmaf(sg, v[k].y, oy));
+        const float2 tw = twlift_inv(sd, k * (32 / Q));
+        v[k] = h ? tw : sd;
+    }
+    dft_lift_inv<Q>(v);
+#pragma unroll
+    for (int s = 0; s < Q; ++s) sm[lay(u, h + 2 * s)] = v[s];
+    if (BLOCK_SYNC) __syncthreads(); else __syncwarp();
+#pragma unroll
+    for (int w = 0; w < Q; ++w) v[w] = sm[lay(w, t)];
+    if (BLOCK_SYNC) __syncthreads(); else __syncwarp();
+#pragma unroll
+    for (int w = 1; w < Q; ++w) v[w] = cmulc_df(v[w], twPQ[w * P + t]);
+    dft_lift_inv<Q>(v);
+}
+
+// Column-pass sub-FFT shape: lane-pair form (P = 2Q) where L = 2 Q^2, else PQ.
+template <int L>
+struct ColFFT {
+    static constexpr bool PAIR = (L == 32 || L == 128 || L == 512);
+    static constexpr int Q = PAIR ? (L == 32 ? 4 : L == 128 ? 8 : 16) : PQ<L>::Q;
+    static constexpr int P = L / Q;
+};
+// Threads per group of the column pass for length L (host side of ColFFT).
+__host__ __device__ __forceinline__ int col_group_p(int L) {
+    return L == 32 ? 8 : L == 128 ? 16 : L == 512 ? 32 : (L <= 32 ? 4 : L <= 128 ? 8 : L <= 512 ? 16 : 32);
+}
+
+// ---------------------------------------------------------------------------
 // exp(2 pi i x) for a 64-bit fixed-point turn fraction x = X / 2^64, returned
 // as a double-float rotation {re_hi, im_hi, re_lo, im_lo} accurate to ~1e-12.
 // x = j/512 + r with |r| <= 1/1024: T[j] = exp(2 pi i j/512) from a

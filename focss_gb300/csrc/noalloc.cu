@@ -73,7 +73,7 @@ __global__ void noalloc_tables_kernel(float4* __restrict__ tw, int N, int N1, in
         if (i < N1 + N2) {
             const int L = i < N1 ? N1 : N2;
             const int k = i < N1 ? i : i - N1;
-            const int P = group_p(L);
+            const int P = i < N1 ? col_group_p(L) : group_p(L);
             const long long e = (long long)(k % P) * (k / P) % L;
             tw[i] = df_rotation(-2.0 * (double)e / L);
         } else if (i < 2 * N1 + 2 * N2) {

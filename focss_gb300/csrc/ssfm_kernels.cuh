@@ -137,8 +137,9 @@ __device__ __noinline__ static void ssfm_advance(SsfmState& s, const SsfmParams&
 // summed over modes (Field::power, src/focss/field.cpp:164-171).  The launch
 // bound (2 groups, 1 CTA) keeps the same 128-register budget as 1 group x 2 CTAs.
 template <int N1, int C>
-__global__ void __launch_bounds__(2 * C * PQ<N1>::P, 1) col_kernel(const PassArgs a) {
-    constexpr int P = PQ<N1>::P, Q = PQ<N1>::Q;
+__global__ void __launch_bounds__(2 * C * ColFFT<N1>::P, 1) col_kernel(const PassArgs a) {
+    constexpr int P = ColFFT<N1>::P, Q = ColFFT<N1>::Q;
+    constexpr bool PAIR = ColFFT<N1>::PAIR;
     extern __shared__ float4 smem4[];
     float4* s_fc = smem4;                                  // column sub-FFT twiddles, (u,t) order
     float4* s_B = s_fc + N1;                               // six-step factors W_N^{n2 P j}, [j][c]
@@ -155,25 +156,29 @@ __global__ void __launch_bounds__(2 * C * PQ<N1>::P, 1) col_kernel(const PassArg
         if (op == COL_IDLE) return;
     }
     const int N2 = a.N2;
-    // Six-step twiddle of column n2, row k1 = t + P j:  W_N^{n2 k1} =
-    // W_N^{n2 t} (per thread) x W_N^{n2 P j} (per CTA table over j and the C
-    // columns), each a quarter turn times a lifting rotation whose inverse
-    // mirrors it exactly.
+    // Element j of a thread is time-domain row t + P j; in the spectral
+    // layout it is row a0 + a1 j (a0 = t, a1 = P for the PQ form; lane-pair
+    // form: a0 = (t>>1) + Q^2 (t&1), a1 = Q).  Six-step twiddle of column n2:
+    // W_N^{n2 (a0 + a1 j)} = W_N^{n2 a0} (per thread) x W_N^{n2 a1 j} (per CTA
+    // table over j and the C columns), each a quarter turn times a lifting
+    // rotation whose inverse mirrors it exactly.
+    constexpr int a1 = PAIR ? Q : P;
     const int log2N = a.log2N2 + ilog2c(N1);
     for (int i = threadIdx.x; i < N1; i += blockDim.x) s_fc[i] = a.tw[i];
     for (int i = threadIdx.x; i < Q * C; i += blockDim.x)
-        s_B[i] = sixstep_factor((blockIdx.x * C + i % C) * P * (i / C), log2N);
+        s_B[i] = sixstep_factor((blockIdx.x * C + i % C) * a1 * (i / C), log2N);
 
     const int modes = a.modes > 1 ? a.modes : 1;
     const int c = threadIdx.x % C, t = (threadIdx.x / C) % P;
+    const int a0 = PAIR ? (t >> 1) + Q * Q * (t & 1) : t;
     const int n2 = blockIdx.x * C + c;
-    const float4 fa = sixstep_factor(n2 * t, log2N);
+    const float4 fa = sixstep_factor(n2 * a0, log2N);
     const float2 tsA = make_float2(fa.x, fa.y);
     const int qA = __float_as_int(fa.z);
     float2* base = a.data + ((size_t)b * modes + mo) * a.N + n2;
     float2 v[Q];
 #pragma unroll
-    for (int j = 0; j < Q; ++j) v[j] = base[(size_t)(t + P * j) * N2];
+    for (int j = 0; j < Q; ++j) v[j] = base[(size_t)(op == COL_FWD ? t + P * j : a0 + a1 * j) * N2];
     __syncthreads();
 
     const ColLayout<P, C> lay{c};
@@ -186,7 +191,10 @@ __global__ void __launch_bounds__(2 * C * PQ<N1>::P, 1) col_kernel(const PassArg
                                              make_float2(fb.x, fb.y)),
                                 tsA);
         }
-        fft_pq_lift_inv<P, Q, true>(v, sx, lay, t, s_fc);
+        if constexpr (PAIR)
+            fft_p2q_lift_inv<Q, true>(v, sx, lay, t, s_fc, C);
+        else
+            fft_pq_lift_inv<P, Q, true>(v, sx, lay, t, s_fc);
     }
     if (op == COL_KERR) {
         // src/focss/solver/ssfm.cpp:160-164: A *= exp(i kappa gamma h |A|^2); the
@@ -242,7 +250,10 @@ __global__ void __launch_bounds__(2 * C * PQ<N1>::P, 1) col_kernel(const PassArg
         }
     }
     if (op == COL_FWD || op == COL_KERR) {
-        fft_pq_lift<P, Q, true>(v, sx, lay, t, s_fc);
+        if constexpr (PAIR)
+            fft_p2q_lift<Q, true>(v, sx, lay, t, s_fc, C);
+        else
+            fft_pq_lift<P, Q, true>(v, sx, lay, t, s_fc);
 #pragma unroll
         for (int j = 0; j < Q; ++j) {
             const float4 fb = s_B[j * C + c];
@@ -250,7 +261,7 @@ __global__ void __launch_bounds__(2 * C * PQ<N1>::P, 1) col_kernel(const PassArg
         }
     }
 #pragma unroll
-    for (int j = 0; j < Q; ++j) base[(size_t)(t + P * j) * N2] = v[j];
+    for (int j = 0; j < Q; ++j) base[(size_t)(op == COL_INV ? t + P * j : a0 + a1 * j) * N2] = v[j];
 
     if (st) {
         block_max_sum(pk, sm, red);
@@ -372,7 +383,7 @@ Launch row_launch_for(int log2N2);
     Launch col_launch_##LG() {                                                 \
         Launch l;                                                              \
         l.fn = col_kernel<L, ColShape<L>::C>;                                  \
-        l.threads = ColShape<L>::C * PQ<L>::P;                                 \
+        l.threads = ColShape<L>::C * ColFFT<L>::P;                             \
         l.per_block = ColShape<L>::C;                                          \
         return l;                                                              \
     }                                                                          \
