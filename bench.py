@@ -245,12 +245,18 @@ def run_ours(args):
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
 
     def propagate(f, seed):
-        steps = 0
-        amp = fg.Amplifier(G, NF, seed=seed)
-        for s in range(W["spans"]):
-            steps += int(ssfm.run(f, fg.SSFM.FORWARD).sum())
-            amp.amplify(f, counter=s)
-        return steps
+        # forward_propagation (systems.cpp:39-56): the 20 spans (ADAPTIVE SSFM,
+        # then EDFA with ASE) as one graph-captured span loop (focss_span_loop)
+        if args.host_loop:
+            steps = 0
+            amp = fg.Amplifier(G, NF, seed=seed)
+            for s in range(W["spans"]):
+                steps += int(ssfm.run(f, fg.SSFM.FORWARD).sum())
+                amp.amplify(f, counter=s)
+            return steps
+        st = fg.span_loop([f], fib, ssfm, W["spans"], after=fg.Amplifier.AMPLIFY,
+                          amplifier=fg.Amplifier(G, NF, seed=seed))
+        return int(st[0].sum())
 
     def barrier():
         if dist is not None:
@@ -689,6 +695,8 @@ def main():
     ap.add_argument("--no-dbp", action="store_true", help="skip the learned-vs-plain DBP section")
     ap.add_argument("--no-sweep", action="store_true", help="skip the uneven-length batched sweep section")
     ap.add_argument("--no-ppe", action="store_true", help="skip the perturbation-equalizer section")
+    ap.add_argument("--host-loop", action="store_true",
+                    help="drive the spans from the host (one SSFM run + EDFA per span) instead of one graph")
     args = ap.parse_args()
     if args.ncu_case:
         return run_ncu_case(args)
