@@ -551,7 +551,8 @@ PPE = dict(
     workload="ppe_16qam_32GBd_2^20sym_20x80km_ssmf_3dBm",
     symbols=2 ** 20, realizations=4, samples_per_symbol=4, power_dbm=3.0, spans=20, span_m=80e3,
     noise_figure_db=5.0, roll_off=0.1, forward="ADAPTIVE, max 0.005 rad/step, max 1 km",
-    sino_radius=32, prune=1e-3, train_symbols=2 ** 16, angle_steps=720, cut=100, seed=4,
+    sino_radius=75, prune=1e-3, train_symbols=2 ** 16, fit="normal equations on the GPU, FP64 solve",
+    angle_steps=720, cut=100, seed=4,
 )
 
 
@@ -559,9 +560,10 @@ def ppe_section(fg, ctx, stream):
     """Perturbation (triplet) equalizer against 1- and 100-step/span DBP on
     one single-channel link: 2^20 received 16QAM symbols (4 realizations of
     2^18), 32 GBaud, 20 x 80 km SSMF with ASE at 3 dBm.  The coefficients
-    come from the SINO::train restatement on an independent training
-    realization (diamond |m|+|n| <= R, pruned below 1e-3 of the largest);
-    the equalizer runs on the CDC + matched-filter symbols."""
+    come from SINO::train on an independent training realization (normal
+    equations formed on the GPU, R = 75 diamond |m|+|n| <= R, 2889 features),
+    pruned below 1e-3 of the largest; the equalizer runs on the CDC +
+    matched-filter symbols."""
     import torch
     from focss_gb300 import dsp, sino
     alpha, beta2, gamma = fiber_params()
@@ -596,7 +598,7 @@ def ppe_section(fg, ctx, stream):
     tx_t, sig_t = link(c["train_symbols"], 1, 41)
     y_t = pse.train_equalize(tx_t, cdc_symbols(sig_t))
     t0 = time.perf_counter()
-    model = sino.SINO(c["sino_radius"], 0.0, sino.SinoType.ORDINARY).train(tx_t, y_t, solver="normal")
+    model = sino.SINO(c["sino_radius"], 0.0, sino.SinoType.ORDINARY).train(tx_t, y_t, solver="gpu")
     fit_s = time.perf_counter() - t0
     m, n, cf = model.terms(c["prune"])
 

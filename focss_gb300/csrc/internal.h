@@ -31,7 +31,7 @@ struct SsfmState {
     int steps;                     // steps done (ADAPTIVE, reference counting)
     unsigned int peak_bits;        // atomicMax accumulator of the peak power (float bits)
     unsigned int blocks_done;      // last-block ticket
-    int pad_;
+    float kerr_coef;               // (float)(kappa*gamma*h) of the next nonlinear step
 };
 
 enum ColOp : int { COL_FWD = 0, COL_KERR = 1, COL_INV = 2, COL_IDLE = 3 };

@@ -129,6 +129,7 @@ __device__ __noinline__ static void ssfm_advance(SsfmState& s, const SsfmParams&
     s.gain_ratio = s.gain_ratio * g / (double)g32;
     s.lin_gain = g32;
     s.row_active = 1;
+    s.kerr_coef = (float)(p.kappa * p.gamma * s.h);
 }
 
 // ---------------------------------------------------------------- column pass
@@ -199,7 +200,7 @@ __global__ void __launch_bounds__(2 * C * ColFFT<N1>::P, 1) col_kernel(const Pas
     if (op == COL_KERR) {
         // src/focss/solver/ssfm.cpp:160-164: A *= exp(i kappa gamma h |A|^2); the
         // peak is taken from |A|^2 before the rotation (which preserves it).
-        const float coef = (float)(a.prm.kappa * a.prm.gamma * st->h);
+        const float coef = st->kerr_coef;
         if (modes == 1) {
 #pragma unroll
             for (int j = 0; j < Q; ++j) {

@@ -109,8 +109,36 @@ class SINO:
         self.trained = True
         return self
 
-    # ---- sino.cpp:42-159, restated with numpy (host)
+    # ---- sino.cpp:42-159 with the normal equations formed on the GPU
+    def _train_gpu(self, transmitted, received):
+        from .api import Domain
+        if not isinstance(transmitted, Field):
+            t = np.atleast_2d(np.asarray(transmitted, np.complex128))
+            r = np.atleast_2d(np.asarray(received, np.complex128))
+            transmitted = Field(Domain(t.shape[0], t.shape[1], 1.0), data=t[None])
+            received = Field(Domain(r.shape[0], r.shape[1], 1.0), data=r[None], ctx=transmitted.ctx)
+        R = self.radius
+        nf = int(lib().focss_sino_num_features(R, int(self.type)))
+        gram = np.zeros((nf + 1, nf + 1), np.complex128)
+        mean = np.zeros(nf + 1, np.complex128)
+        sd = np.zeros(nf, np.float64)
+        lw = complex(self.linear_weight)
+        check(lib().focss_sino_gram(transmitted.ctx.h, transmitted.h, received.h, R, int(self.type), lw.real, lw.imag,
+                                    gram.ctypes.data_as(C.c_void_p), mean.ctypes.data_as(C.c_void_p),
+                                    sd.ctypes.data_as(C.c_void_p)), transmitted.ctx.h)
+        Gu = np.triu(gram)
+        G = Gu + np.conj(np.triu(Gu, 1)).T          # Hermitian from the upper triangle
+        raw = np.linalg.solve(G[:nf, :nf], G[:nf, nf])
+        raw = raw / sd
+        x_mean, y_mean = mean[:nf], mean[nf]
+        return raw, x_mean, y_mean
+
+    # ---- sino.cpp:42-159, restated with numpy (host), or solver="gpu"
     def train(self, transmitted, received, solver="lstsq"):
+        if solver == "gpu":
+            raw, x_mean, y_mean = self._train_gpu(transmitted, received)
+            self.intercept = y_mean - np.sum(raw * x_mean)
+            return self._install(raw)
         tx = np.atleast_2d(np.asarray(transmitted.numpy()[0] if isinstance(transmitted, Field) else transmitted))
         rx = np.atleast_2d(np.asarray(received.numpy()[0] if isinstance(received, Field) else received))
         R = self.radius
@@ -153,6 +181,17 @@ class SINO:
             raw = np.linalg.lstsq(Z, resp, rcond=None)[0]
         raw = raw / x_std
         self.intercept = y_mean - np.sum(raw * x_mean)
+        return self._install(raw)
+
+    def _pairs(self):
+        R = self.radius
+        mb = R // 2
+        return [(m, n) for m in range(-mb, mb + 1) for n in range(abs(m), R - abs(m) + 1)]
+
+    def _install(self, raw):
+        """Weights matrix from the raw feature weights (sino.cpp:126-153)."""
+        R = self.radius
+        pairs = self._pairs()
         W = np.zeros((2 * R + 1, 2 * R + 1), np.complex128)
         for i, (m, n) in enumerate(pairs):
             w = raw[i]

@@ -309,6 +309,21 @@ FOCSS_API focss_status focss_sino_equalize(focss_ctx* ctx, const focss_field* rx
                                            int n_terms, const int32_t* m, const int32_t* n, const double* coef,
                                            double linear_weight_re, double linear_weight_im, focss_field* out);
 
+/* Normal equations of SINO::train (src/focss/equalizer/sino.cpp:42-159) on the
+ * device: the symmetry-reduced triplet features of tx (|m| <= R/2,
+ * |m| <= n <= R-|m|, plus tx itself for type 0 = ORDINARY) over the samples
+ * [R, N-R) of every mode, z-scored per feature (mean, standard deviation
+ * normalized by the count), and the responses rx (type 1 = FIXED: rx - lw*tx;
+ * type 2 = HOMOGENEOUS: rx) centred, appended as column nf.  Outputs:
+ * gram = [Z y]^H [Z y] accumulated in FP64, (nf+1) x (nf+1) complex
+ * (interleaved FP64) row-major, upper triangle valid; mean = nf+1 complex means (interleaved FP64, the last one the
+ * responses'); sd = nf standard deviations.  nf = focss_sino_num_features.
+ * tx and rx: single realizations of one domain.  The caller solves
+ * gram[:nf,:nf] w = gram[:nf,nf] (FP64) and unscales as sino.cpp:122-153. */
+FOCSS_API int focss_sino_num_features(int radius, int type);
+FOCSS_API focss_status focss_sino_gram(focss_ctx* ctx, const focss_field* tx, const focss_field* rx, int radius,
+                                       int type, double lw_re, double lw_im, double* gram, double* mean, double* sd);
+
 /* ---------------------------------------------------------- learned DBP */
 /* No reference counterpart: a few-step learned replacement of
  * backward_propagation (src/tasks/systems.cpp:73-91).  Per realization (one
