@@ -479,4 +479,30 @@ __device__ __forceinline__ float4 turns_rotation_df(unsigned long long X, const 
     return make_float4(re_hi, im_hi, re_lo, im_lo);
 }
 
+// v * exp(2 pi i x), x = X / 2^64 as in turns_rotation_df, applied to the data
+// in two steps: w = v * T[j] (double-float table entry, compensated product),
+// then w + w * (cos(theta) - 1 + i sin(theta)) for the residual |theta| <=
+// pi/512, whose angle is carried as the exact split th + tl.  Every constant
+// stays at ~48 bits; the intermediate w adds one data rounding.
+__device__ __forceinline__ float2 turns_rotate(float2 v, unsigned long long X, const float4* __restrict__ T512) {
+    const unsigned long long Y = X + (1ull << 54);
+    const unsigned yh = (unsigned)(Y >> 32);
+    const int j = (int)((yh >> 23) & 511u);
+    const unsigned A = yh & 0x7FFFFFu;
+    const unsigned B = (unsigned)(Y >> 9) & 0x7FFFFFu;
+    const float fA = u23_to_float(A) - 4194304.0f;
+    const float fB = u23_to_float(B);
+    const float c32_hi = 1.462918119976564e-09f, c32_lo = -4.070940267922164e-17f;
+    const float c9 = 1.7439342975337076e-16f;
+    const float th = fA * c32_hi;
+    const float tl = fmaf(fA, c32_hi, -th) + fmaf(fA, c32_lo, fB * c9);
+    const float th2 = th * th;
+    const float sl = fmaf(-th2 * th, 1.0f / 6.0f, tl);                             // sin = th + sl
+    const float cm1 = fmaf(th2 * th2, 1.0f / 24.0f, fmaf(-0.5f, th2, -th * tl));  // cos - 1
+    const float2 w = cmul_df(v, T512[j]);
+    const float re = w.x + fmaf(-w.y, th, fmaf(w.x, cm1, -(w.y * sl)));
+    const float im = w.y + fmaf(w.x, th, fmaf(w.y, cm1, w.x * sl));
+    return make_float2(re, im);
+}
+
 }  // namespace fg

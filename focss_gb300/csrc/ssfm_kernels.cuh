@@ -329,8 +329,7 @@ __global__ void __launch_bounds__(R* PQ<N2>::P, 2) row_kernel(const PassArgs a) 
             const unsigned long long kp = (unsigned long long)(k <= (N >> 1) ? k : N - k);
             const unsigned long long kk = kp * kp;
             const unsigned long long X = dhi * kk + __umul64hi(dlo, kk);
-            const float4 rot = turns_rotation_df(X, s_T);
-            v[j] = cmul_df(cscale(v[j], g), rot);
+            v[j] = turns_rotate(cscale(v[j], g), X, s_T);
         }
     } else if (op == ROW_TABLE) {
         const float2* tb = a.table + (size_t)k1 * N2 + t;
