@@ -89,6 +89,8 @@ SIGNATURES = {
     "focss_wdm_mux": (I, [P, P, D, P]),
     "focss_hard_decision": (I, [P, P, P]),
     "focss_soft_decision": (I, [P, P, D, P]),
+    "focss_find_certainty": (I, [P, P, P, P]),
+    "focss_certainty_decision": (I, [P, P, D, P]),
     "focss_hd_codes": (I, [P, P, P]),
     "focss_error_counts": (I, [P, P, P, I, P, P]),
     "focss_bit_error_rate": (I, [P, P, P, I, P]),

@@ -234,6 +234,50 @@ __global__ void soft_decision_kernel(const float2* __restrict__ in, float2* __re
     }
 }
 
+// find_certainty (src/tasks/wdm_scoring.cpp:105-126), device part: per
+// realization the smallest |gray[rx_code] / scale - rx| over samples whose
+// decision differs from the transmitted one, scale = sqrt(n) / ||tx||_F.
+// Distances are non-negative doubles, so their bit patterns order like the
+// values and atomicMin on them is a min over doubles.
+__global__ void certainty_kernel(const float2* __restrict__ tx, const float2* __restrict__ rx, size_t per,
+                                 const double* __restrict__ psum_tx, unsigned long long* __restrict__ dmin) {
+    const int b = blockIdx.y;
+    const double scale = sqrt((double)per) / sqrt(psum_tx[b]);
+    const double s10 = 1.0 / sqrt(10.0);
+    double best = __longlong_as_double(0x7FF0000000000000LL);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < per; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t k = (size_t)b * per + i;
+        const double rr = rx[k].x, ri = rx[k].y;
+        const unsigned tc = demod16(scale * tx[k].x, scale * tx[k].y);
+        const unsigned rc = demod16(scale * rr, scale * ri);
+        if (tc ^ rc) best = fmin(best, hypot(c_gray_re[rc] * s10 / scale - rr, c_gray_im[rc] * s10 / scale - ri));
+    }
+    for (int o = 16; o > 0; o >>= 1) best = fmin(best, __shfl_xor_sync(0xffffffffu, best, o));
+    if ((threadIdx.x & 31) == 0 && best < __longlong_as_double(0x7FF0000000000000LL))
+        atomicMin(dmin + b, (unsigned long long)__double_as_longlong(best));
+}
+
+// sd (src/tasks/wdm_scoring.cpp:128-144): at the RMS amplitude amp, a sample
+// snaps to its decided point when closer than certainty / sqrt(5).
+__global__ void certainty_decision_kernel(const float2* __restrict__ in, float2* __restrict__ out, size_t per,
+                                          int batch, const double* __restrict__ psum, double certainty) {
+    const double s10 = 1.0 / sqrt(10.0);
+    const double thr = certainty / sqrt(5.0);
+    const size_t n = per * batch;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int b = (int)(i / per);
+        const double amp = sqrt(psum[b]) / sqrt((double)per);
+        double re = (double)in[i].x / amp, im = (double)in[i].y / amp;
+        const unsigned c = demod16(re, im);
+        const double gr = c_gray_re[c] * s10, gi = c_gray_im[c] * s10;
+        if (hypot(gr - re, gi - im) < thr) {
+            re = gr;
+            im = gi;
+        }
+        out[i] = make_float2((float)(amp * re), (float)(amp * im));
+    }
+}
+
 // hd_sequence_16qam (modulation.cpp:148-156): scale = sqrt(modes / average_power).
 __global__ void hd_codes_kernel(const float2* __restrict__ in, int32_t* __restrict__ codes, int modes, int samples,
                                 size_t per, int batch, const double* __restrict__ psum) {
@@ -638,6 +682,51 @@ FOCSS_API focss_status focss_soft_decision(focss_ctx* c, const focss_field* in, 
     const size_t per = (size_t)in->modes * in->samples;
     FG_LAUNCH(fg::soft_decision_kernel<<<fg::grid_for(in->n(), 256), 256, 0, c->stream>>>(in->d, out->d, in->modes, in->samples, per, in->batch, c->d_red, uncertainty));
     return fg::cuda_check(c, cudaGetLastError(), "soft_decision");
+}
+
+FOCSS_API focss_status focss_find_certainty(focss_ctx* c, const focss_field* tx, const focss_field* rx,
+                                           double* certainty) {
+    if (!c || !tx || !rx || !certainty) return FOCSS_ERR_INVALID_ARG;
+    focss_status st = fg::check_same(c, tx, rx);
+    if (st == FOCSS_OK) st = fg::ensure_red(c, 2 * (size_t)tx->batch);
+    if (st == FOCSS_OK) st = fg::power_sums(c, tx, c->d_red);
+    if (st != FOCSS_OK) return st;
+    const int B = tx->batch;
+    const size_t per = (size_t)tx->modes * tx->samples;
+    unsigned long long* dmin = (unsigned long long*)(c->d_red + B);
+    std::vector<unsigned long long> inf(B, 0x7FF0000000000000ull);
+    cudaError_t e = cudaMemcpyAsync(dmin, inf.data(), sizeof(unsigned long long) * B, cudaMemcpyHostToDevice, c->stream);
+    const int gx = std::max(1, std::min(64, (int)((per + 1023) / 1024)));
+    if (e == cudaSuccess)
+        FG_LAUNCH(fg::certainty_kernel<<<dim3(gx, B), 256, 0, c->stream>>>(tx->d, rx->d, per, c->d_red, dmin));
+    if (e == cudaSuccess) e = cudaGetLastError();
+    std::vector<double> host(2 * (size_t)B);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(host.data(), c->d_red, sizeof(double) * 2 * B, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return fg::cuda_check(c, e, "find_certainty");
+    for (int b = 0; b < B; ++b) {
+        // wdm_scoring.cpp:107-125, same expression order
+        const double scale = std::sqrt((double)per) / std::sqrt(host[b]);
+        double threshold = 1.0 / std::sqrt(5.0) / scale;
+        double d;
+        std::memcpy(&d, &host[B + b], sizeof(double));
+        if (threshold > d) threshold = d;
+        certainty[b] = std::sqrt(5.0) * scale * threshold;
+    }
+    return FOCSS_OK;
+}
+
+FOCSS_API focss_status focss_certainty_decision(focss_ctx* c, const focss_field* in, double certainty,
+                                               focss_field* out) {
+    if (!c || !in || !out || !(certainty >= 0)) return FOCSS_ERR_INVALID_ARG;
+    focss_status st = fg::check_same(c, in, out);
+    if (st == FOCSS_OK) st = fg::ensure_red(c, (size_t)in->batch);
+    if (st == FOCSS_OK) st = fg::power_sums(c, in, c->d_red);
+    if (st != FOCSS_OK) return st;
+    const size_t per = (size_t)in->modes * in->samples;
+    FG_LAUNCH(fg::certainty_decision_kernel<<<fg::grid_for(in->n(), 256), 256, 0, c->stream>>>(in->d, out->d, per, in->batch, c->d_red, certainty));
+    return fg::cuda_check(c, cudaGetLastError(), "certainty_decision");
 }
 
 FOCSS_API focss_status focss_hd_codes(focss_ctx* c, const focss_field* in, int32_t* codes) {

@@ -121,6 +121,31 @@ def soft_decision_16qam(f: Field, uncertainty: float) -> Field:
     return out
 
 
+def find_certainty(tx: Field, rx: Field):
+    """find_certainty (src/tasks/wdm_scoring.cpp:105-126), one value per
+    realization (each realization is one matrix: rows = modes)."""
+    out = np.zeros(tx.batch)
+    check(lib().focss_find_certainty(tx.ctx.h, tx.h, rx.h, _vp(out)), tx.ctx.h)
+    return out
+
+
+def certainty_decision(f: Field, certainty: float) -> Field:
+    """sd (src/tasks/wdm_scoring.cpp:128-144): snap to the decided point when
+    closer than certainty / sqrt(5) at the RMS amplitude, else keep."""
+    out = _like(f)
+    check(lib().focss_certainty_decision(f.ctx.h, f.h, float(certainty), out.h), f.ctx.h)
+    return out
+
+
+sd = certainty_decision
+
+
+def hd(f: Field) -> Field:
+    """hd (src/tasks/wdm_scoring.cpp:146-156): the hard decision at the RMS
+    amplitude, which is hard_decision_16qam's sqrt(average power / modes)."""
+    return hard_decision_16qam(f)
+
+
 def hd_sequence_16qam(f: Field):
     codes = np.zeros(f.shape, np.int32)
     check(lib().focss_hd_codes(f.ctx.h, f.h, _vp(codes)), f.ctx.h)

@@ -263,6 +263,20 @@ FOCSS_API focss_status focss_hard_decision(focss_ctx* ctx, const focss_field* in
  * boundary (0, +-2/sqrt(10)); there the received value is kept. */
 FOCSS_API focss_status focss_soft_decision(focss_ctx* ctx, const focss_field* in, double uncertainty,
                                           focss_field* out);
+/* Certainty-based decisions of the WDM scoring task.  Each realization is one
+ * matrix of the task (rows = modes; a dataset field has channel * modes + mode
+ * rows), scaled by its RMS amplitude over all rows and samples.
+ * find_certainty (src/tasks/wdm_scoring.cpp:105-126): certainty[b] =
+ * sqrt(5) * min(1/sqrt(5), smallest RMS-normalized distance from a wrongly
+ * decided received sample to its decided point); host array of batch.
+ * sd (src/tasks/wdm_scoring.cpp:128-144) = focss_certainty_decision: a sample
+ * snaps to its decided point when closer than certainty / sqrt(5), else it is
+ * kept.  hd (src/tasks/wdm_scoring.cpp:146-156) is focss_hard_decision (the
+ * RMS amplitude equals sqrt(average power / modes)). */
+FOCSS_API focss_status focss_find_certainty(focss_ctx* ctx, const focss_field* tx, const focss_field* rx,
+                                           double* certainty);
+FOCSS_API focss_status focss_certainty_decision(focss_ctx* ctx, const focss_field* in, double certainty,
+                                               focss_field* out);
 /* hd_sequence_16qam (src/focss/processing/modulation.cpp:148-156): codes is a
  * host int32 array of batch*modes*samples. */
 FOCSS_API focss_status focss_hd_codes(focss_ctx* ctx, const focss_field* in, int32_t* codes);

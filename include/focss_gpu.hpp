@@ -553,6 +553,20 @@ inline Field soft_decision_16qam(const Field& signal, const double& uncertainty)
     detail::check(focss_soft_decision(gpu_context(), signal.handle(), uncertainty, out.mut()), gpu_context());
     return out;
 }
+/* src/tasks/wdm_scoring.cpp:105-156 (file-local helpers of the WDM scoring
+ * task): one matrix per realization, rows = modes (channel * modes + mode for
+ * a loaded dataset field). */
+inline double find_certainty(const Field& tx, const Field& rx) {
+    Vector<double> v((size_t)tx.batch());
+    detail::check(focss_find_certainty(gpu_context(), tx.handle(), rx.handle(), v.data()), gpu_context());
+    return v[0];
+}
+inline Field sd(const Field& field, const double& certainty) {
+    Field out(field.domain(), field.batch());
+    detail::check(focss_certainty_decision(gpu_context(), field.handle(), certainty, out.mut()), gpu_context());
+    return out;
+}
+inline Field hd(const Field& field) { return hard_decision_16qam(field); }
 inline Vector<int> hd_sequence_16qam(const Field& signal) {
     Vector<std::int32_t> c((size_t)signal.batch() * signal.size());
     detail::check(focss_hd_codes(gpu_context(), signal.handle(), c.data()), gpu_context());

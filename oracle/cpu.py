@@ -61,6 +61,9 @@ def lib():
             "ofc_hd_sequence": (None, [I, I, P, P]),
             "ofc_hard_decision": (None, [I, I, P, P]),
             "ofc_soft_decision": (None, [I, I, P, D, P]),
+            "ofc_find_certainty": (D, [I, I, P, P]),
+            "ofc_certainty_decision": (None, [I, I, P, D, P]),
+            "ofc_hd_rms": (None, [I, I, P, P]),
             "ofc_error_counts": (None, [I, I, P, P, I, P, P]),
             "ofc_bit_error_rate": (D, [I, I, P, P, I]),
             "ofc_symbol_error_rate": (D, [I, I, P, P, I]),
@@ -276,6 +279,31 @@ def soft_decision(a, uncertainty):
     m, n = _shape(a)
     out = np.zeros_like(a)
     lib().ofc_soft_decision(m, n, _ptr(a), uncertainty, _ptr(out))
+    return out
+
+
+def find_certainty(tx, rx):
+    """find_certainty (src/tasks/wdm_scoring.cpp:105-126); rows x cols arrays."""
+    tx, rx = _c128(tx), _c128(rx)
+    m, n = _shape(tx)
+    return float(lib().ofc_find_certainty(m, n, _ptr(tx), _ptr(rx)))
+
+
+def certainty_decision(a, certainty):
+    """sd (src/tasks/wdm_scoring.cpp:128-144)."""
+    a = _c128(a)
+    m, n = _shape(a)
+    out = np.zeros_like(a)
+    lib().ofc_certainty_decision(m, n, _ptr(a), certainty, _ptr(out))
+    return out
+
+
+def hd_rms(a):
+    """hd (src/tasks/wdm_scoring.cpp:146-156)."""
+    a = _c128(a)
+    m, n = _shape(a)
+    out = np.zeros_like(a)
+    lib().ofc_hd_rms(m, n, _ptr(a), _ptr(out))
     return out
 
 

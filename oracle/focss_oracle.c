@@ -601,6 +601,69 @@ void ofc_soft_decision(int modes, int samples, const double* a, double uncertain
     }
 }
 
+/* Decisions of the WDM scoring task (src/tasks/wdm_scoring.cpp:105-156) on a
+ * rows x cols matrix (rows = channel * modes + mode, row-major here).  The
+ * amplitude scale is the matrix's RMS over all its elements (arma
+ * norm(., "fro") / sqrt(n_elem)). */
+static double fro2(size_t n, const double* a) {
+    double p = 0;
+    for (size_t i = 0; i < n; ++i) p += a[2 * i] * a[2 * i] + a[2 * i + 1] * a[2 * i + 1];
+    return p;
+}
+
+double ofc_find_certainty(int rows, int cols, const double* tx, const double* rx) {
+    /* wdm_scoring.cpp:105-126: the smallest distance from a wrongly decided
+     * received sample to its decided point, capped at 1/sqrt(5), in units of
+     * the transmitted RMS amplitude, times sqrt(5) */
+    double t[32];
+    ofc_gray16(t);
+    const size_t n = (size_t)rows * cols;
+    const double scale = sqrt((double)n) / sqrt(fro2(n, tx));
+    double threshold = 1.0 / sqrt(5.0) / scale;
+    for (size_t i = 0; i < n; ++i) {
+        uint32_t tc = ofc_demodulate16(scale * tx[2 * i], scale * tx[2 * i + 1]);
+        uint32_t rc = ofc_demodulate16(scale * rx[2 * i], scale * rx[2 * i + 1]);
+        if (tc ^ rc) {
+            double d = hypot(t[2 * rc] / scale - rx[2 * i], t[2 * rc + 1] / scale - rx[2 * i + 1]);
+            if (threshold > d) threshold = d;
+        }
+    }
+    return sqrt(5.0) * scale * threshold;
+}
+
+void ofc_certainty_decision(int rows, int cols, const double* a, double certainty, double* out) {
+    /* wdm_scoring.cpp:128-144 ("sd"): a sample is replaced by its decided
+     * point when it lies closer than certainty / sqrt(5) (RMS-normalized) */
+    double t[32];
+    ofc_gray16(t);
+    const size_t n = (size_t)rows * cols;
+    const double amp = sqrt(fro2(n, a)) / sqrt((double)n);
+    const double threshold = certainty / sqrt(5.0);
+    for (size_t i = 0; i < n; ++i) {
+        double re = a[2 * i] / amp, im = a[2 * i + 1] / amp;
+        uint32_t c = ofc_demodulate16(re, im);
+        if (hypot(t[2 * c] - re, t[2 * c + 1] - im) < threshold) {
+            re = t[2 * c];
+            im = t[2 * c + 1];
+        }
+        out[2 * i] = amp * re;
+        out[2 * i + 1] = amp * im;
+    }
+}
+
+void ofc_hd_rms(int rows, int cols, const double* a, double* out) {
+    /* wdm_scoring.cpp:146-156 ("hd"): hard decision at the RMS amplitude */
+    double t[32];
+    ofc_gray16(t);
+    const size_t n = (size_t)rows * cols;
+    const double amp = sqrt(fro2(n, a)) / sqrt((double)n);
+    for (size_t i = 0; i < n; ++i) {
+        uint32_t c = ofc_demodulate16(a[2 * i] / amp, a[2 * i + 1] / amp);
+        out[2 * i] = amp * t[2 * c];
+        out[2 * i + 1] = amp * t[2 * c + 1];
+    }
+}
+
 static int popcount4(uint32_t d) {
     int n = 0;
     while (d) {

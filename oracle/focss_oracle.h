@@ -93,6 +93,9 @@ uint32_t ofc_demodulate16(double re, double im);          /* :98-110 */
 void ofc_hd_sequence(int modes, int samples, const double* a, int32_t* codes);
 void ofc_hard_decision(int modes, int samples, const double* a, double* out);
 void ofc_soft_decision(int modes, int samples, const double* a, double uncertainty, double* out);
+double ofc_find_certainty(int rows, int cols, const double* tx, const double* rx);
+void ofc_certainty_decision(int rows, int cols, const double* a, double certainty, double* out);
+void ofc_hd_rms(int rows, int cols, const double* a, double* out);
 void ofc_error_counts(int modes, int samples, const double* tx,
                       const double* rx, int cut, uint64_t* bit_errors,
                       uint64_t* symbol_errors);

@@ -2,12 +2,12 @@
 // in the reference's own idiom (src/tasks/sp_run.cpp:10-53,
 // src/tasks/systems.cpp:26-71): 16QAM -> RRC shaping -> `spans` x 80 km SSMF,
 // UNIFORM 1 km steps, lossless EDFA without noise -> CDC -> matched filter ->
-// phase-shift equalizer -> Q, BER, decisions.
+// phase-shift equalizer -> Q, BER, decisions, decision certainty.
 //
 // usage: facade_link <codes.i32> <out_prefix> [spans]
 // writes <out_prefix>_sym.c128 (symbols), _tx.c128 (transmitted field), _after.c128 (after the
 // spans), _rx.c128 (equalized symbols), _codes.i32 (decisions) and
-// _metrics.txt ("q ber").
+// _metrics.txt ("q ber certainty").
 #include <cstdio>
 #include <fstream>
 #include <string>
@@ -64,11 +64,14 @@ int main(int argc, char** argv) {
         rx = focss::PhaseShiftEqualizer(3600).train_equalize(symbols, rx);
         const double q = focss::q2_factor(symbols, rx, 100);
         const double ber = focss::bit_error_rate_16qam(symbols, rx, 100);
+        const double certainty = focss::find_certainty(symbols, rx);
+        const focss::Field snapped = focss::sd(rx, certainty);
+        if (snapped.size() != rx.size() || focss::hd(rx).size() != rx.size()) return 4;
         write_vec(out + "_rx.c128", rx.data());
         write_vec(out + "_codes.i32", focss::hd_sequence_16qam(rx));
         std::ofstream m(out + "_metrics.txt");
         m.precision(17);
-        m << q << " " << ber << "\n";
+        m << q << " " << ber << " " << certainty << "\n";
         std::printf("Q %.4f dB  BER %.3e\n", q, ber);
     } catch (const focss::gpu_error& e) {
         std::fprintf(stderr, "%s\n", e.what());

@@ -83,7 +83,7 @@ def test_facade_link_matches_oracle(tmp_path, oracle_cpu):
     after = np.fromfile(prefix + "_after.c128", np.complex128)
     rx = np.fromfile(prefix + "_rx.c128", np.complex128)
     dec = np.fromfile(prefix + "_codes.i32", np.int32)
-    q_gpu, ber_gpu = map(float, open(prefix + "_metrics.txt").read().split())
+    q_gpu, ber_gpu, cert_gpu = map(float, open(prefix + "_metrics.txt").read().split())
     assert x0.size == ns * osf and rx.size == ns
 
     ofib = cpu.Fiber(ALPHA, BETA2, GAMMA, 80e3, 1.55e-6, 1.0)
@@ -102,3 +102,4 @@ def test_facade_link_matches_oracle(tmp_path, oracle_cpu):
     assert ber_gpu == cpu.bit_error_rate(tx, s, 100)
     np.testing.assert_array_equal(dec, cpu.hd_sequence(s))
     assert rel_l2(rx, s) < 1e-4
+    assert abs(cert_gpu - cpu.find_certainty(tx, rx)) < 1e-12

@@ -125,3 +125,36 @@ def test_rrc_round_trip_full_size(ctx):
     assert np.all(dsp.bit_error_rate_16qam(sym, back, 0) == 0)
     assert np.all(dsp.q2_factor(sym, back, 0) > 40)
     np.testing.assert_array_equal(dsp.hd_sequence_16qam(back), codes)
+
+
+def test_certainty_decisions(ctx, oracle_cpu):
+    """find_certainty / sd / hd (src/tasks/wdm_scoring.cpp:105-156) on
+    3 realizations of a 6-row (3 channels x 2 modes) dataset-shaped field:
+    the certainty equals the oracle's to FP64 rounding of the RMS sums, the
+    snapped samples are the same (bit-exact decision pattern) and the outputs
+    match to FP32 rounding."""
+    rng = np.random.default_rng(105)
+    rows, n, b = 6, 1 << 14, 3
+    codes = rng.integers(0, 16, (b, rows, n))
+    tx = f32(oracle_cpu.qam16_map(codes.ravel()).reshape(b, rows, n) * 0.8)
+    rx = f32(tx + 0.11 * (rng.standard_normal(tx.shape) + 1j * rng.standard_normal(tx.shape)))
+    t = fg.Field(fg.Domain(rows, n, 1.0), data=tx, batch=b, ctx=ctx)
+    r = fg.Field(fg.Domain(rows, n, 1.0), data=rx, batch=b, ctx=ctx)
+    cert = dsp.find_certainty(t, r)
+    want = [oracle_cpu.find_certainty(tx[i], rx[i]) for i in range(b)]
+    np.testing.assert_allclose(cert, want, rtol=1e-12)
+    assert all(0 < c < 1 for c in cert)
+    for c in (cert[0], 0.6):
+        got = dsp.certainty_decision(r, c).numpy()
+        for i in range(b):
+            ref = oracle_cpu.certainty_decision(rx[i], c)
+            snapped = np.abs(ref - rx[i]) > 1e-6 * np.abs(rx[i]).max()
+            got_snapped = np.abs(got[i] - rx[i]) > 1e-6 * np.abs(rx[i]).max()
+            np.testing.assert_array_equal(got_snapped, snapped)
+            assert 0 < snapped.sum() < snapped.size
+            assert rel_l2(got[i], ref) < TOL
+    h = dsp.hd(r).numpy()
+    for i in range(b):
+        assert rel_l2(h[i], oracle_cpu.hd_rms(rx[i])) < TOL
+    # a field with no decision errors sits at the 1/sqrt(5) cap: certainty 1
+    assert abs(dsp.find_certainty(t, t)[0] - 1.0) < 1e-12
