@@ -13,3 +13,4 @@ from .api import (  # noqa: F401
 )
 from . import dsp  # noqa: F401,E402
 from .dsp import PhaseShiftEqualizer, ScalarEqualizer  # noqa: F401,E402
+from .wdm_ppe import WdmPPE  # noqa: F401,E402

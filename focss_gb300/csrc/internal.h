@@ -151,6 +151,14 @@ focss_status ssfm_plan(Ctx* ctx, int N, const Plan** out);
 bool amplifier_coeffs(int op, double gain, double noise_factor, double f0, double dt, double* scale,
                       double* sigma);
 
+// ---- triplet.cu
+// Triplet sum over `modes` consecutive rows of each realization of `in`
+// (realizations in_bstride apart) into out (batch x modes x samples); with rx
+// the equalizer (rx - y) * inv_lw.
+focss_status run_triplet_rows(Ctx* c, const float2* in, size_t in_bstride, int modes, int samples, int batch,
+                              const float2* rx, int radius, int n_terms, const int32_t* m, const int32_t* n,
+                              const double* coef, float2 inv_lw, float2* out);
+
 // ---- span_loop.cu
 void free_loop_graphs(Ctx* ctx);
 // Plain transforms on a field buffer of `batch` x N (modes folded into batch).

@@ -12,7 +12,10 @@
 // responses appended as one more column are formed on the device; the
 // (2R+1)^2/2-sized Hermitian system is then solved by the caller in FP64
 // (normal equations: the same solution as the reference's least squares for a
-// full-rank design).  The Gram product is a tiled complex kernel on the CUDA
+// full-rank design).  WdmPPE::train (src/focss/equalizer/wdm_sino.cpp:28-142)
+// is the same pipeline on the centre channel of a 3-channel dual-polarization
+// matrix with the XPM triplets of the neighbours as further features.
+// The Gram product is a tiled complex kernel on the CUDA
 // cores (64 x 64 output tiles, 4 x 4 complex outputs per thread) reading the
 // FP32 features and accumulating in FP64.
 #include <algorithm>
@@ -80,6 +83,62 @@ __global__ void responses_kernel(const float2* __restrict__ tx, const float2* __
         float2 v = rx[(size_t)mode * N + k];
         if (fixed) v = csub(v, cmul(tx[(size_t)mode * N + k], lw));
         y[i] = v;
+    }
+}
+
+// WdmPPE (src/focss/equalizer/wdm_sino.cpp:42-82) on a 6-row realization
+// (rows channel * 2 + polarization: left neighbour 0-1, centre 2-3, right
+// neighbour 4-5).  T1 (neighbour rows r0, r1 = 0, 1) and T3 (4, 5) of
+// wdm_sino.cpp:166-200 for polarization `pol`:
+//   A_c(k+m) [2 A_r0(k+n) A_r0*(k+m+n) + A_r1(k+n) A_r1*(k+m+n)] + A_o(k+m) A_r0(k+n) A_r1*(k+m+n)
+// with (c, o, r0, r1) = (2, 3, r0, r1) for pol 0 and (3, 2, r1, r0) for pol 1.
+__device__ __forceinline__ float2 t13(const float2* __restrict__ a, int N, int pol, int k, int m, int n, int r0,
+                                      int r1) {
+    const int c = 2 + pol, o = 3 - pol;
+    const int p = pol ? r1 : r0, q = pol ? r0 : r1;
+    const float2 inner = cadd(cscale(cmulc(a[(size_t)p * N + k + n], a[(size_t)p * N + k + m + n]), 2.f),
+                              cmulc(a[(size_t)q * N + k + n], a[(size_t)q * N + k + m + n]));
+    return cadd(cmul(a[(size_t)c * N + k + m], inner),
+                cmul(a[(size_t)o * N + k + m], cmulc(a[(size_t)p * N + k + n], a[(size_t)q * N + k + m + n])));
+}
+
+// Z[f][i] for i = pol * nspm + (k - R): kinds 0-3 SPM (the SINO features on
+// the centre rows), 4 the transmitted centre sample, 5 XPM T1(m, n) + T3(m, -n).
+__global__ void wdm_features_kernel(const float2* __restrict__ tx, int N, int R, const Feature* __restrict__ fs,
+                                    int nf, float2* __restrict__ Z, size_t kp) {
+    const int nspm = N - 2 * R;
+    const size_t ns = 2 * (size_t)nspm;
+    const int f = blockIdx.y;
+    const Feature F = fs[f];
+    const float2* centre = tx + 2 * (size_t)N;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ns; i += (size_t)gridDim.x * blockDim.x) {
+        const int pol = (int)(i / nspm), k = (int)(i % nspm) + R;
+        float2 v;
+        if (F.kind == 4) {
+            v = centre[(size_t)pol * N + k];
+        } else if (F.kind == 5) {
+            v = cadd(t13(tx, N, pol, k, F.m, F.n, 0, 1), t13(tx, N, pol, k, F.m, -F.n, 4, 5));
+        } else {
+            v = term(centre, 2, N, pol, k, F.m, F.n);
+            if (F.kind == 1) v = cadd(v, term(centre, 2, N, pol, k, -F.m, -F.n));
+            if (F.kind == 2) v = cadd(v, term(centre, 2, N, pol, k, F.n, F.m));
+            if (F.kind == 3) {
+                v = cadd(v, term(centre, 2, N, pol, k, F.n, F.m));
+                v = cadd(v, term(centre, 2, N, pol, k, -F.m, -F.n));
+                v = cadd(v, term(centre, 2, N, pol, k, -F.n, -F.m));
+            }
+        }
+        Z[(size_t)f * kp + i] = v;
+    }
+}
+
+// Responses of the centre polarizations: rows row0, row0 + 1 of rx.
+__global__ void wdm_responses_kernel(const float2* __restrict__ rx, int row0, int N, int R, float2* __restrict__ y) {
+    const int nspm = N - 2 * R;
+    const size_t ns = 2 * (size_t)nspm;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ns; i += (size_t)gridDim.x * blockDim.x) {
+        const int pol = (int)(i / nspm), k = (int)(i % nspm) + R;
+        y[i] = rx[(size_t)(row0 + pol) * N + k];
     }
 }
 
@@ -185,6 +244,64 @@ __global__ void __launch_bounds__(256) gram_kernel(const float2* __restrict__ Z,
             G[(size_t)(bi * GT + ty * 4 + r) * nfp + bj * GT + tx + 16 * c] = acc[r][c];
 }
 
+// SPM feature list in the order of sino.cpp:70-100 / wdm_sino.cpp:47-71.
+void spm_features(int R, std::vector<Feature>& fs) {
+    const int mb = R / 2;
+    for (int m = -mb; m <= mb; ++m)
+        for (int n = std::abs(m); n <= R - std::abs(m); ++n) {
+            const int kind = (m == 0 && n == 0) ? 0 : (m == n) ? 1 : (m == -n) ? 2 : 3;
+            fs.push_back({m, n, kind});
+        }
+}
+
+// Device buffers of one fit: Z holds nf feature columns and the responses
+// (column nf), each kp samples long (zero-padded), nfp columns in all.
+struct FitBuffers {
+    float2* Z = nullptr;
+    Feature* fs = nullptr;
+    double2* G = nullptr;
+    double* stat = nullptr;
+    ~FitBuffers() {
+        cudaFree(Z);
+        cudaFree(fs);
+        cudaFree(G);
+        cudaFree(stat);
+    }
+};
+
+cudaError_t fit_alloc(FitBuffers& b, const std::vector<Feature>& fs, size_t kp, int nfp, cudaStream_t s) {
+    const int nf = (int)fs.size();
+    cudaError_t e = cudaMalloc(&b.Z, sizeof(float2) * (size_t)nfp * kp);
+    if (e == cudaSuccess) e = cudaMalloc(&b.fs, sizeof(Feature) * std::max(nf, 1));
+    if (e == cudaSuccess) e = cudaMalloc(&b.G, sizeof(double2) * (size_t)nfp * nfp);
+    if (e == cudaSuccess) e = cudaMalloc(&b.stat, sizeof(double) * (3 * (size_t)nfp + 2));
+    if (e == cudaSuccess) e = cudaMemsetAsync(b.Z, 0, sizeof(float2) * (size_t)nfp * kp, s);
+    if (e == cudaSuccess && nf) e = cudaMemcpyAsync(b.fs, fs.data(), sizeof(Feature) * nf, cudaMemcpyHostToDevice, s);
+    return e;
+}
+
+// z-score the feature columns, centre the responses, form the Gram matrix and
+// copy gram ((nf+1)^2 complex128, upper triangle), mean (nf+1 complex128) and
+// sd (nf doubles) to the host.
+cudaError_t fit_finish(FitBuffers& b, size_t kp, size_t ns, int nf, int nfp, double* gram, double* mean, double* sd,
+                       cudaStream_t s) {
+    column_stats_kernel<<<nf + 1, 256, 0, s>>>(b.Z, kp, ns, nf, b.stat, b.stat + 2 * (size_t)nfp);
+    count_launch();
+    dim3 g2(nfp / GT, nfp / GT);
+    gram_kernel<<<g2, 256, 0, s>>>(b.Z, kp, nfp, b.G);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMemcpy2DAsync(gram, sizeof(double2) * (nf + 1), b.G, sizeof(double2) * nfp,
+                              sizeof(double2) * (nf + 1), nf + 1, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(mean, b.stat, sizeof(double) * 2 * (nf + 1), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(sd, b.stat + 2 * (size_t)nfp, sizeof(double) * nf, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return e;
+}
+
 }  // namespace
 }  // namespace fg
 
@@ -204,14 +321,8 @@ FOCSS_API focss_status focss_sino_gram(focss_ctx* c, const focss_field* tx, cons
         return set_error(c, FOCSS_ERR_INVALID_ARG, "sino_gram: tx and rx must be single realizations of one domain");
     const int N = tx->samples, modes = tx->modes, R = radius;
     if (N <= 2 * R + 1) return set_error(c, FOCSS_ERR_INVALID_ARG, "sino_gram: field shorter than the radius");
-    // feature list in the order of sino.cpp:70-100
     std::vector<Feature> fs;
-    const int mb = R / 2;
-    for (int m = -mb; m <= mb; ++m)
-        for (int n = std::abs(m); n <= R - std::abs(m); ++n) {
-            const int kind = (m == 0 && n == 0) ? 0 : (m == n) ? 1 : (m == -n) ? 2 : 3;
-            fs.push_back({m, n, kind});
-        }
+    spm_features(R, fs);
     if (type == 0) fs.push_back({0, 0, 4});
     const int nf = (int)fs.size();
     if (nf != focss_sino_num_features(R, type)) return set_error(c, FOCSS_ERR_INVALID_ARG, "sino_gram: feature count");
@@ -219,45 +330,64 @@ FOCSS_API focss_status focss_sino_gram(focss_ctx* c, const focss_field* tx, cons
     const size_t kp = (ns + GK - 1) / GK * GK;
     const int nfp = (nf + 1 + GT - 1) / GT * GT;  // features + responses, padded
     cudaStream_t s = c->stream;
-    float2* Z = nullptr;
-    Feature* dfs = nullptr;
-    double2* dG = nullptr;
-    double* dstat = nullptr;
-    cudaError_t e = cudaMalloc(&Z, sizeof(float2) * (size_t)nfp * kp);
-    if (e == cudaSuccess) e = cudaMalloc(&dfs, sizeof(Feature) * nf);
-    if (e == cudaSuccess) e = cudaMalloc(&dG, sizeof(double2) * (size_t)nfp * nfp);
-    if (e == cudaSuccess) e = cudaMalloc(&dstat, sizeof(double) * (3 * (size_t)nfp + 2));
-    if (e == cudaSuccess) e = cudaMemsetAsync(Z, 0, sizeof(float2) * (size_t)nfp * kp, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(dfs, fs.data(), sizeof(Feature) * nf, cudaMemcpyHostToDevice, s);
+    FitBuffers b;
+    cudaError_t e = fit_alloc(b, fs, kp, nfp, s);
     if (e == cudaSuccess) {
         dim3 grid((unsigned)std::min<size_t>((ns + 255) / 256, 1024), nf);
-        features_kernel<<<grid, 256, 0, s>>>(tx->d, modes, N, R, dfs, nf, Z, kp);
+        features_kernel<<<grid, 256, 0, s>>>(tx->d, modes, N, R, b.fs, nf, b.Z, kp);
         count_launch();
         responses_kernel<<<grid_for_(ns), 256, 0, s>>>(tx->d, rx->d, modes, N, R,
                                                         make_float2((float)lw_re, (float)lw_im), type == 1,
-                                                        Z + (size_t)nf * kp);
+                                                        b.Z + (size_t)nf * kp);
         count_launch();
-        column_stats_kernel<<<nf + 1, 256, 0, s>>>(Z, kp, ns, nf, dstat, dstat + 2 * (size_t)nfp);
-        count_launch();
-        dim3 g2(nfp / GT, nfp / GT);
-        gram_kernel<<<g2, 256, 0, s>>>(Z, kp, nfp, dG);
-        count_launch();
-        e = cudaGetLastError();
+        e = fit_finish(b, kp, ns, nf, nfp, gram, mean, sd, s);
     }
-    // gram: (nf+1) x (nf+1) complex128 (upper triangle valid); mean: nf+1 complex; sd: nf
-    if (e == cudaSuccess)
-        e = cudaMemcpy2DAsync(gram, sizeof(double2) * (nf + 1), dG, sizeof(double2) * nfp,
-                              sizeof(double2) * (nf + 1), nf + 1, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(mean, dstat, sizeof(double) * 2 * (nf + 1), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(sd, dstat + 2 * (size_t)nfp, sizeof(double) * nf, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    cudaFree(Z);
-    cudaFree(dfs);
-    cudaFree(dG);
-    cudaFree(dstat);
     return cuda_check(c, e, "sino_gram");
+}
+
+FOCSS_API int focss_wdm_ppe_num_features(int c_radius, int d_radius) {
+    // wdm_sino.cpp:32-34
+    const int n_spm = c_radius < 0 ? 0 : c_radius * (c_radius + 2) / 2 + 1;
+    const int n_xpm = d_radius < 0 ? 0 : 2 * d_radius * d_radius + 2 * d_radius + 1;
+    return n_spm + n_xpm + 1;
+}
+
+FOCSS_API focss_status focss_wdm_ppe_gram(focss_ctx* c, const focss_field* tx, const focss_field* rx, int c_radius,
+                                          int d_radius, double* gram, double* mean, double* sd) {
+    using namespace fg;
+    if (!c || !tx || !rx || !gram || !mean || !sd || c_radius < -1 || d_radius < -1) return FOCSS_ERR_INVALID_ARG;
+    if (tx->modes != 6 || (rx->modes != 6 && rx->modes != 2) || tx->samples != rx->samples || tx->batch != 1 ||
+        rx->batch != 1)
+        return set_error(c, FOCSS_ERR_INVALID_ARG,
+                         "wdm_ppe_gram: tx must be one 6-row realization (3 channels x 2 polarizations), rx 6 or 2 rows");
+    const int N = tx->samples, R = std::max(c_radius, d_radius);
+    if (R < 0 || N <= 2 * R + 1) return set_error(c, FOCSS_ERR_INVALID_ARG, "wdm_ppe_gram: radius vs field length");
+    // feature order of wdm_sino.cpp:43-80
+    std::vector<Feature> fs;
+    if (c_radius >= 0) spm_features(c_radius, fs);
+    for (int m = -d_radius; m <= d_radius; ++m) {
+        const int nb = d_radius - std::abs(m);
+        for (int n = -nb; n <= nb; ++n) fs.push_back({m, n, 5});
+    }
+    fs.push_back({0, 0, 4});
+    const int nf = (int)fs.size();
+    if (nf != focss_wdm_ppe_num_features(c_radius, d_radius))
+        return set_error(c, FOCSS_ERR_INVALID_ARG, "wdm_ppe_gram: feature count");
+    const size_t ns = 2 * (size_t)(N - 2 * R);
+    const size_t kp = (ns + GK - 1) / GK * GK;
+    const int nfp = (nf + 1 + GT - 1) / GT * GT;
+    cudaStream_t s = c->stream;
+    FitBuffers b;
+    cudaError_t e = fit_alloc(b, fs, kp, nfp, s);
+    if (e == cudaSuccess) {
+        dim3 grid((unsigned)std::min<size_t>((ns + 255) / 256, 1024), nf);
+        wdm_features_kernel<<<grid, 256, 0, s>>>(tx->d, N, R, b.fs, nf, b.Z, kp);
+        count_launch();
+        wdm_responses_kernel<<<grid_for_(ns), 256, 0, s>>>(rx->d, rx->modes == 6 ? 2 : 0, N, R, b.Z + (size_t)nf * kp);
+        count_launch();
+        e = fit_finish(b, kp, ns, nf, nfp, gram, mean, sd, s);
+    }
+    return cuda_check(c, e, "wdm_ppe_gram");
 }
 
 }  // extern "C"

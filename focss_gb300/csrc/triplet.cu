@@ -34,7 +34,8 @@ constexpr int TK = TT * NT;
 __device__ __forceinline__ int padi(int j) { return j + (j >> 3); }
 
 struct TripletArgs {
-    const float2* in;       // batch x modes x N
+    const float2* in;       // batch realizations, `in_bstride` apart, modes x N each
+    size_t in_bstride;
     const float2* rx;       // equalizer: batch x modes x N, or null
     float2* out;
     float2 inv_lw;          // 1 / linear_weight (equalizer)
@@ -59,7 +60,7 @@ __global__ void __launch_bounds__(NT) triplet_kernel(const TripletArgs a) {
     float2* As = sh;                           // MODES x padi(alen)
     const int astride = padi(alen) + 1;
     float2* Qs = As + MODES * astride;         // padi(qlen)
-    const float2* in = a.in + (size_t)b * MODES * N;
+    const float2* in = a.in + (size_t)b * a.in_bstride;
 
     // A tile: index i <-> sample k0 - halo_a + i (zero outside [0, N))
     for (int p = 0; p < MODES; ++p)
@@ -171,9 +172,15 @@ bool build_terms(int n_terms, const int32_t* m, const int32_t* n, const double* 
     return true;
 }
 
-focss_status run_triplet(Ctx* c, const Field* in, const Field* rx, int radius, int n_terms, const int32_t* m,
-                         const int32_t* n, const double* coef, float2 inv_lw, Field* out) {
-    if (in->modes < 1 || in->modes > 2)
+}  // namespace
+
+// The triplet sum over `modes` consecutive rows of each realization of `in`
+// (realizations in_bstride apart), written to `out` (batch x modes x N);
+// with rx, the equalizer (rx - y) / linear_weight instead.
+focss_status run_triplet_rows(Ctx* c, const float2* in, size_t in_bstride, int modes, int samples, int batch,
+                              const float2* rx, int radius, int n_terms, const int32_t* m, const int32_t* n,
+                              const double* coef, float2 inv_lw, float2* out) {
+    if (modes < 1 || modes > 2)
         return set_error(c, FOCSS_ERR_UNSUPPORTED, "triplet: 1 or 2 modes");
     if (n_terms <= 0 || !m || !n || !coef) return set_error(c, FOCSS_ERR_INVALID_ARG, "triplet: empty term list");
     for (int i = 0; i < n_terms; ++i)
@@ -197,12 +204,13 @@ focss_status run_triplet(Ctx* c, const Field* in, const Field* rx, int radius, i
         e = cudaMemcpyAsync(dcoef, t.coef.data(), sizeof(float2) * t.coef.size(), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return cuda_check(c, e, "triplet upload");
     TripletArgs a{};
-    a.in = in->d;
-    a.rx = rx ? rx->d : nullptr;
-    a.out = out->d;
+    a.in = in;
+    a.in_bstride = in_bstride;
+    a.rx = rx;
+    a.out = out;
     a.inv_lw = inv_lw;
-    a.modes = in->modes;
-    a.samples = in->samples;
+    a.modes = modes;
+    a.samples = samples;
     a.radius = radius;
     a.groups = (int)ng;
     a.g_m = (const int*)d;
@@ -212,10 +220,10 @@ focss_status run_triplet(Ctx* c, const Field* in, const Field* rx, int radius, i
     a.halo_q = t.halo_q;
     a.halo_a = t.halo_a;
     const int alen = TK + 2 * t.halo_a, qlen = TK + 2 * t.halo_q;
-    const size_t smem = sizeof(float2) * ((size_t)in->modes * (alen + alen / 8 + 2) + qlen + qlen / 8 + 2);
+    const size_t smem = sizeof(float2) * ((size_t)modes * (alen + alen / 8 + 2) + qlen + qlen / 8 + 2);
     if (smem > 200 * 1024) return set_error(c, FOCSS_ERR_UNSUPPORTED, "triplet: term offsets too large for a tile");
-    dim3 grid((in->samples + TK - 1) / TK, in->batch);
-    if (in->modes == 1) {
+    dim3 grid((samples + TK - 1) / TK, batch);
+    if (modes == 1) {
         cudaFuncSetAttribute(triplet_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         triplet_kernel<1><<<grid, NT, smem, s>>>(a);
     } else {
@@ -228,6 +236,12 @@ focss_status run_triplet(Ctx* c, const Field* in, const Field* rx, int radius, i
     return cuda_check(c, e, "triplet");
 }
 
+namespace {
+focss_status run_triplet(Ctx* c, const Field* in, const Field* rx, int radius, int n_terms, const int32_t* m,
+                         const int32_t* n, const double* coef, float2 inv_lw, Field* out) {
+    return run_triplet_rows(c, in->d, (size_t)in->modes * in->samples, in->modes, in->samples, in->batch,
+                            rx ? rx->d : nullptr, radius, n_terms, m, n, coef, inv_lw, out->d);
+}
 }  // namespace
 }  // namespace fg
 

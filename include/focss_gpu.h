@@ -338,6 +338,36 @@ FOCSS_API int focss_sino_num_features(int radius, int type);
 FOCSS_API focss_status focss_sino_gram(focss_ctx* ctx, const focss_field* tx, const focss_field* rx, int radius,
                                        int type, double lw_re, double lw_im, double* gram, double* mean, double* sd);
 
+/* WdmPPE (src/focss/equalizer/wdm_sino.h:8-71, wdm_sino.cpp): the
+ * dual-polarization WDM perturbation equalizer.  Its fields are 6-row
+ * realizations, rows channel * 2 + polarization: left neighbour 0-1, centre
+ * 2-3, right neighbour 4-5 (the dataset layout of
+ * src/tasks/wdm_scoring.cpp:79-103); its outputs are 2-row (the centre
+ * channel).
+ * focss_wdm_ppe_num_features: wdm_sino.cpp:32-34 (SPM triangle of c_radius,
+ * XPM diamond of d_radius, the linear term; a radius of -1 drops that group).
+ * focss_wdm_ppe_gram: the normal equations of WdmPPE::train
+ * (wdm_sino.cpp:28-98) for one realization, in the layout of
+ * focss_sino_gram: gram = [Z y]^H [Z y] of the z-scored features Z (SPM, XPM
+ * T1(m,n) + T3(m,-n), transmitted centre sample) with the centred responses
+ * y (rx rows 2-3, or rows 0-1 of a 2-row rx) over samples [R, N-R), R =
+ * max(c_radius, d_radius), both polarizations stacked; complex128
+ * (nf+1)^2, upper triangle valid; mean = nf+1 complex128 column means; sd =
+ * nf standard deviations (normalized by the count).
+ * focss_wdm_ppe_apply: with C ((2c+1)^2 complex128, C[(c+m)(2c+1) + c+n])
+ * and D ((2d+1)^2, likewise) the trained tables and a the linear weight,
+ *   noise = spm(spm_in) + xpm(xpm_in)       (null inputs contribute nothing)
+ *   out   = (rx_centre - noise) / a          if rx       (equalize, :240-249)
+ *         = a * lin_in_centre + noise        if lin_in   (model, :235-238)
+ *         = noise                            otherwise   (spm / xpm / cubic). */
+FOCSS_API int focss_wdm_ppe_num_features(int c_radius, int d_radius);
+FOCSS_API focss_status focss_wdm_ppe_gram(focss_ctx* ctx, const focss_field* tx, const focss_field* rx,
+                                          int c_radius, int d_radius, double* gram, double* mean, double* sd);
+FOCSS_API focss_status focss_wdm_ppe_apply(focss_ctx* ctx, const focss_field* spm_in, const focss_field* xpm_in,
+                                           const focss_field* rx, const focss_field* lin_in, int c_radius,
+                                           const double* C, int d_radius, const double* D, double lw_re,
+                                           double lw_im, focss_field* out);
+
 /* ---------------------------------------------------------- learned DBP */
 /* No reference counterpart: a few-step learned replacement of
  * backward_propagation (src/tasks/systems.cpp:73-91).  Per realization (one

@@ -142,7 +142,10 @@ def test_certainty_decisions(ctx, oracle_cpu):
     r = fg.Field(fg.Domain(rows, n, 1.0), data=rx, batch=b, ctx=ctx)
     cert = dsp.find_certainty(t, r)
     want = [oracle_cpu.find_certainty(tx[i], rx[i]) for i in range(b)]
-    np.testing.assert_allclose(cert, want, rtol=1e-12)
+    # the RMS sums run in different orders (the oracle's sequential FP64 sum of
+    # 1e5 terms is off by ~1e-12), and |gray / scale - rx| amplifies the scale
+    # difference by |gray / scale| / distance (~25 here)
+    np.testing.assert_allclose(cert, want, rtol=1e-9)
     assert all(0 < c < 1 for c in cert)
     for c in (cert[0], 0.6):
         got = dsp.certainty_decision(r, c).numpy()
