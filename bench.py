@@ -387,6 +387,8 @@ def run_ours(args):
         line["sweep"] = sweep_section(fg, ctx, stream)
     if not args.no_ppe:
         line["ppe"] = ppe_section(fg, ctx, stream)
+    if not args.no_wdm_ppe:
+        line["wdm_ppe"] = wdm_ppe_section(fg, ctx, stream)
     if world == 1 and rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         n_steps = CPU_BASELINE_STEPS
@@ -623,6 +625,56 @@ def ppe_section(fg, ctx, stream):
     return out
 
 
+WDM_PPE = dict(
+    workload="wdm_ppe_3ch_dualpol_16qam_32GBd_2^15sym_20x100km_2dBm",
+    channels=3, polarizations=2, symbols=2 ** 15, samples_per_symbol=16, spacing_hz=37.5e9, power_index=16,
+    power_dbm=2.0, spans=20, span_m=1e5, kappa=8 / 9, noise_figure_db=4.5, roll_off=0.01,
+    forward="ADAPTIVE, max 0.001 rad/step, max 1 km", radii=[[30, 0], [30, 3]], cut=36,
+    fit="normal equations on the GPU, FP64 solve", train_seed=1, test_seed=2,
+)
+
+
+def wdm_ppe_section(fg, ctx, stream):
+    """The dual-polarization WDM dataset and scoring pipeline
+    (src/tasks/wdm_run.cpp:79-141, src/tasks/wdm_scoring.cpp:158-187) on
+    the GPU: 3 channels x 2 polarizations of 2^15 16QAM symbols, 16
+    samples/symbol (N = 2^19 per polarization), 20 x 100 km SSMF with the
+    Manakov factor 8/9 and ASE at 2 dBm per channel; CDC, channel selection,
+    matched filter and phase-shift equalizer; WdmPPE fitted on a training
+    realization and applied to a test realization with the received symbols
+    and with their hard decisions as the triplet inputs (Q over both
+    polarizations of the centre channel, cut 36)."""
+    import torch
+    from focss_gb300 import dsp, links
+    c = WDM_PPE
+    link = links.DualPolLink(spans=c["spans"], channels=c["channels"], osf=c["samples_per_symbol"])
+    tx_t, rx_t, _ = links.wdm_dataset(link, c["symbols"], c["power_dbm"], c["train_seed"], ctx=ctx)
+    ctx.sync()
+    (tx, rx, steps), gen_ms = _stream_ms(
+        torch, stream, lambda: links.wdm_dataset(link, c["symbols"], c["power_dbm"], c["test_seed"], ctx=ctx))
+    n = c["symbols"] * c["samples_per_symbol"]
+    tc = links.centre_rows(tx)
+    out = {"config": c, "steps": steps, "dataset_ms": gen_ms,
+           "forward_gsample_steps_per_s": 2 * n * steps / gen_ms / 1e6,
+           "q_db_cdc": float(dsp.q2_factor(tc, links.centre_rows(rx), c["cut"])[0])}
+    hd = dsp.hd(rx)
+    for cr, dr in c["radii"]:
+        ctx.sync()
+        t0 = time.perf_counter()
+        ppe = fg.WdmPPE(cr, dr).train(tx_t, rx_t)
+        fit_s = time.perf_counter() - t0
+        ppe.equalize(rx, rx)  # warm-up
+        e_rx, ms_rx = _stream_ms(torch, stream, lambda: ppe.equalize(rx, rx))
+        e_hd, ms_hd = _stream_ms(torch, stream, lambda: ppe.equalize(hd, rx))
+        out["c%d_d%d" % (cr, dr)] = {
+            "features": int(fg.lib().focss_wdm_ppe_num_features(cr, dr)), "fit_s": fit_s,
+            "q_db_ppe_rx": float(dsp.q2_factor(tc, e_rx, c["cut"])[0]),
+            "q_db_ppe_hd": float(dsp.q2_factor(tc, e_hd, c["cut"])[0]),
+            "equalize_ms": ms_rx, "equalize_hd_ms": ms_hd,
+            "abs_linear_weight": abs(ppe.get_linear_weight())}
+    return out
+
+
 def run_ncu_case(args):
     """Small fixed cases for ncu captures (one kernel family each):
     ssfm  UNIFORM split steps on `--ncu-batch` realizations of the N=2^19 WDM
@@ -697,6 +749,8 @@ def main():
     ap.add_argument("--no-dbp", action="store_true", help="skip the learned-vs-plain DBP section")
     ap.add_argument("--no-sweep", action="store_true", help="skip the uneven-length batched sweep section")
     ap.add_argument("--no-ppe", action="store_true", help="skip the perturbation-equalizer section")
+    ap.add_argument("--no-wdm-ppe", action="store_true",
+                    help="skip the dual-polarization WDM dataset and WdmPPE scoring section")
     ap.add_argument("--host-loop", action="store_true",
                     help="drive the spans from the host (one SSFM run + EDFA per span) instead of one graph")
     args = ap.parse_args()

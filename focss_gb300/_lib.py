@@ -62,6 +62,7 @@ SIGNATURES = {
     "focss_field_copy": (I, [P, P]),
     "focss_field_device_ptr": (P, [P]),
     "focss_field_copy_realizations": (I, [P, I, P, I, I]),
+    "focss_field_copy_modes": (I, [P, I, P, I, I]),
     "focss_field_scale": (I, [P, D, D]),
     "focss_field_power": (I, [P, P, P]),
     "focss_field_fft": (I, [P]),

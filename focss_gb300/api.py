@@ -191,6 +191,12 @@ class Field:
         check(lib().focss_field_copy_realizations(self.h, dst_first, src.h, src_first, count), self.ctx.h)
         return self
 
+    def copy_modes(self, dst_first: int, src: "Field", src_first: int, count: int):
+        """Copy modes src[src_first : src_first + count] into this field's
+        modes [dst_first, ...), in every realization."""
+        check(lib().focss_field_copy_modes(self.h, dst_first, src.h, src_first, count), self.ctx.h)
+        return self
+
     def slice(self, first: int, count: int) -> "Field":
         out = Field(self.domain, batch=count, ctx=self.ctx)
         return out.copy_realizations(0, self, first, count)

@@ -355,6 +355,24 @@ FOCSS_API focss_status focss_field_copy_realizations(focss_field* dst, int dst_f
                           "copy_realizations");
 }
 
+FOCSS_API focss_status focss_field_copy_modes(focss_field* dst, int dst_first, const focss_field* src, int src_first,
+                                              int count) {
+    if (!dst || !src || count < 0 || dst_first < 0 || src_first < 0) return FOCSS_ERR_INVALID_ARG;
+    if (dst->batch != src->batch || dst->samples != src->samples || dst_first + count > dst->modes ||
+        src_first + count > src->modes)
+        return fg::set_error(dst->ctx, FOCSS_ERR_INVALID_ARG, "copy_modes: shapes");
+    if (count == 0) return FOCSS_OK;
+    // one row of count * samples values per realization
+    const size_t row = sizeof(float2) * (size_t)count * src->samples;
+    return fg::cuda_check(dst->ctx,
+                          cudaMemcpy2DAsync(dst->d + (size_t)dst_first * dst->samples,
+                                            sizeof(float2) * (size_t)dst->modes * dst->samples,
+                                            src->d + (size_t)src_first * src->samples,
+                                            sizeof(float2) * (size_t)src->modes * src->samples, row, src->batch,
+                                            cudaMemcpyDeviceToDevice, dst->ctx->stream),
+                          "copy_modes");
+}
+
 FOCSS_API focss_status focss_field_scale(focss_field* f, double re, double im) {
     if (!f) return FOCSS_ERR_INVALID_ARG;
     return fg::cuda_check(f->ctx, fg::launch_scale(f->d, f->n(), make_float2((float)re, (float)im), f->ctx->stream),

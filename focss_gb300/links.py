@@ -13,8 +13,8 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import dsp
-from .api import (Amplifier, Domain, Fiber, Field, SSFM, backward_propagation, db_to_linear, db_to_natural,
-                  dbm_to_watts, disp_to_beta2)
+from .api import (Amplifier, Domain, Fiber, Field, SSFM, backward_propagation, cd_compensation, db_to_linear,
+                  db_to_natural, dbm_to_watts, disp_to_beta2, span_loop)
 
 LIGHT_SPEED = 299792458.0
 
@@ -87,6 +87,85 @@ def centre_channel(link: Link, field: Field, dbp_osf=2):
     """wdm_select(centre) then decimate to dbp_osf samples/symbol (wdm_run.cpp:33-35)."""
     sel = dsp.wdm_select(field, 0, link.spacing)
     return dsp.decimate(sel, link.osf // dbp_osf)
+
+
+@dataclass
+class DualPolLink:
+    """The dual-polarization WDM experiment of src/tasks/parameters.h:4-19 and
+    src/tasks/wdm_run.cpp:79-141 (Manakov Kerr factor 8/9, 100 km spans,
+    37.5 GHz spacing), with three channels: the layout WdmPPE expects
+    (src/tasks/wdm_scoring.cpp:158-187)."""
+    spans: int = 20
+    span_m: float = 1e5
+    alpha_db_km: float = 0.2
+    dispersion: float = 17e-6
+    gamma: float = 1.4e-3
+    kappa: float = 8.0 / 9.0
+    wavelength: float = 1.55e-6
+    noise_figure_db: float = 4.5
+    max_phase: float = 1e-3
+    max_step: float = 1e3
+    baud: float = 32e9
+    channels: int = 3
+    spacing: float = 37.5e9
+    osf: int = 16
+    roll_off: float = 0.01  # rrc_shaping's default (modulation.cpp:85-96)
+
+    def fiber(self):
+        return Fiber(db_to_natural(self.alpha_db_km * 1e-3), disp_to_beta2(self.dispersion, self.wavelength),
+                     self.gamma, self.span_m, self.wavelength, self.kappa)
+
+    def gain(self):
+        return db_to_linear(self.alpha_db_km * self.span_m / 1e3)
+
+    def f0(self):
+        return LIGHT_SPEED / self.wavelength
+
+
+def power_node(power_index: int) -> float:
+    """Launch power per channel in dBm (wdm_run.cpp:22-24)."""
+    return 0.5 * power_index - 6.0
+
+
+def wdm_dataset(link: DualPolLink, n_symbols: int, power_dbm: float, seed: int, ctx=None, spans=None):
+    """wdm_run.cpp:79-141 on the GPU for one realization: per channel 2 x
+    n_symbols 16QAM symbols at power/2 per polarization, RRC shaping, WDM
+    multiplexing, `spans` adaptive-step spans with ASE (one graph-captured
+    span loop), then CDC, channel selection, matched filter and a 720-step
+    phase-shift equalizer per channel.  Returns (tx, rx, steps): 6-row Fields
+    (rows channel * 2 + polarization, the dataset layout of save_field) of
+    the transmitted symbols and the received, equalized symbols."""
+    spans = link.spans if spans is None else spans
+    rng = np.random.default_rng(seed)
+    nch = link.channels
+    codes = rng.integers(0, 16, (nch, 2, n_symbols))
+    sym = dsp.qam16_map(codes, Domain(2, n_symbols, 1 / link.baud, link.f0()), batch=nch, ctx=ctx)
+    sym *= np.sqrt(dbm_to_watts(power_dbm) / 2)
+    sig = dsp.wdm_mux(dsp.rrc_shaping(sym, link.osf, link.roll_off), link.spacing)
+    fib = link.fiber()
+    ssfm = SSFM(fib)
+    ssfm.set_grid(SSFM.ADAPTIVE)
+    ssfm.set_maximum_phase_shift(link.max_phase)
+    ssfm.set_maximum_step_size(link.max_step)
+    amp = Amplifier(link.gain(), db_to_linear(link.noise_figure_db), seed=seed)
+    steps = span_loop([sig], fib, ssfm, spans, after=Amplifier.AMPLIFY, amplifier=amp)[0]
+    cd_compensation(sig, fib, spans)
+    dom = Domain(2 * nch, n_symbols, 1 / link.baud, link.f0())
+    tx, rx = Field(dom, ctx=sig.ctx), Field(dom, ctx=sig.ctx)
+    pse = dsp.PhaseShiftEqualizer(720)
+    for ch in range(nch):
+        t = sym.slice(ch, 1)
+        r = dsp.rrc_sampling(dsp.wdm_select(sig, ch - nch // 2, link.spacing), link.osf, link.roll_off)
+        tx.copy_modes(2 * ch, t, 0, 2)
+        rx.copy_modes(2 * ch, pse.train_equalize(t, r), 0, 2)
+    return tx, rx, int(steps.sum())
+
+
+def centre_rows(f: Field) -> Field:
+    """Rows 2-3 (the centre channel) of a 6-row dataset field."""
+    out = Field(Domain(2, f.domain.samples, f.domain.time_step, f.domain.center_frequency), batch=f.batch,
+                ctx=f.ctx)
+    return out.copy_modes(0, f, 2, 2)
 
 
 def _timed(fn, ctx, repeat=3):

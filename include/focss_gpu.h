@@ -121,6 +121,12 @@ FOCSS_API focss_status focss_field_copy(focss_field* dst, const focss_field* src
  * modes and samples): Field copies (src/focss/field.cpp:56-68) of batch slices. */
 FOCSS_API focss_status focss_field_copy_realizations(focss_field* dst, int dst_first, const focss_field* src,
                                                      int src_first, int count);
+/* Copy modes src[src_first ... src_first+count) to dst[dst_first ...] in every
+ * realization (same batch and samples): gathers channels' polarizations into
+ * the rows of a dataset matrix (channel * modes + mode, the layout of
+ * src/tasks/wdm_run.cpp:55-77) and back. */
+FOCSS_API focss_status focss_field_copy_modes(focss_field* dst, int dst_first, const focss_field* src, int src_first,
+                                              int count);
 /* Device pointer to the complex64 data (for interop); valid until destroy. */
 FOCSS_API void* focss_field_device_ptr(focss_field* field);
 /* Field::operator*=(const complex_t&) (src/focss/field.cpp:387-391). */

@@ -104,3 +104,25 @@ def test_gpu_fit_matches_oracle_fit(ctx, c, d):
     assert np.max(np.abs(g.D - h.D)) < 1e-4 * scale + 1e-6
     assert abs(g.get_linear_weight() - h.linear_weight) < 1e-5
     assert abs(g.get_intercept() - h.intercept) < 1e-5
+
+
+def test_wdm_dataset_ppe_pipeline(ctx):
+    """wdm_run -> wdm_scoring on the GPU (src/tasks/wdm_run.cpp:79-141,
+    src/tasks/wdm_scoring.cpp:158-187): a 3-channel dual-polarization link
+    (Manakov 8/9, 4 x 100 km at 4 dBm per channel, 2^12 symbols, 16
+    samples/symbol).  WdmPPE trained on one realization raises the centre
+    channel's Q on another, with the received symbols and with their hard
+    decisions as the triplet inputs."""
+    from focss_gb300 import dsp, links
+    link = links.DualPolLink(spans=4)
+    tx_t, rx_t, _ = links.wdm_dataset(link, 1 << 12, 4.0, seed=1, ctx=ctx)
+    tx, rx, steps = links.wdm_dataset(link, 1 << 12, 4.0, seed=2, ctx=ctx)
+    assert tx.domain.modes == 6 and rx.domain.samples == 1 << 12 and steps > 4
+    ppe = WdmPPE(12, 1).train(tx_t, rx_t)
+    cut = 36
+    tc = links.centre_rows(tx)
+    q_cdc = dsp.q2_factor(tc, links.centre_rows(rx), cut)[0]
+    q_rx = dsp.q2_factor(tc, ppe.equalize(rx, rx), cut)[0]
+    q_hd = dsp.q2_factor(tc, ppe.equalize(dsp.hd(rx), rx), cut)[0]
+    print("Q cdc %.3f  ppe(rx) %.3f  ppe(hd) %.3f dB, |a| %.4f" % (q_cdc, q_rx, q_hd, abs(ppe.get_linear_weight())))
+    assert q_rx > q_cdc + 0.2 and q_hd > q_cdc + 0.2
