@@ -13,6 +13,9 @@
  *                                    src/focss/equalizer/linear.h
  *   save/load_transmission           src/focss/functions.cpp:174-221
  *   save_field / load_field          src/tasks/wdm_run.cpp:55-77, wdm_scoring.cpp:79-103
+ *   find_certainty, sd, hd           src/tasks/wdm_scoring.cpp:105-156
+ *   SINO                             src/focss/equalizer/sino.h:8-50
+ *   WdmPPE                           src/focss/equalizer/wdm_sino.h:8-71
  * so that callers such as src/tasks/systems.cpp compile against it unchanged
  * (include/focss_compat/ maps the reference's header names onto this file).
  *
@@ -760,6 +763,284 @@ class ScalarEqualizer {
         return s;
     }
     Vector<double> scalars_;
+};
+
+/* -------------------------------------------------- perturbation equalizers */
+namespace detail {
+/* x = G^-1 g for the fit's normal equations: gram is the (nf+1)^2 row-major
+ * complex matrix [Z y]^H [Z y] (upper triangle valid), G its leading nf x nf
+ * block, g its last column.  Right-looking Cholesky G = U^H U in FP64 on
+ * the upper triangle (contiguous inner loops), then U^H w = g and U x = w. */
+inline ComplexVector solve_normal_equations(const ComplexVector& gram, int nf) {
+    const size_t n = (size_t)nf, w = n + 1;
+    ComplexVector U(n * n);
+    for (size_t i = 0; i < n; ++i)
+        for (size_t j = i; j < n; ++j) U[i * n + j] = gram[i * w + j];
+    for (size_t k = 0; k < n; ++k) {
+        const double d = U[k * n + k].real();
+        if (!(d > 0)) throw gpu_error(FOCSS_ERR_INVALID_ARG, "focss: normal equations are not positive definite (rank-deficient design)");
+        const double r = std::sqrt(d);
+        U[k * n + k] = r;
+        for (size_t j = k + 1; j < n; ++j) U[k * n + j] /= r;
+        for (size_t i = k + 1; i < n; ++i) {
+            const complex_t a = std::conj(U[k * n + i]);
+            complex_t* row = &U[i * n];
+            const complex_t* top = &U[k * n];
+            for (size_t j = i; j < n; ++j) row[j] -= a * top[j];
+        }
+    }
+    ComplexVector x(n);
+    for (size_t i = 0; i < n; ++i) x[i] = gram[i * w + n];
+    for (size_t p = 0; p < n; ++p) {  // U^H w = g
+        x[p] /= U[p * n + p].real();
+        for (size_t i = p + 1; i < n; ++i) x[i] -= std::conj(U[p * n + i]) * x[p];
+    }
+    for (size_t i = n; i-- > 0;) {  // U x = w
+        complex_t acc = x[i];
+        for (size_t j = i + 1; j < n; ++j) acc -= U[i * n + j] * x[j];
+        x[i] = acc / U[i * n + i].real();
+    }
+    return x;
+}
+
+/* The coefficient table of the symmetry-reduced triplet features
+ * (src/focss/equalizer/sino.cpp:126-153, wdm_sino.cpp:105-128): R x R
+ * diamond, C(m,n) = C(n,m) = C(-m,-n) = C(-n,-m); returns the next index. */
+inline size_t fill_symmetric(ComplexVector& W, int R, const ComplexVector& raw, size_t index) {
+    const size_t w = 2 * (size_t)R + 1;
+    auto at = [&](int m, int n) -> complex_t& { return W[(size_t)(R + m) * w + (size_t)(R + n)]; };
+    for (int m = -(R / 2); m <= R / 2; ++m)
+        for (int n = std::abs(m); n <= R - std::abs(m); ++n) {
+            const complex_t v = raw[index++];
+            at(m, n) = v;
+            if (m == n) {
+                at(-m, -n) = v;
+            } else if (m == -n) {
+                at(n, m) = v;
+            } else {
+                at(n, m) = v;
+                at(-m, -n) = v;
+                at(-n, -m) = v;
+            }
+        }
+    return index;
+}
+
+/* The 16-byte complex layout shared with the C ABI's interleaved doubles. */
+inline double* cplx(ComplexVector& v) { return reinterpret_cast<double*>(v.data()); }
+inline const double* cplx(const ComplexVector& v) { return reinterpret_cast<const double*>(v.data()); }
+}  // namespace detail
+
+/* src/focss/equalizer/sino.h:8-50.  train() forms the normal equations on
+ * the GPU (focss_sino_gram) and solves them on the host in FP64: the
+ * reference's least-squares solution for a full-rank design.  lambda is kept
+ * for the interface; the reference's active solve does not use it either
+ * (sino.cpp:114-118).  Unlike the reference, train() writes no
+ * "data/mmm.csv": call save_matrix() for that file. */
+enum SinoType { ORDINARY, FIXED, HOMOGENEOUS };
+
+class SINO {
+  public:
+    SINO() : SINO(0) {}
+    explicit SINO(const int& radius) : SINO(radius, 1.0, ORDINARY) {}
+    SINO(const int& radius, const double& lambda) : SINO(radius, lambda, ORDINARY) {}
+    SINO(const int& radius, const double& lambda, const SinoType& type)
+        : radius_(radius), lambda_(lambda), type_(type), trained_(false) {}
+    SINO& set_radius(const int& radius) { radius_ = radius; trained_ = false; return *this; }
+    SINO& set_lambda(const double& lambda) { lambda_ = lambda; trained_ = false; return *this; }
+    SINO& set_type(const SinoType& type) { type_ = type; trained_ = false; return *this; }
+    SINO& set_linear_weight(const complex_t& w) { linear_weight_ = w; trained_ = false; return *this; }
+
+    /* sino.cpp:42-159 */
+    void train(const Field& transmitted, const Field& received) {
+        const int nf = focss_sino_num_features(radius_, (int)type_);
+        if (nf <= 0) throw gpu_error(FOCSS_ERR_INVALID_ARG, "focss: SINO radius must be >= 0");
+        ComplexVector gram((size_t)(nf + 1) * (nf + 1)), mean((size_t)nf + 1);
+        Vector<double> sd((size_t)nf);
+        detail::check(focss_sino_gram(gpu_context(), transmitted.handle(), received.handle(), radius_, (int)type_,
+                                      linear_weight_.real(), linear_weight_.imag(), detail::cplx(gram),
+                                      detail::cplx(mean), sd.data()),
+                      gpu_context());
+        ComplexVector raw = detail::solve_normal_equations(gram, nf);
+        complex_t dot = 0;
+        for (int i = 0; i < nf; ++i) {
+            raw[(size_t)i] /= sd[(size_t)i];
+            dot += raw[(size_t)i] * mean[(size_t)i];
+        }
+        intercept_ = mean[(size_t)nf] - dot;
+        const size_t w = 2 * (size_t)radius_ + 1;
+        weights_.assign(w * w, complex_t(0, 0));
+        const size_t next = detail::fill_symmetric(weights_, radius_, raw, 0);
+        if (type_ == ORDINARY) linear_weight_ = raw[next];
+        else if (type_ == HOMOGENEOUS) linear_weight_ = 0.0;
+        trained_ = true;
+    }
+
+    complex_t get_intercept() const { return intercept_; }
+    complex_t get_linear_weight() const { return linear_weight_; }
+    complex_t get_coo_weight() const { return weights_[(size_t)radius_ * (2 * radius_ + 1) + radius_]; }
+    /* (2R+1)^2 row-major table W(m, n) = weights()[(R+m)(2R+1) + R+n]. */
+    const ComplexVector& weights() const { return weights_; }
+
+    /* sino.cpp:180-220 */
+    Field linear(const Field& original) const { return linear_weight_ * original; }
+    Field cubic(const Field& original) const {
+        Terms t = terms();
+        Field out(original.domain(), original.batch());
+        detail::check(focss_triplet_apply(gpu_context(), original.handle(), radius_, (int)t.m.size(), t.m.data(),
+                                          t.n.data(), detail::cplx(t.c), out.mut()),
+                      gpu_context());
+        return out;
+    }
+    /* (rx - cubic(tx)) / linear_weight (sino.cpp:188-191) */
+    Field equalize(const Field& rx, const Field& tx) const { return equalize_with(rx, tx, linear_weight_); }
+    /* linear + cubic (sino.cpp:183-186): (-a x - cubic(x)) / -1 */
+    Field model(const Field& original) const {
+        return equalize_with(original * (-linear_weight_), original, complex_t(-1, 0));
+    }
+
+    void save_matrix(const std::string& filename) const {
+        std::ofstream f(filename);
+        save_matrix(f);
+    }
+    /* sino.cpp:222-259: real, imaginary, modulus and argument tables */
+    void save_matrix(std::ostream& output) const {
+        const int w = 2 * radius_ + 1;
+        for (int part = 0; part < 4; ++part) {
+            if (part) output << "\n\n";
+            for (int m = 0; m < w; ++m) {
+                for (int n = 0; n < w; ++n) {
+                    const complex_t v = weights_[(size_t)m * w + n];
+                    output << (part == 0 ? v.real() : part == 1 ? v.imag() : part == 2 ? std::abs(v) : std::arg(v))
+                           << ' ';
+                }
+                output << '\n';
+            }
+        }
+    }
+
+  private:
+    struct Terms {
+        Vector<std::int32_t> m, n;
+        ComplexVector c;
+    };
+    /* the diamond |m| + |n| <= R of the table (sino.cpp:206-214) */
+    Terms terms() const {
+        if (!trained_) throw gpu_error(FOCSS_ERR_INVALID_ARG, "focss: SINO is not trained");
+        Terms t;
+        const int w = 2 * radius_ + 1;
+        for (int m = -radius_; m <= radius_; ++m)
+            for (int n = -(radius_ - std::abs(m)); n <= radius_ - std::abs(m); ++n) {
+                t.m.push_back(m);
+                t.n.push_back(n);
+                t.c.push_back(weights_[(size_t)(m + radius_) * w + (n + radius_)]);
+            }
+        return t;
+    }
+    Field equalize_with(const Field& rx, const Field& tx, const complex_t& a) const {
+        Terms t = terms();
+        Field out(rx.domain(), rx.batch());
+        detail::check(focss_sino_equalize(gpu_context(), rx.handle(), tx.handle(), radius_, (int)t.m.size(),
+                                          t.m.data(), t.n.data(), detail::cplx(t.c), a.real(), a.imag(), out.mut()),
+                      gpu_context());
+        return out;
+    }
+
+    int radius_;
+    double lambda_;
+    SinoType type_;
+    bool trained_;
+    complex_t intercept_ = 0;
+    complex_t linear_weight_ = 0;
+    ComplexVector weights_;
+};
+
+/* src/focss/equalizer/wdm_sino.h:8-71 with Fields in place of arma::cx_mat:
+ * inputs are 6-row Fields (rows channel * 2 + polarization: left neighbour
+ * 0-1, centre 2-3, right neighbour 4-5, the layout load_field returns for
+ * 3 channels x 2 modes); outputs are 2-row Fields (the centre channel).
+ * train() forms the normal equations on the GPU (focss_wdm_ppe_gram) and
+ * solves them on the host in FP64. */
+class WdmPPE {
+  public:
+    WdmPPE() : WdmPPE(0, 0) {}
+    explicit WdmPPE(const int& radii) : WdmPPE(radii, radii) {}
+    WdmPPE(const int& c_radius, const int& d_radius) : c_(c_radius), d_(d_radius), trained_(false) {}
+    WdmPPE& set_c_radius(const int& c_radius) { c_ = c_radius; trained_ = false; return *this; }
+    WdmPPE& set_d_radius(const int& d_radius) { d_ = d_radius; trained_ = false; return *this; }
+
+    /* wdm_sino.cpp:28-142 */
+    void train(const Field& tx, const Field& rx) {
+        const int nf = focss_wdm_ppe_num_features(c_, d_);
+        ComplexVector gram((size_t)(nf + 1) * (nf + 1)), mean((size_t)nf + 1);
+        Vector<double> sd((size_t)nf);
+        detail::check(focss_wdm_ppe_gram(gpu_context(), tx.handle(), rx.handle(), c_, d_, detail::cplx(gram),
+                                         detail::cplx(mean), sd.data()),
+                      gpu_context());
+        ComplexVector raw = detail::solve_normal_equations(gram, nf);
+        complex_t dot = 0;
+        for (int i = 0; i < nf; ++i) {
+            raw[(size_t)i] /= sd[(size_t)i];
+            dot += raw[(size_t)i] * mean[(size_t)i];
+        }
+        intercept_ = mean[(size_t)nf] - dot;
+        size_t index = 0;
+        C_.assign(c_ >= 0 ? (size_t)(2 * c_ + 1) * (2 * c_ + 1) : 0, complex_t(0, 0));
+        D_.assign(d_ >= 0 ? (size_t)(2 * d_ + 1) * (2 * d_ + 1) : 0, complex_t(0, 0));
+        if (c_ >= 0) index = detail::fill_symmetric(C_, c_, raw, 0);
+        for (int m = -d_; m <= d_; ++m)
+            for (int n = -(d_ - std::abs(m)); n <= d_ - std::abs(m); ++n)
+                D_[(size_t)(d_ + m) * (2 * d_ + 1) + (d_ + n)] = raw[index++];
+        linear_weight_ = raw[index];
+        trained_ = true;
+    }
+
+    complex_t get_intercept() const { return intercept_; }
+    complex_t get_linear_weight() const { return linear_weight_; }
+    complex_t get_coo_weight() const { return C_[(size_t)c_ * (2 * c_ + 1) + c_]; }
+    /* (2c+1)^2 and (2d+1)^2 row-major tables, C(m, n) = C_table()[(c+m)(2c+1) + c+n] */
+    const ComplexVector& C_table() const { return C_; }
+    const ComplexVector& D_table() const { return D_; }
+
+    /* wdm_sino.cpp:235-300 */
+    Field linear(const Field& field) const { return apply(nullptr, nullptr, nullptr, &field); }
+    Field spm(const Field& field) const { return apply(&field, nullptr, nullptr, nullptr); }
+    Field xpm(const Field& field) const { return apply(nullptr, &field, nullptr, nullptr); }
+    Field cubic(const Field& field) const {
+        return apply(c_ >= 0 ? &field : nullptr, d_ >= 0 ? &field : nullptr, nullptr, nullptr);
+    }
+    Field model(const Field& field) const {
+        return apply(c_ >= 0 ? &field : nullptr, d_ >= 0 ? &field : nullptr, nullptr, &field);
+    }
+    Field equalize(const Field& tx, const Field& rx) const { return equalize(tx, tx, rx); }
+    Field equalize(const Field& tx_spm, const Field& tx_xpm, const Field& rx) const {
+        return apply(c_ >= 0 ? &tx_spm : nullptr, d_ >= 0 ? &tx_xpm : nullptr, &rx, nullptr);
+    }
+
+  private:
+    Field apply(const Field* spm_in, const Field* xpm_in, const Field* rx, const Field* lin_in) const {
+        if (!trained_) throw gpu_error(FOCSS_ERR_INVALID_ARG, "focss: WdmPPE is not trained");
+        const Field* ref = spm_in ? spm_in : xpm_in ? xpm_in : lin_in ? lin_in : rx;
+        Domain dom = ref->domain();
+        dom.modes = 2;
+        Field out(dom, ref->batch());
+        const complex_t zero[1] = {complex_t(0, 0)};
+        detail::check(
+            focss_wdm_ppe_apply(gpu_context(), spm_in ? spm_in->handle() : nullptr,
+                                xpm_in ? xpm_in->handle() : nullptr, rx ? rx->handle() : nullptr,
+                                lin_in ? lin_in->handle() : nullptr, c_,
+                                C_.empty() ? reinterpret_cast<const double*>(zero) : detail::cplx(C_), d_,
+                                D_.empty() ? reinterpret_cast<const double*>(zero) : detail::cplx(D_),
+                                linear_weight_.real(), linear_weight_.imag(), out.mut()),
+            gpu_context());
+        return out;
+    }
+
+    int c_, d_;
+    bool trained_;
+    complex_t intercept_ = 0;
+    complex_t linear_weight_ = 0;
+    ComplexVector C_, D_;
 };
 
 }  // namespace focss

@@ -20,6 +20,7 @@ from conftest import ALPHA, BETA2, F0, GAMMA, ROOT, rel_l2
 INC = os.path.join(ROOT, "include")
 LIB = os.path.join(ROOT, "focss_gb300", "libfocss_gpu.so")
 SRC = os.path.join(ROOT, "tests", "cpp", "facade_link.cpp")
+PPE_SRC = os.path.join(ROOT, "tests", "cpp", "facade_ppe.cpp")
 
 
 def _cxx():
@@ -29,12 +30,12 @@ def _cxx():
     return cxx
 
 
-def _build_example(tmp_path):
+def _build_example(tmp_path, src=SRC):
     if not os.path.exists(LIB):
         from focss_gb300 import build as gbuild
         gbuild.build()
-    exe = str(tmp_path / "facade_link")
-    cmd = [_cxx(), "-std=c++17", "-O2", "-Wall", "-Werror", "-I" + INC, SRC, LIB,
+    exe = str(tmp_path / os.path.splitext(os.path.basename(src))[0])
+    cmd = [_cxx(), "-std=c++17", "-O2", "-Wall", "-Werror", "-I" + INC, src, LIB,
            "-Wl,-rpath," + os.path.dirname(LIB), "-o", exe]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
@@ -43,6 +44,7 @@ def _build_example(tmp_path):
 
 def test_facade_example_builds(tmp_path):
     _build_example(tmp_path)
+    _build_example(tmp_path, PPE_SRC)
 
 
 def test_reference_caller_compiles_against_facade(tmp_path):
@@ -103,3 +105,55 @@ def test_facade_link_matches_oracle(tmp_path, oracle_cpu):
     np.testing.assert_array_equal(dec, cpu.hd_sequence(s))
     assert rel_l2(rx, s) < 1e-4
     assert abs(cert_gpu - cpu.find_certainty(tx, rx)) < 1e-12
+
+
+@pytest.mark.gpu
+def test_facade_perturbation_equalizers_match_oracle(tmp_path, oracle_cpu):
+    """WdmPPE(8, 2) and SINO(6) trained through the C++ facade agree with the
+    FP64 least-squares restatements (oracle/wdm_ppe_ref.py, the numpy SINO fit)
+    on a synthetic 3-channel dual-polarization link with known tables, and
+    their equalizer / model outputs match the oracle's to FP32 rounding."""
+    from oracle import wdm_ppe_ref as W
+    from focss_gb300 import sino
+    exe = _build_example(tmp_path, PPE_SRC)
+    rng = np.random.default_rng(17)
+    n, c, d = 1 << 13, 8, 2
+    gray = np.array([complex(a, b) for b in (-3, -1, 3, 1) for a in (-3, -1, 3, 1)]) / np.sqrt(10)
+    tx = gray[rng.integers(0, 16, (6, n))].astype(np.complex64).astype(np.complex128)
+    truth = W.WdmPPE(c, d).install((rng.standard_normal(W.n_features(c, d)) +
+                                    1j * rng.standard_normal(W.n_features(c, d))) * 0.01)
+    truth.linear_weight = 0.9 - 0.2j
+    rx = tx.copy()
+    rx[2:4] = truth.model(tx) + 1e-3 * (rng.standard_normal((2, n)) + 1j * rng.standard_normal((2, n)))
+    rx = rx.astype(np.complex64).astype(np.complex128)
+    tx.tofile(tmp_path / "tx.c128")
+    rx.tofile(tmp_path / "rx.c128")
+    prefix = str(tmp_path / "out")
+    r = subprocess.run([exe, str(tmp_path / "tx.c128"), str(tmp_path / "rx.c128"), str(n), prefix],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    rd = lambda k, shape: np.fromfile(prefix + k, np.complex128).reshape(shape)  # noqa: E731
+    sc = np.loadtxt(prefix + "_scalars.txt")
+    ref = W.WdmPPE(c, d).train(tx, rx)
+    scale = np.max(np.abs(ref.C))
+    assert np.max(np.abs(rd("_wdm_C.c128", ref.C.shape) - ref.C)) < 1e-4 * scale
+    assert np.max(np.abs(rd("_wdm_D.c128", ref.D.shape) - ref.D)) < 1e-4 * scale
+    assert abs(complex(sc[0], sc[1]) - ref.linear_weight) < 1e-5
+    assert abs(complex(sc[2], sc[3]) - ref.intercept) < 1e-5
+    assert rel_l2(rd("_wdm_eq.c128", (2, n)), ref.equalize(tx, rx)) < 1e-5
+    assert rel_l2(rd("_wdm_model.c128", (2, n)), ref.model(tx)) < 1e-5
+    s = sino.SINO(6).train(tx[2:4], rx[2:4], solver="lstsq")
+    sscale = np.max(np.abs(s.weights))
+    assert np.max(np.abs(rd("_sino_W.c128", s.weights.shape) - s.weights)) < 1e-4 * sscale
+    assert abs(complex(sc[4], sc[5]) - s.linear_weight) < 1e-5
+    assert abs(complex(sc[6], sc[7]) - s.intercept) < 1e-5
+    R = 6
+    k = np.arange(R, n - R)
+    eq_ref = rx[2:4].copy()
+    for (m, nn, cf) in zip(*s.terms()):
+        eq_ref[:, k] -= cf * sino._term(tx[2:4], k, m, nn)
+    eq_ref /= s.linear_weight
+    assert rel_l2(rd("_sino_eq.c128", (2, n)), eq_ref) < 1e-5
+    model_ref = s.linear_weight * tx[2:4] + (rx[2:4] - s.linear_weight * eq_ref)
+    assert rel_l2(rd("_sino_model.c128", (2, n)), model_ref) < 1e-5
+    assert abs(sc[8] - oracle_cpu.find_certainty(tx, rx)) < 1e-9
