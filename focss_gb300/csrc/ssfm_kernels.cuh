@@ -323,14 +323,22 @@ __global__ void __launch_bounds__(R* PQ<N2>::P, 2) row_kernel(const PassArgs a) 
     if (op == ROW_SSFM) {
         // exp(-alpha hl/2)/N * exp(i beta2/2 hl w_k^2) (ssfm.cpp:142-158), w_k = k' dw,
         // phase in turns = a k'^2 mod 1 formed exactly from the 96-bit fraction.
+        // The thread's own bins go through its column of the exchange buffer
+        // so that this long per-bin body is emitted once (a rolled loop), not
+        // Q times: the unrolled kernel overflowed the instruction cache.
+        float2* mine = sx + lay(0, t);
 #pragma unroll
+        for (int j = 0; j < Q; ++j) mine[j * (P + 1)] = v[j];
+#pragma unroll 1
         for (int j = 0; j < Q; ++j) {
             const int k = k1 + N1 * (t + P * j);
             const unsigned long long kp = (unsigned long long)(k <= (N >> 1) ? k : N - k);
             const unsigned long long kk = kp * kp;
             const unsigned long long X = dhi * kk + __umul64hi(dlo, kk);
-            v[j] = turns_rotate(cscale(v[j], g), X, s_T);
+            mine[j * (P + 1)] = turns_rotate(cscale(mine[j * (P + 1)], g), X, s_T);
         }
+#pragma unroll
+        for (int j = 0; j < Q; ++j) v[j] = mine[j * (P + 1)];
     } else if (op == ROW_TABLE) {
         const float2* tb = a.table + (size_t)k1 * N2 + t;
 #pragma unroll
