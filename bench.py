@@ -458,7 +458,8 @@ def sweep_section(fg, ctx, stream):
     in -4..+4 dBm, 8 samples/symbol, 15 x 80 km SSMF with ASE.  All lengths
     are one span-loop graph launch for the forward propagation and one for
     DBP at 1/2/4/8/16 steps per span (25 fields); the FFT split of every
-    length is picked by the autotuner first."""
+    length (forward and DBP; -1 = the single-CTA kernel) is picked by the
+    autotuner first."""
     import torch
     from focss_gb300 import dsp
     alpha, beta2, gamma = fiber_params()
@@ -505,6 +506,8 @@ def sweep_section(fg, ctx, stream):
     fwd_ss = float(sum(int(st.sum()) * f.domain.samples for st, f in zip(steps, work)))
 
     rx = [dsp.decimate(w, osf // dosf) for w in work]
+    for r in rx:  # DBP lengths too (2^12..2^14 may take the single-CTA kernel)
+        tuned[r.domain.samples] = fg.autotune(r.domain.samples, r.batch, ctx=ctx)[0]
     ks = sw["dbp_steps_per_span"]
     dbp = [r.copy() for k in ks for r in rx]
     ssfms = [fg.SSFM(fib, k) for k in ks for _ in rx]
@@ -683,7 +686,12 @@ def run_ncu_case(args):
           |m|+|n| <= 32 with decaying random coefficients;
     ldbp  learned-DBP forward + backward, 20 spans x 2 steps, 63/255 taps,
           8 x 2^16 samples;
-    cnn   correction-CNN forward + backward, 8 x 2^15 symbols."""
+    cnn   correction-CNN forward + backward, 8 x 2^15 symbols;
+    fit   SINO normal equations (features, z-scores, FP64-accumulated Gram),
+          R = 32 (577 features) on 2^17 symbols x 2 modes;
+    wdmppe  WdmPPE (c, d) = (30, 3): equalizer on 16 x 6-row realizations of
+          2^18 symbols (201 MB in, 67 MB out), then the fit's features on one
+          6-row realization of 2^16 symbols."""
     import focss_gb300 as fg
     from focss_gb300 import dsp
     ctx = fg.Context(0)
@@ -728,6 +736,24 @@ def run_ncu_case(args):
         net.set_params(he_init(rng))
         net.forward(y)
         net.loss_grad(y, y)
+    elif kind == "fit":
+        from focss_gb300 import sino
+        ns = 2 ** 17
+        tx = dsp.qam16_map(rng.integers(0, 16, (1, 2, ns)), fg.Domain(2, ns, 1 / 32e9, F0), ctx=ctx)
+        rx = tx.copy()
+        sino.SINO(32).train(tx, rx, solver="gpu")
+    elif kind == "wdmppe":
+        c, d, ns, B = 30, 3, 2 ** 18, 16
+        codes = rng.integers(0, 16, (B, 6, ns))
+        tx = dsp.qam16_map(codes, fg.Domain(6, ns, 1 / 32e9, F0), batch=B, ctx=ctx)
+        ppe = fg.WdmPPE(c, d)
+        nf = int(fg.lib().focss_wdm_ppe_num_features(c, d))
+        ppe.install((rng.standard_normal(nf) + 1j * rng.standard_normal(nf)) * 1e-3)
+        ppe.linear_weight = 1.0
+        for _ in range(2):
+            ppe.equalize(tx, tx)
+        t1 = dsp.qam16_map(codes[:1, :, :2 ** 16], fg.Domain(6, 2 ** 16, 1 / 32e9, F0), ctx=ctx)
+        fg.WdmPPE(c, d).train(t1, t1)
     else:
         raise SystemExit("unknown ncu case %r" % kind)
     ctx.sync()
@@ -738,7 +764,7 @@ def run_ncu_case(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ncu-case", nargs="?", const="ssfm", default=None,
-                    help="small fixed case for ncu captures: ssfm (default), ppe, ldbp, cnn")
+                    help="small fixed case for ncu captures: ssfm (default), ppe, ldbp, cnn, fit, wdmppe")
     ap.add_argument("--ncu-batch", type=int, default=40)
     ap.add_argument("--split", type=int, default=0, help="ncu case: log2 N1 of the FFT split (0: balanced)")
     ap.add_argument("--gpus", type=int, default=1)

@@ -358,17 +358,22 @@ def span_loop(fields, fiber: Fiber, ssfms, spans: int, direction: float = SSFM.F
 
 
 def autotune(samples: int, batch: int, ctx: Context | None = None):
-    """Time every admissible FFT split of length `samples` on `batch`
-    realizations and keep the fastest for this context's split-step runs.
-    Returns (log2 N1, ms per step)."""
+    """Time every admissible FFT split of length `samples` (and, for
+    2^12..2^14, the single-CTA kernel) on `batch` realizations and keep the
+    fastest for this context's split-step runs.  Returns (log2 N1 or
+    SPLIT_SINGLE_CTA, ms per step)."""
     ctx = ctx or Context.default()
     l1, ms = C.c_int(), C.c_double()
     check(lib().focss_autotune(ctx.h, samples, batch, C.byref(l1), C.byref(ms)), ctx.h)
     return l1.value, ms.value
 
 
+SPLIT_SINGLE_CTA = -1  # FOCSS_SPLIT_SINGLE_CTA: one CTA per realization, field in shared memory
+
+
 def set_fft_split(samples: int, log2_n1: int, ctx: Context | None = None):
-    """Pin the split of length-`samples` split-step runs (0 = balanced default)."""
+    """Pin the split of length-`samples` split-step runs (0 = balanced
+    default, SPLIT_SINGLE_CTA = the single-CTA kernel for 2^12..2^14)."""
     ctx = ctx or Context.default()
     check(lib().focss_set_fft_split(ctx.h, samples, log2_n1), ctx.h)
 

@@ -145,6 +145,15 @@ PassArgs ssfm_args(const Field* f, const focss_fiber& fib, const focss_ssfm_opts
                    int* n_done);
 // The plan ssfm_run uses for length N (autotuned or pinned split, else balanced).
 focss_status ssfm_plan(Ctx* ctx, int N, const Plan** out);
+// Split value selecting the single-CTA kernel (ssfm_block.cu) for a length.
+constexpr int kSingleCta = -1;
+// log2 N1 of the single-CTA kernel's split for length N, 0 if it has none.
+int block_split(int N);
+// One launch running the whole SSFM of `batch` single-mode realizations, at
+// most `cap` column phases each (plan split must be block_split(N)).
+cudaError_t launch_block(const Plan& p, PassArgs a, int batch, int cap, cudaStream_t s);
+// True when field f's SSFM runs take the single-CTA kernel.
+bool ssfm_single_cta(const Ctx* ctx, const Field* f);
 
 // Amplifier operation `op` (FOCSS_AMP_*) as A <- scale*A + sigma*(z0 + i z1);
 // false for an unknown op (capi.cu).

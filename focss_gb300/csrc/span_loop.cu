@@ -97,7 +97,7 @@ std::string loop_key(int nf, Field* const* fs, const focss_fiber& fib, const foc
         auto it = ctx->ssfm_split.find(f->samples);
         std::snprintf(buf, sizeof buf, "%p %d %d %d %a %a %d %d %a %a %d;", (void*)f->d, f->modes, f->samples,
                       f->batch, f->dt, f->f0, opts[i].grid, opts[i].total_steps, opts[i].maximum_phase_shift,
-                      opts[i].maximum_step_size, it == ctx->ssfm_split.end() ? -1 : it->second);
+                      opts[i].maximum_step_size, it == ctx->ssfm_split.end() ? -99 : it->second);
         k += buf;
     }
     return k;
@@ -155,7 +155,11 @@ cudaError_t record_branch(Ctx* ctx, LoopGraph* g, int i, Field* f, const Plan& p
         if (e == cudaSuccess) e = cudaMemsetAsync(state, 0, sizeof(SsfmState) * B, s);
         if (e == cudaSuccess) e = cudaMemsetAsync(ctr, 0, sizeof(int) * 2, s);  // [0], [1]: per span
         if (e != cudaSuccess) break;
-        if (o.grid == FOCSS_UNIFORM) {
+        if (ssfm_single_cta(ctx, f)) {
+            // the whole span in one launch (single-CTA kernel), bounded like the loop below
+            e = launch_block(p, a, B, o.grid == FOCSS_UNIFORM ? o.total_steps + 2 : (int)kMaxPairs, s);
+            g->static_kernels += 1;
+        } else if (o.grid == FOCSS_UNIFORM) {
             for (int k = 0; k < o.total_steps + 2 && e == cudaSuccess; ++k) {
                 e = launch_col(p, a, B, s);
                 if (e == cudaSuccess) e = launch_row(p, a, B, s);
@@ -359,6 +363,12 @@ FOCSS_API focss_status focss_set_fft_split(focss_ctx* c, int samples, int log2_n
         c->ssfm_split.erase(samples);
         return FOCSS_OK;
     }
+    if (log2_n1 == fg::kSingleCta) {
+        if (!fg::block_split(samples))
+            return fg::set_error(c, FOCSS_ERR_UNSUPPORTED, "set_fft_split: the single-CTA kernel covers 2^12..2^14");
+        c->ssfm_split[samples] = log2_n1;
+        return FOCSS_OK;
+    }
     if (!fg::split_supported(samples, log2_n1))
         return fg::set_error(c, FOCSS_ERR_UNSUPPORTED, "set_fft_split: split outside [2^4, 2^10] x [2^4, 2^10]");
     c->ssfm_split[samples] = log2_n1;
@@ -390,11 +400,17 @@ FOCSS_API focss_status focss_autotune(focss_ctx* c, int samples, int batch, int*
     const focss_fiber fib{0.2e-3 * std::log(10.0) / 10, -2.168e-26, 1.3e-3, 8e3, 1.55e-6, 1.0};
     const focss_ssfm_opts o{FOCSS_UNIFORM, 8, 0.0, 0.0};
     const auto saved = c->ssfm_split;
-    int best = -1;
+    // candidates: every two-pass split, and the single-CTA kernel where it exists
+    std::vector<int> cands;
+    for (int l1 = 4; l1 <= 10; ++l1)
+        if (fg::split_supported(samples, l1)) cands.push_back(l1);
+    if (fg::block_split(samples)) cands.push_back(fg::kSingleCta);
+    constexpr int kNone = -100;
+    int best = kNone;
     double best_ms = 1e300;
     focss_status st = fg::cuda_check(c, e, "autotune set-up");
-    for (int l1 = 4; l1 <= 10 && st == FOCSS_OK; ++l1) {
-        if (!fg::split_supported(samples, l1)) continue;
+    for (size_t ci = 0; ci < cands.size() && st == FOCSS_OK; ++ci) {
+        const int l1 = cands[ci];
         c->ssfm_split[samples] = l1;
         st = fg::ssfm_run(c, &f, fib, o, FOCSS_FORWARD, nullptr);  // warm-up (plan, attributes)
         if (st != FOCSS_OK) break;
@@ -420,7 +436,7 @@ FOCSS_API focss_status focss_autotune(focss_ctx* c, int samples, int batch, int*
     cudaFree(f.d);
     c->ssfm_split = saved;
     if (st != FOCSS_OK) return st;
-    if (best < 0) return fg::set_error(c, FOCSS_ERR_UNSUPPORTED, "autotune: no admissible split");
+    if (best == kNone) return fg::set_error(c, FOCSS_ERR_UNSUPPORTED, "autotune: no admissible split");
     c->ssfm_split[samples] = best;
     if (log2_n1) *log2_n1 = best;
     if (ms_per_step) *ms_per_step = best_ms;

@@ -212,8 +212,17 @@ PassArgs ssfm_args(const Field* f, const focss_fiber& fib, const focss_ssfm_opts
 
 focss_status ssfm_plan(Ctx* ctx, int N, const Plan** out) {
     auto it = ctx->ssfm_split.find(N);
-    return get_plan_split(ctx, N, it != ctx->ssfm_split.end() ? it->second : default_split(N), out);
+    int l1 = it != ctx->ssfm_split.end() ? it->second : default_split(N);
+    if (l1 == kSingleCta) l1 = block_split(N);
+    return get_plan_split(ctx, N, l1, out);
 }
+
+bool ssfm_single_cta(const Ctx* ctx, const Field* f) {
+    auto it = ctx->ssfm_split.find(f->samples);
+    return it != ctx->ssfm_split.end() && it->second == kSingleCta && f->modes == 1 && block_split(f->samples) != 0;
+}
+
+focss_status ssfm_finish(Ctx* ctx, Field* f, const focss_ssfm_opts& o, int* steps_out);
 
 focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ssfm_opts& o, double dir,
                       int* steps_out) {
@@ -237,6 +246,11 @@ focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ss
         cap = (long long)o.total_steps + 2;
     } else {
         cap = 1ll << 17;  // ~100x the step count of a 0.005 rad/step span at +11 dBm
+    }
+    if (ssfm_single_cta(ctx, f)) {
+        st = cuda_check(ctx, launch_block(*p, a, f->batch, (int)std::min<long long>(cap, 1 << 30), s), "ssfm block");
+        if (st != FOCSS_OK) return st;
+        return ssfm_finish(ctx, f, o, steps_out);
     }
     const int chunk = 16;
     long long launched = 0;
@@ -290,6 +304,14 @@ focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ss
         }
     }
     if (ev) cudaEventDestroy(ev);
+    return ssfm_finish(ctx, f, o, steps_out);
+}
+
+// Reads the step states back after a run: every realization must be idle;
+// steps_out gets the step counts.
+focss_status ssfm_finish(Ctx* ctx, Field* f, const focss_ssfm_opts& o, int* steps_out) {
+    cudaStream_t s = ctx->stream;
+    focss_status st;
     std::vector<SsfmState> hs(f->batch);
     st = cuda_check(ctx,
                     cudaMemcpyAsync(hs.data(), ctx->d_state, sizeof(SsfmState) * f->batch,

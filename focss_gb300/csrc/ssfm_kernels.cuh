@@ -133,61 +133,44 @@ __device__ __noinline__ static void ssfm_advance(SsfmState& s, const SsfmParams&
 }
 
 // ---------------------------------------------------------------- column pass
-// A CTA holds the same C columns of every mode of one realization (a.modes
-// groups of C*P threads; 1 or 2 modes), so the Kerr phase can use the power
-// summed over modes (Field::power, src/focss/field.cpp:164-171).  The launch
-// bound (2 groups, 1 CTA) keeps the same 128-register budget as 1 group x 2 CTAs.
+// The work of one thread group (C columns x P threads, `gt` its thread index)
+// on columns [n2_0, n2_0 + C) of one mode of one realization; `data` points
+// at that mode's first sample (row stride N2; global memory in the two-pass
+// kernels, shared memory in the single-CTA kernel).  `sB` holds the six-step
+// factors W_N^{n2 a1 j} of these columns at sB[j * sB_stride + c].  Adds the
+// time-domain field's peak and sum of |A|^2 to pk / sm.
 template <int N1, int C>
-__global__ void __launch_bounds__(2 * C * ColFFT<N1>::P, 1) col_kernel(const PassArgs a) {
+__device__ __forceinline__ void col_work(const PassArgs& a, int op, const SsfmState* st, float2* data, int n2_0,
+                                         const float4* s_fc, const float4* sB, int sB_stride, float2* sx,
+                                         float2* s_x0, int mo, int modes, int gt, float& pk, float& sm) {
     constexpr int P = ColFFT<N1>::P, Q = ColFFT<N1>::Q;
     constexpr bool PAIR = ColFFT<N1>::PAIR;
-    extern __shared__ float4 smem4[];
-    float4* s_fc = smem4;                                  // column sub-FFT twiddles, (u,t) order
-    float4* s_B = s_fc + N1;                               // six-step factors W_N^{n2 P j}, [j][c]
-    float2* s_x0 = reinterpret_cast<float2*>(s_B + Q * C); // exchange buffers, N1*C per mode
-    const int mo = threadIdx.x / (C * P);                  // mode of this thread group
-    float2* sx = s_x0 + (size_t)mo * N1 * C;
-    __shared__ float red[64];
-
-    const int b = blockIdx.y;
-    SsfmState* st = a.state ? a.state + b : nullptr;
-    int op = a.op;
-    if (st) {
-        op = *(volatile int*)&st->action;
-        if (op == COL_IDLE) return;
-    }
     const int N2 = a.N2;
     // Element j of a thread is time-domain row t + P j; in the spectral
     // layout it is row a0 + a1 j (a0 = t, a1 = P for the PQ form; lane-pair
     // form: a0 = (t>>1) + Q^2 (t&1), a1 = Q).  Six-step twiddle of column n2:
-    // W_N^{n2 (a0 + a1 j)} = W_N^{n2 a0} (per thread) x W_N^{n2 a1 j} (per CTA
-    // table over j and the C columns), each a quarter turn times a lifting
-    // rotation whose inverse mirrors it exactly.
+    // W_N^{n2 (a0 + a1 j)} = W_N^{n2 a0} (per thread) x W_N^{n2 a1 j} (per
+    // column table over j), each a quarter turn times a lifting rotation whose
+    // inverse mirrors it exactly.
     constexpr int a1 = PAIR ? Q : P;
     const int log2N = a.log2N2 + ilog2c(N1);
-    for (int i = threadIdx.x; i < N1; i += blockDim.x) s_fc[i] = a.tw[i];
-    for (int i = threadIdx.x; i < Q * C; i += blockDim.x)
-        s_B[i] = sixstep_factor((blockIdx.x * C + i % C) * a1 * (i / C), log2N);
-
-    const int modes = a.modes > 1 ? a.modes : 1;
-    const int c = threadIdx.x % C, t = (threadIdx.x / C) % P;
+    const int c = gt % C, t = (gt / C) % P;
     const int a0 = PAIR ? (t >> 1) + Q * Q * (t & 1) : t;
-    const int n2 = blockIdx.x * C + c;
+    const int n2 = n2_0 + c;
     const float4 fa = sixstep_factor(n2 * a0, log2N);
     const float2 tsA = make_float2(fa.x, fa.y);
     const int qA = __float_as_int(fa.z);
-    float2* base = a.data + ((size_t)b * modes + mo) * a.N + n2;
+    float2* base = data + n2;
     float2 v[Q];
 #pragma unroll
     for (int j = 0; j < Q; ++j) v[j] = base[(size_t)(op == COL_FWD ? t + P * j : a0 + a1 * j) * N2];
     __syncthreads();
 
     const ColLayout<P, C> lay{c};
-    float pk = 0.0f, sm = 0.0f;
     if (op != COL_FWD) {
 #pragma unroll
         for (int j = 0; j < Q; ++j) {
-            const float4 fb = s_B[j * C + c];
+            const float4 fb = sB[j * sB_stride + c];
             v[j] = lift_rot_inv(lift_rot_inv(quarter_turns(v[j], -(qA + __float_as_int(fb.z)) & 3),
                                              make_float2(fb.x, fb.y)),
                                 tsA);
@@ -257,12 +240,45 @@ __global__ void __launch_bounds__(2 * C * ColFFT<N1>::P, 1) col_kernel(const Pas
             fft_pq_lift<P, Q, true>(v, sx, lay, t, s_fc);
 #pragma unroll
         for (int j = 0; j < Q; ++j) {
-            const float4 fb = s_B[j * C + c];
+            const float4 fb = sB[j * sB_stride + c];
             v[j] = quarter_turns(lift_rot(lift_rot(v[j], tsA), make_float2(fb.x, fb.y)), qA + __float_as_int(fb.z));
         }
     }
 #pragma unroll
     for (int j = 0; j < Q; ++j) base[(size_t)(op == COL_INV ? t + P * j : a0 + a1 * j) * N2] = v[j];
+}
+
+// A CTA holds the same C columns of every mode of one realization (a.modes
+// groups of C*P threads; 1 or 2 modes), so the Kerr phase can use the power
+// summed over modes (Field::power, src/focss/field.cpp:164-171).  The launch
+// bound (2 groups, 1 CTA) keeps the same 128-register budget as 1 group x 2 CTAs.
+template <int N1, int C>
+__global__ void __launch_bounds__(2 * C * ColFFT<N1>::P, 1) col_kernel(const PassArgs a) {
+    constexpr int P = ColFFT<N1>::P, Q = ColFFT<N1>::Q;
+    constexpr int a1 = ColFFT<N1>::PAIR ? Q : P;
+    extern __shared__ float4 smem4[];
+    float4* s_fc = smem4;                                  // column sub-FFT twiddles, (u,t) order
+    float4* s_B = s_fc + N1;                               // six-step factors W_N^{n2 a1 j}, [j][c]
+    float2* s_x0 = reinterpret_cast<float2*>(s_B + Q * C); // exchange buffers, N1*C per mode
+    const int mo = threadIdx.x / (C * P);                  // mode of this thread group
+    float2* sx = s_x0 + (size_t)mo * N1 * C;
+    __shared__ float red[64];
+
+    const int b = blockIdx.y;
+    SsfmState* st = a.state ? a.state + b : nullptr;
+    int op = a.op;
+    if (st) {
+        op = *(volatile int*)&st->action;
+        if (op == COL_IDLE) return;
+    }
+    const int log2N = a.log2N2 + ilog2c(N1);
+    for (int i = threadIdx.x; i < N1; i += blockDim.x) s_fc[i] = a.tw[i];
+    for (int i = threadIdx.x; i < Q * C; i += blockDim.x)
+        s_B[i] = sixstep_factor((blockIdx.x * C + i % C) * a1 * (i / C), log2N);
+    const int modes = a.modes > 1 ? a.modes : 1;
+    float pk = 0.0f, sm = 0.0f;
+    col_work<N1, C>(a, op, st, a.data + ((size_t)b * modes + mo) * a.N, blockIdx.x * C, s_fc, s_B, C, sx, s_x0, mo,
+                    modes, threadIdx.x % (C * P), pk, sm);
 
     if (st) {
         block_max_sum(pk, sm, red);
@@ -288,36 +304,21 @@ __global__ void __launch_bounds__(2 * C * ColFFT<N1>::P, 1) col_kernel(const Pas
 }
 
 // ---------------------------------------------------------------- row pass
-template <int N2, int R>
-__global__ void __launch_bounds__(R* PQ<N2>::P, 2) row_kernel(const PassArgs a) {
+// The work of the P threads of row k1 (`rl` the row's slot in the exchange
+// buffer, t the thread in the row) of one mode; `data` points at that mode's
+// first sample (global or shared memory).  ROW_SSFM applies exp(-alpha hl/2)/N
+// (FP32 gain g) times the dispersion phase from the 96-bit fraction dhi/dlo.
+template <int N2>
+__device__ __forceinline__ void row_work(const PassArgs& a, int op, float2* data, int k1, int rl, int t,
+                                         const float4* s_tw, const float4* s_T, float2* sx, float g,
+                                         unsigned long long dhi, unsigned long long dlo) {
     constexpr int P = PQ<N2>::P, Q = PQ<N2>::Q;
-    extern __shared__ float4 smem4[];
-    float4* s_tw = smem4;                                    // W_N2^e (double-float)
-    float4* s_T = s_tw + N2;                                 // exp(2 pi i j/512)
-    float2* sx = reinterpret_cast<float2*>(s_T + 512);       // R * Q * (P+1)
-
-    const int b = blockIdx.y;  // realization * modes + mode
-    const SsfmState* st = a.state ? a.state + b / (a.modes > 1 ? a.modes : 1) : nullptr;
-    unsigned long long dhi = 0ull, dlo = 0ull;
-    float g = a.scale;
-    if (st) {
-        if (!*(volatile const int*)&st->row_active) return;
-        dhi = st->disp_hi;
-        dlo = st->disp_lo << 32;
-        g = st->lin_gain;
-    }
-    for (int i = threadIdx.x; i < N2; i += blockDim.x) s_tw[i] = a.tw[a.N1 + i];
-    if (st)
-        for (int i = threadIdx.x; i < 512; i += blockDim.x) s_T[i] = a.tw[2 * a.N1 + 2 * N2 + i];
-    const int rl = threadIdx.x / P, t = threadIdx.x % P;
-    const int k1 = blockIdx.x * R + rl;
-    float2* base = a.data + (size_t)b * a.N + (size_t)k1 * N2 + t;
+    float2* base = data + (size_t)k1 * N2 + t;
     float2 v[Q];
 #pragma unroll
     for (int j = 0; j < Q; ++j) v[j] = base[P * j];
     __syncthreads();
     const RowLayout<P> lay{rl * Q * (P + 1)};
-    const int op = st ? (int)ROW_SSFM : a.op;
     if (op != ROW_INV) fft_pq<P, Q, false, false>(v, sx, lay, t, s_tw);
     const int N = a.N, N1 = a.N1;
     if (op == ROW_SSFM) {
@@ -356,6 +357,110 @@ __global__ void __launch_bounds__(R* PQ<N2>::P, 2) row_kernel(const PassArgs a) 
     if (op != ROW_FWD) fft_pq<P, Q, true, false>(v, sx, lay, t, s_tw);
 #pragma unroll
     for (int j = 0; j < Q; ++j) base[P * j] = v[j];
+}
+
+template <int N2, int R>
+__global__ void __launch_bounds__(R* PQ<N2>::P, 2) row_kernel(const PassArgs a) {
+    constexpr int P = PQ<N2>::P;
+    extern __shared__ float4 smem4[];
+    float4* s_tw = smem4;                                    // W_N2^e (double-float)
+    float4* s_T = s_tw + N2;                                 // exp(2 pi i j/512)
+    float2* sx = reinterpret_cast<float2*>(s_T + 512);       // R * Q * (P+1)
+
+    const int b = blockIdx.y;  // realization * modes + mode
+    const SsfmState* st = a.state ? a.state + b / (a.modes > 1 ? a.modes : 1) : nullptr;
+    unsigned long long dhi = 0ull, dlo = 0ull;
+    float g = a.scale;
+    if (st) {
+        if (!*(volatile const int*)&st->row_active) return;
+        dhi = st->disp_hi;
+        dlo = st->disp_lo << 32;
+        g = st->lin_gain;
+    }
+    for (int i = threadIdx.x; i < N2; i += blockDim.x) s_tw[i] = a.tw[a.N1 + i];
+    if (st)
+        for (int i = threadIdx.x; i < 512; i += blockDim.x) s_T[i] = a.tw[2 * a.N1 + 2 * N2 + i];
+    const int rl = threadIdx.x / P, t = threadIdx.x % P;
+    row_work<N2>(a, st ? (int)ROW_SSFM : a.op, a.data + (size_t)b * a.N, blockIdx.x * R + rl, rl, t, s_tw, s_T, sx,
+                 g, dhi, dlo);
+}
+
+// ---------------------------------------------------------------- single CTA
+// For N = N1 N2 <= 2^14 one CTA of kBlockThreads runs a realization's whole
+// split-step loop with the field resident in shared memory: the column and
+// row work of the two-pass kernels (the same arithmetic, so the same
+// results), over all columns and then all rows of the field, with thread 0
+// advancing the step state between the phases.  HBM is read once and written
+// once per SSFM run instead of twice per step, and a run is one launch.
+constexpr int kBlockThreads = 256;
+
+template <int N1, int N2>
+struct BlockShape {
+    static constexpr int C = 16;
+    static constexpr int G = kBlockThreads / (C * ColFFT<N1>::P);  // column groups
+    static constexpr int RPI = kBlockThreads / PQ<N2>::P;          // rows per row phase step
+    static constexpr size_t XCH = (size_t)G * N1 * C > (size_t)RPI * PQ<N2>::Q * (PQ<N2>::P + 1)
+                                      ? (size_t)G * N1 * C
+                                      : (size_t)RPI * PQ<N2>::Q * (PQ<N2>::P + 1);
+    static constexpr size_t SMEM = sizeof(float4) * ((size_t)N1 + (size_t)ColFFT<N1>::Q * N2 + N2 + 512) +
+                                   sizeof(float2) * ((size_t)N1 * N2 + XCH);
+    static_assert(G >= 1 && N2 % (G * C) == 0 && N1 % RPI == 0, "single-CTA split");
+};
+
+template <int N1, int N2>
+__global__ void __launch_bounds__(kBlockThreads, 1) block_kernel(const PassArgs a, int cap) {
+    using S = BlockShape<N1, N2>;
+    constexpr int C = S::C, G = S::G, RPI = S::RPI;
+    constexpr int Pc = ColFFT<N1>::P, Qc = ColFFT<N1>::Q, Pr = PQ<N2>::P;
+    constexpr int a1 = ColFFT<N1>::PAIR ? Qc : Pc;
+    constexpr int N = N1 * N2;
+    extern __shared__ float4 smem4[];
+    float4* s_fc = smem4;                                 // column sub-FFT twiddles
+    float4* s_B = s_fc + N1;                              // six-step factors, [j][n2]
+    float4* s_tw = s_B + Qc * N2;                         // row sub-FFT twiddles
+    float4* s_T = s_tw + N2;                              // exp(2 pi i j/512)
+    float2* s_f = reinterpret_cast<float2*>(s_T + 512);   // the field, N samples
+    float2* s_x = s_f + N;                                // exchange buffers
+    __shared__ float red[64];
+
+    SsfmState* st = a.state + blockIdx.x;
+    const int log2N = a.log2N2 + ilog2c(N1);
+    for (int i = threadIdx.x; i < N1; i += kBlockThreads) s_fc[i] = a.tw[i];
+    for (int i = threadIdx.x; i < N2; i += kBlockThreads) s_tw[i] = a.tw[N1 + i];
+    for (int i = threadIdx.x; i < 512; i += kBlockThreads) s_T[i] = a.tw[2 * N1 + 2 * N2 + i];
+    for (int i = threadIdx.x; i < Qc * N2; i += kBlockThreads)
+        s_B[i] = sixstep_factor((i % N2) * a1 * (i / N2), log2N);
+    float4* g4 = reinterpret_cast<float4*>(a.data + (size_t)blockIdx.x * N);
+    float4* f4 = reinterpret_cast<float4*>(s_f);
+    for (int i = threadIdx.x; i < N / 2; i += kBlockThreads) f4[i] = g4[i];
+    __syncthreads();
+
+    const int grp = threadIdx.x / (C * Pc), gt = threadIdx.x % (C * Pc);
+    const int rl = threadIdx.x / Pr, t = threadIdx.x % Pr;
+    for (int it = 0; it < cap; ++it) {
+        const int op = *(volatile const int*)&st->action;
+        if (op == COL_IDLE) break;
+        float pk = 0.0f, sm = 0.0f;
+        for (int cb = 0; cb < N2 / (G * C); ++cb) {
+            const int n2_0 = (cb * G + grp) * C;
+            col_work<N1, C>(a, op, st, s_f, n2_0, s_fc, s_B + n2_0, N2, s_x + (size_t)grp * N1 * C, s_x, grp, 1, gt,
+                            pk, sm);
+            __syncthreads();
+        }
+        block_max_sum(pk, sm, red);
+        if (threadIdx.x == 0) ssfm_advance(*st, a.prm, op, pk, (double)sm);
+        __syncthreads();
+        if (*(volatile const int*)&st->row_active) {
+            const float g = *(volatile const float*)&st->lin_gain;
+            const unsigned long long dhi = *(volatile const unsigned long long*)&st->disp_hi;
+            const unsigned long long dlo = *(volatile const unsigned long long*)&st->disp_lo << 32;
+            for (int rb = 0; rb < N1 / RPI; ++rb) {
+                row_work<N2>(a, ROW_SSFM, s_f, rb * RPI + rl, rl, t, s_tw, s_T, s_x, g, dhi, dlo);
+                __syncthreads();
+            }
+        }
+    }
+    for (int i = threadIdx.x; i < N / 2; i += kBlockThreads) g4[i] = f4[i];
 }
 
 typedef void (*PassFn)(PassArgs);

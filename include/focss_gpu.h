@@ -207,14 +207,20 @@ FOCSS_API focss_status focss_span_loop(focss_ctx* ctx, int n_fields, focss_field
                                        const focss_amp* amp, int spans, double direction, int* steps_out);
 
 /* Split-step FFT autotuner (no reference counterpart).  The two-pass FFT of
- * length N = N1*N2 can use any split with N1, N2 in [2^4, 2^10]; this times
- * every admissible split on a scratch batch of `batch` realizations (a few
- * UNIFORM steps each, CUDA events) and keeps the fastest for this context's
- * split-step runs of length `samples`.  log2_n1 / ms_per_step (may be NULL)
- * receive the choice and its time per step for the whole batch. */
+ * length N = N1*N2 can use any split with N1, N2 in [2^4, 2^10]; for N in
+ * [2^12, 2^14] a single-CTA kernel (FOCSS_SPLIT_SINGLE_CTA: one CTA per
+ * realization runs the whole SSFM with the field in shared memory) is a
+ * further candidate.  This times every candidate on a scratch batch of
+ * `batch` realizations (a few UNIFORM steps each, CUDA events) and keeps the
+ * fastest for this context's split-step runs of length `samples`.
+ * log2_n1 / ms_per_step (may be NULL) receive the choice and its time per
+ * step for the whole batch. */
+#define FOCSS_SPLIT_SINGLE_CTA (-1)
 FOCSS_API focss_status focss_autotune(focss_ctx* ctx, int samples, int batch, int* log2_n1, double* ms_per_step);
 /* Pin the split used for split-step runs of length `samples` (log2_n1 = 0
- * restores the balanced default). */
+ * restores the balanced default; FOCSS_SPLIT_SINGLE_CTA selects the
+ * single-CTA kernel for single-mode fields of 2^12..2^14 samples, other
+ * fields of that length keep the balanced two-pass split). */
 FOCSS_API focss_status focss_set_fft_split(focss_ctx* ctx, int samples, int log2_n1);
 
 /* --------------------------------------------------- TX / resampling DSP */

@@ -133,7 +133,7 @@ def test_every_fft_split_matches_oracle(ctx, oracle_cpu):
         assert rel_l2(f.numpy()[0, 0], a) < 2e-6, l1
     fg.set_fft_split(n, 0, ctx=ctx)
     l1, ms = fg.autotune(n, 8, ctx=ctx)
-    assert 4 <= l1 <= 10 and ms > 0
+    assert (4 <= l1 <= 10 or l1 == fg.SPLIT_SINGLE_CTA) and ms > 0
     f = fg.Field(fg.Domain(1, n, dt, F0), data=x[None, None], ctx=ctx)
     fg.SSFM(fib, 10).run(f)
     assert rel_l2(f.numpy()[0, 0], a) < 2e-6

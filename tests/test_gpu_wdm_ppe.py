@@ -126,3 +126,22 @@ def test_wdm_dataset_ppe_pipeline(ctx):
     q_hd = dsp.q2_factor(tc, ppe.equalize(dsp.hd(rx), rx), cut)[0]
     print("Q cdc %.3f  ppe(rx) %.3f  ppe(hd) %.3f dB, |a| %.4f" % (q_cdc, q_rx, q_hd, abs(ppe.get_linear_weight())))
     assert q_rx > q_cdc + 0.2 and q_hd > q_cdc + 0.2
+
+
+def test_copy_modes(ctx):
+    """focss_field_copy_modes gathers channels' polarizations into dataset
+    rows (channel * 2 + polarization) and back, in every realization."""
+    rng = np.random.default_rng(4)
+    n, B = 1000, 3
+    chans = [_qam(rng, (B, 2, n)) for _ in range(3)]
+    six = fg.Field(fg.Domain(6, n, 1.0), batch=B, ctx=ctx)
+    for ch, a in enumerate(chans):
+        six.copy_modes(2 * ch, fg.Field(fg.Domain(2, n, 1.0), data=a, batch=B, ctx=ctx), 0, 2)
+    got = six.numpy()
+    np.testing.assert_array_equal(got, np.concatenate(chans, axis=1))
+    back = fg.Field(fg.Domain(2, n, 1.0), batch=B, ctx=ctx).copy_modes(0, six, 2, 2)
+    np.testing.assert_array_equal(back.numpy(), chans[1])
+    one = fg.Field(fg.Domain(1, n, 1.0), batch=B, ctx=ctx).copy_modes(0, six, 5, 1)
+    np.testing.assert_array_equal(one.numpy()[:, 0], chans[2][:, 1])
+    with pytest.raises(fg.FocssError):
+        six.copy_modes(5, back, 0, 2)  # rows 5..6 of a 6-row field
