@@ -687,6 +687,8 @@ def run_ncu_case(args):
     ldbp  learned-DBP forward + backward, 20 spans x 2 steps, 63/255 taps,
           8 x 2^16 samples;
     cnn   correction-CNN forward + backward, 8 x 2^15 symbols;
+    block single-CTA split-step kernel, 304 realizations of N = 2^14 (2 CTAs
+          per SM of work, 40 MB), UNIFORM 10 steps in one launch;
     fit   SINO normal equations (features, z-scores, FP64-accumulated Gram),
           R = 32 (577 features) on 2^17 symbols x 2 modes;
     wdmppe  WdmPPE (c, d) = (30, 3): equalizer on 16 x 6-row realizations of
@@ -736,6 +738,12 @@ def run_ncu_case(args):
         net.set_params(he_init(rng))
         net.forward(y)
         net.loss_grad(y, y)
+    elif kind == "block":
+        n, B = 1 << 14, 304
+        x = (rng.standard_normal((B, 1, n)) + 1j * rng.standard_normal((B, 1, n))) * 0.02
+        f = fg.Field(fg.Domain(1, n, DT, F0), data=x.astype(np.complex64), batch=B, ctx=ctx)
+        fg.set_fft_split(n, fg.SPLIT_SINGLE_CTA, ctx=ctx)
+        fg.SSFM(fib, 10).run(f)
     elif kind == "fit":
         from focss_gb300 import sino
         ns = 2 ** 17
@@ -764,7 +772,7 @@ def run_ncu_case(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ncu-case", nargs="?", const="ssfm", default=None,
-                    help="small fixed case for ncu captures: ssfm (default), ppe, ldbp, cnn, fit, wdmppe")
+                    help="small fixed case for ncu captures: ssfm (default), ppe, ldbp, cnn, block, fit, wdmppe")
     ap.add_argument("--ncu-batch", type=int, default=40)
     ap.add_argument("--split", type=int, default=0, help="ncu case: log2 N1 of the FFT split (0: balanced)")
     ap.add_argument("--gpus", type=int, default=1)
