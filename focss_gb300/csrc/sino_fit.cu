@@ -16,8 +16,9 @@
 // is the same pipeline on the centre channel of a 3-channel dual-polarization
 // matrix with the XPM triplets of the neighbours as further features.
 // The Gram product is a tiled complex kernel on the CUDA
-// cores (64 x 64 output tiles, 4 x 4 complex outputs per thread) reading the
-// FP32 features and accumulating in FP64.
+// cores (64 x 64 output tiles, 4 x 4 complex outputs per thread, the samples
+// split over the grid's z dimension) reading the FP32 features, summing runs
+// of 16 samples in FP32 and accumulating those sums in FP64.
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -35,6 +36,7 @@ inline int grid_for_(size_t n) {
     return (int)std::min<size_t>(g ? g : 1, (size_t)152 * 32);
 }
 constexpr int GK = 16;  // samples per shared-memory chunk
+constexpr int kFlush = 1;  // chunks summed in FP32 before an FP64 accumulation (16 samples; 64 measurably loses accuracy)
 
 struct Feature {
     int m, n, kind;  // kind: 0 = (0,0), 1 = m == n, 2 = m == -n, 3 = general, 4 = transmitted sample
@@ -185,8 +187,15 @@ __global__ void column_stats_kernel(float2* __restrict__ Z, size_t kp, size_t ns
         col[i] = make_float2((float)((col[i].x - mr) * sc), (float)((col[i].y - mi) * sc));
 }
 
-// G[a][b] = sum_i conj(Z[a][i]) Z[b][i] for the upper-triangle tiles (a <= b);
-// Z is zero-padded to multiples of GT features and GK samples.
+// G[a][b] += sum_i conj(Z[a][i]) Z[b][i] for the upper-triangle tiles (a <= b)
+// over this CTA's share of the samples (grid.z splits them; G starts at zero
+// and the shares meet in FP64 atomics).  Z is zero-padded to multiples of GT
+// features and GK samples.  Each run of kFlush x GK = 16 samples is summed in
+// FP32 (products of FP32 features) and added to FP64 accumulators: the normal
+// equations square the design's condition number, so sums over ~1e5 samples
+// must not run in FP32, but 16-term partial sums keep their error near that
+// of the FP32 features and the multiply-adds on the FP32 pipes (GB300's FP64
+// rate is a small fraction of its FP32 rate).
 __global__ void __launch_bounds__(256) gram_kernel(const float2* __restrict__ Z, size_t kp, int nfp,
                                                    double2* __restrict__ G) {
     const int bi = blockIdx.y, bj = blockIdx.x;
@@ -194,8 +203,6 @@ __global__ void __launch_bounds__(256) gram_kernel(const float2* __restrict__ Z,
     __shared__ float2 As[GK][GT + 1];
     __shared__ float2 Bs[GK][GT + 1];
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-    // FP64 accumulation: the normal equations square the design's condition
-    // number, so FP32 sums over ~1e5 samples are too coarse for the solve.
     double2 acc[4][4];
 #pragma unroll
     for (int r = 0; r < 4; ++r)
@@ -203,7 +210,14 @@ __global__ void __launch_bounds__(256) gram_kernel(const float2* __restrict__ Z,
         for (int c = 0; c < 4; ++c) acc[r][c] = make_double2(0.0, 0.0);
     const float2* Za = Z + (size_t)bi * GT * kp;
     const float2* Zb = Z + (size_t)bj * GT * kp;
-    for (size_t k0 = 0; k0 < kp; k0 += GK) {
+    const size_t chunks = kp / GK;
+    const size_t c0 = chunks * blockIdx.z / gridDim.z, c1 = chunks * (blockIdx.z + 1) / gridDim.z;
+    float2 part[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) part[r][c] = make_float2(0.f, 0.f);
+    for (size_t k0 = c0 * GK, ci = 0; k0 < c1 * GK; k0 += GK, ++ci) {
         // 64 features x 16 samples per operand: 4 loads per thread, samples fastest
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -215,24 +229,28 @@ __global__ void __launch_bounds__(256) gram_kernel(const float2* __restrict__ Z,
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < GK; ++kk) {
-            double2 av[4], bv[4];
+            float2 av[4], bv[4];
 #pragma unroll
-            for (int r = 0; r < 4; ++r) {
-                const float2 x = As[kk][ty * 4 + r];
-                av[r] = make_double2(x.x, x.y);
-            }
+            for (int r = 0; r < 4; ++r) av[r] = As[kk][ty * 4 + r];
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                const float2 x = Bs[kk][tx + 16 * c];  // consecutive lanes, consecutive words
-                bv[c] = make_double2(x.x, x.y);
-            }
+            for (int c = 0; c < 4; ++c) bv[c] = Bs[kk][tx + 16 * c];  // consecutive lanes, consecutive words
 #pragma unroll
             for (int r = 0; r < 4; ++r)
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
                     // conj(a) * b
-                    acc[r][c].x = fma(av[r].x, bv[c].x, fma(av[r].y, bv[c].y, acc[r][c].x));
-                    acc[r][c].y = fma(av[r].x, bv[c].y, fma(-av[r].y, bv[c].x, acc[r][c].y));
+                    part[r][c].x = fmaf(av[r].x, bv[c].x, fmaf(av[r].y, bv[c].y, part[r][c].x));
+                    part[r][c].y = fmaf(av[r].x, bv[c].y, fmaf(-av[r].y, bv[c].x, part[r][c].y));
+                }
+        }
+        if ((ci & (kFlush - 1)) == kFlush - 1 || k0 + GK >= c1 * GK) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    acc[r][c].x += (double)part[r][c].x;
+                    acc[r][c].y += (double)part[r][c].y;
+                    part[r][c] = make_float2(0.f, 0.f);
                 }
         }
         __syncthreads();
@@ -240,8 +258,11 @@ __global__ void __launch_bounds__(256) gram_kernel(const float2* __restrict__ Z,
 #pragma unroll
     for (int r = 0; r < 4; ++r)
 #pragma unroll
-        for (int c = 0; c < 4; ++c)
-            G[(size_t)(bi * GT + ty * 4 + r) * nfp + bj * GT + tx + 16 * c] = acc[r][c];
+        for (int c = 0; c < 4; ++c) {
+            double2* g = G + (size_t)(bi * GT + ty * 4 + r) * nfp + bj * GT + tx + 16 * c;
+            atomicAdd(&g->x, acc[r][c].x);
+            atomicAdd(&g->y, acc[r][c].y);
+        }
 }
 
 // SPM feature list in the order of sino.cpp:70-100 / wdm_sino.cpp:47-71.
@@ -287,7 +308,13 @@ cudaError_t fit_finish(FitBuffers& b, size_t kp, size_t ns, int nf, int nfp, dou
                        cudaStream_t s) {
     column_stats_kernel<<<nf + 1, 256, 0, s>>>(b.Z, kp, ns, nf, b.stat, b.stat + 2 * (size_t)nfp);
     count_launch();
-    dim3 g2(nfp / GT, nfp / GT);
+    // split the samples so that the upper-triangle tiles fill every SM twice
+    const int tiles = (nfp / GT) * (nfp / GT + 1) / 2;
+    const int chunks = (int)(kp / GK);
+    const int ks = std::max(1, std::min({(2 * 152 + tiles - 1) / tiles, 32, chunks}));
+    dim3 g2(nfp / GT, nfp / GT, ks);
+    cudaError_t e0 = cudaMemsetAsync(b.G, 0, sizeof(double2) * (size_t)nfp * nfp, s);
+    if (e0 != cudaSuccess) return e0;
     gram_kernel<<<g2, 256, 0, s>>>(b.Z, kp, nfp, b.G);
     count_launch();
     cudaError_t e = cudaGetLastError();

@@ -135,17 +135,17 @@ __device__ __noinline__ static void ssfm_advance(SsfmState& s, const SsfmParams&
 // ---------------------------------------------------------------- column pass
 // The work of one thread group (C columns x P threads, `gt` its thread index)
 // on columns [n2_0, n2_0 + C) of one mode of one realization; `data` points
-// at that mode's first sample (row stride N2; global memory in the two-pass
-// kernels, shared memory in the single-CTA kernel).  `sB` holds the six-step
+// at that mode's first sample and rows are `ld` samples apart (N2 in global
+// memory for the two-pass kernels; padded in the single-CTA kernel's shared
+// memory).  `sB` holds the six-step
 // factors W_N^{n2 a1 j} of these columns at sB[j * sB_stride + c].  Adds the
 // time-domain field's peak and sum of |A|^2 to pk / sm.
 template <int N1, int C>
 __device__ __forceinline__ void col_work(const PassArgs& a, int op, const SsfmState* st, float2* data, int n2_0,
                                          const float4* s_fc, const float4* sB, int sB_stride, float2* sx,
-                                         float2* s_x0, int mo, int modes, int gt, float& pk, float& sm) {
+                                         float2* s_x0, int mo, int modes, int gt, int ld, float& pk, float& sm) {
     constexpr int P = ColFFT<N1>::P, Q = ColFFT<N1>::Q;
     constexpr bool PAIR = ColFFT<N1>::PAIR;
-    const int N2 = a.N2;
     // Element j of a thread is time-domain row t + P j; in the spectral
     // layout it is row a0 + a1 j (a0 = t, a1 = P for the PQ form; lane-pair
     // form: a0 = (t>>1) + Q^2 (t&1), a1 = Q).  Six-step twiddle of column n2:
@@ -163,7 +163,7 @@ __device__ __forceinline__ void col_work(const PassArgs& a, int op, const SsfmSt
     float2* base = data + n2;
     float2 v[Q];
 #pragma unroll
-    for (int j = 0; j < Q; ++j) v[j] = base[(size_t)(op == COL_FWD ? t + P * j : a0 + a1 * j) * N2];
+    for (int j = 0; j < Q; ++j) v[j] = base[(size_t)(op == COL_FWD ? t + P * j : a0 + a1 * j) * ld];
     __syncthreads();
 
     const ColLayout<P, C> lay{c};
@@ -245,7 +245,7 @@ __device__ __forceinline__ void col_work(const PassArgs& a, int op, const SsfmSt
         }
     }
 #pragma unroll
-    for (int j = 0; j < Q; ++j) base[(size_t)(op == COL_INV ? t + P * j : a0 + a1 * j) * N2] = v[j];
+    for (int j = 0; j < Q; ++j) base[(size_t)(op == COL_INV ? t + P * j : a0 + a1 * j) * ld] = v[j];
 }
 
 // A CTA holds the same C columns of every mode of one realization (a.modes
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(2 * C * ColFFT<N1>::P, 1) col_kernel(const Pas
     const int modes = a.modes > 1 ? a.modes : 1;
     float pk = 0.0f, sm = 0.0f;
     col_work<N1, C>(a, op, st, a.data + ((size_t)b * modes + mo) * a.N, blockIdx.x * C, s_fc, s_B, C, sx, s_x0, mo,
-                    modes, threadIdx.x % (C * P), pk, sm);
+                    modes, threadIdx.x % (C * P), a.N2, pk, sm);
 
     if (st) {
         block_max_sum(pk, sm, red);
@@ -306,14 +306,15 @@ __global__ void __launch_bounds__(2 * C * ColFFT<N1>::P, 1) col_kernel(const Pas
 // ---------------------------------------------------------------- row pass
 // The work of the P threads of row k1 (`rl` the row's slot in the exchange
 // buffer, t the thread in the row) of one mode; `data` points at that mode's
-// first sample (global or shared memory).  ROW_SSFM applies exp(-alpha hl/2)/N
-// (FP32 gain g) times the dispersion phase from the 96-bit fraction dhi/dlo.
+// first sample (global or shared memory), rows `ld` samples apart.  ROW_SSFM
+// applies exp(-alpha hl/2)/N (FP32 gain g) times the dispersion phase from the
+// 96-bit fraction dhi/dlo.
 template <int N2>
 __device__ __forceinline__ void row_work(const PassArgs& a, int op, float2* data, int k1, int rl, int t,
                                          const float4* s_tw, const float4* s_T, float2* sx, float g,
-                                         unsigned long long dhi, unsigned long long dlo) {
+                                         unsigned long long dhi, unsigned long long dlo, int ld) {
     constexpr int P = PQ<N2>::P, Q = PQ<N2>::Q;
-    float2* base = data + (size_t)k1 * N2 + t;
+    float2* base = data + (size_t)k1 * ld + t;
     float2 v[Q];
 #pragma unroll
     for (int j = 0; j < Q; ++j) v[j] = base[P * j];
@@ -382,7 +383,7 @@ __global__ void __launch_bounds__(R* PQ<N2>::P, 2) row_kernel(const PassArgs a) 
         for (int i = threadIdx.x; i < 512; i += blockDim.x) s_T[i] = a.tw[2 * a.N1 + 2 * N2 + i];
     const int rl = threadIdx.x / P, t = threadIdx.x % P;
     row_work<N2>(a, st ? (int)ROW_SSFM : a.op, a.data + (size_t)b * a.N, blockIdx.x * R + rl, rl, t, s_tw, s_T, sx,
-                 g, dhi, dlo);
+                 g, dhi, dlo, N2);
 }
 
 // ---------------------------------------------------------------- single CTA
@@ -396,6 +397,10 @@ constexpr int kBlockThreads = 256;
 
 template <int N1, int N2>
 struct BlockShape {
+    // rows of the resident field are LD = N2 + 8 samples apart: the row
+    // phase's warps read 4 rows x 64 bytes, which then fall on both halves of
+    // the banks (two wavefronts instead of four)
+    static constexpr int LD = N2 + 8;
     static constexpr int C = 16;
     static constexpr int G = kBlockThreads / (C * ColFFT<N1>::P);  // column groups
     static constexpr int RPI = kBlockThreads / PQ<N2>::P;          // rows per row phase step
@@ -403,7 +408,7 @@ struct BlockShape {
                                       ? (size_t)G * N1 * C
                                       : (size_t)RPI * PQ<N2>::Q * (PQ<N2>::P + 1);
     static constexpr size_t SMEM = sizeof(float4) * ((size_t)N1 + (size_t)ColFFT<N1>::Q * N2 + N2 + 512) +
-                                   sizeof(float2) * ((size_t)N1 * N2 + XCH);
+                                   sizeof(float2) * ((size_t)N1 * LD + XCH);
     static_assert(G >= 1 && N2 % (G * C) == 0 && N1 % RPI == 0, "single-CTA split");
 };
 
@@ -413,14 +418,14 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_kernel(const PassArgs 
     constexpr int C = S::C, G = S::G, RPI = S::RPI;
     constexpr int Pc = ColFFT<N1>::P, Qc = ColFFT<N1>::Q, Pr = PQ<N2>::P;
     constexpr int a1 = ColFFT<N1>::PAIR ? Qc : Pc;
-    constexpr int N = N1 * N2;
+    constexpr int N = N1 * N2, LD = S::LD;
     extern __shared__ float4 smem4[];
     float4* s_fc = smem4;                                 // column sub-FFT twiddles
     float4* s_B = s_fc + N1;                              // six-step factors, [j][n2]
     float4* s_tw = s_B + Qc * N2;                         // row sub-FFT twiddles
     float4* s_T = s_tw + N2;                              // exp(2 pi i j/512)
-    float2* s_f = reinterpret_cast<float2*>(s_T + 512);   // the field, N samples
-    float2* s_x = s_f + N;                                // exchange buffers
+    float2* s_f = reinterpret_cast<float2*>(s_T + 512);   // the field, N1 rows of LD
+    float2* s_x = s_f + (size_t)N1 * LD;                  // exchange buffers
     __shared__ float red[64];
 
     SsfmState* st = a.state + blockIdx.x;
@@ -432,7 +437,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_kernel(const PassArgs 
         s_B[i] = sixstep_factor((i % N2) * a1 * (i / N2), log2N);
     float4* g4 = reinterpret_cast<float4*>(a.data + (size_t)blockIdx.x * N);
     float4* f4 = reinterpret_cast<float4*>(s_f);
-    for (int i = threadIdx.x; i < N / 2; i += kBlockThreads) f4[i] = g4[i];
+    for (int i = threadIdx.x; i < N / 2; i += kBlockThreads) f4[(i / (N2 / 2)) * (LD / 2) + i % (N2 / 2)] = g4[i];
     __syncthreads();
 
     const int grp = threadIdx.x / (C * Pc), gt = threadIdx.x % (C * Pc);
@@ -444,7 +449,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_kernel(const PassArgs 
         for (int cb = 0; cb < N2 / (G * C); ++cb) {
             const int n2_0 = (cb * G + grp) * C;
             col_work<N1, C>(a, op, st, s_f, n2_0, s_fc, s_B + n2_0, N2, s_x + (size_t)grp * N1 * C, s_x, grp, 1, gt,
-                            pk, sm);
+                            LD, pk, sm);
             __syncthreads();
         }
         block_max_sum(pk, sm, red);
@@ -455,12 +460,12 @@ __global__ void __launch_bounds__(kBlockThreads, 1) block_kernel(const PassArgs 
             const unsigned long long dhi = *(volatile const unsigned long long*)&st->disp_hi;
             const unsigned long long dlo = *(volatile const unsigned long long*)&st->disp_lo << 32;
             for (int rb = 0; rb < N1 / RPI; ++rb) {
-                row_work<N2>(a, ROW_SSFM, s_f, rb * RPI + rl, rl, t, s_tw, s_T, s_x, g, dhi, dlo);
+                row_work<N2>(a, ROW_SSFM, s_f, rb * RPI + rl, rl, t, s_tw, s_T, s_x, g, dhi, dlo, LD);
                 __syncthreads();
             }
         }
     }
-    for (int i = threadIdx.x; i < N / 2; i += kBlockThreads) g4[i] = f4[i];
+    for (int i = threadIdx.x; i < N / 2; i += kBlockThreads) g4[i] = f4[(i / (N2 / 2)) * (LD / 2) + i % (N2 / 2)];
 }
 
 typedef void (*PassFn)(PassArgs);
