@@ -8,7 +8,7 @@
 // FIR(x, h)[n] = sum_{t<T} h[t] x[(n + t - c) mod N], c = (T-1)/2 (circular).
 // It replaces the many-step split-step DBP of backward_propagation
 // (src/tasks/systems.cpp:73-91) with few learned steps per span; plain DBP is
-// initialisation, fallback and judge.
+// its initialisation, its fallback and the yardstick of its Q.
 //
 // Gradients use the Wirtinger convention g = dL/d(conj z) for complex values;
 // for real parameters dL/dxi is returned.  Loss: L = mean_k |symbols_k - t_k|^2.
