@@ -105,6 +105,8 @@ SIGNATURES = {
     "focss_sino_equalize": (I, [P, P, P, I, I, P, P, P, D, D, P]),
     "focss_sino_num_features": (I, [I, I]),
     "focss_sino_gram": (I, [P, P, P, I, I, D, D, P, P, P]),
+    "focss_sino_residual": (I, [P, P, P, I, I, D, D, P, P]),
+    "focss_wdm_ppe_residual": (I, [P, P, P, I, I, P, P]),
     "focss_wdm_ppe_num_features": (I, [I, I]),
     "focss_wdm_ppe_gram": (I, [P, P, P, I, I, P, P, P]),
     "focss_wdm_ppe_apply": (I, [P, P, P, P, P, I, P, I, P, D, D, P]),

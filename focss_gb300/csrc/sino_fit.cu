@@ -265,6 +265,44 @@ __global__ void __launch_bounds__(256) gram_kernel(const float2* __restrict__ Z,
         }
 }
 
+// Residual of the normal equations for iterative refinement, in FP64 on the
+// z-scored design: v = y - Z x (one thread per sample), then r = Z^H v (one
+// CTA per feature).  Z and y are the FP32 columns the Gram kernel reads, so
+// a refined solution solves the normal equations of exactly that design to
+// FP64 accuracy however the Gram matrix was rounded.
+__global__ void design_apply_kernel(const float2* __restrict__ Z, size_t kp, size_t ns, int nf,
+                                    const double2* __restrict__ x, double2* __restrict__ v) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ns; i += (size_t)gridDim.x * blockDim.x) {
+        const float2 y = Z[(size_t)nf * kp + i];
+        double re = y.x, im = y.y;
+        for (int f = 0; f < nf; ++f) {
+            const float2 z = Z[(size_t)f * kp + i];
+            const double2 xf = __ldg(x + f);
+            re = fma(-(double)z.x, xf.x, fma((double)z.y, xf.y, re));
+            im = fma(-(double)z.x, xf.y, fma(-(double)z.y, xf.x, im));
+        }
+        v[i] = make_double2(re, im);
+    }
+}
+
+__global__ void design_adjoint_kernel(const float2* __restrict__ Z, size_t kp, size_t ns,
+                                      const double2* __restrict__ v, double2* __restrict__ r) {
+    __shared__ double red[32];
+    const int f = blockIdx.x;
+    const float2* col = Z + (size_t)f * kp;
+    double re = 0, im = 0;
+    for (size_t i = threadIdx.x; i < ns; i += blockDim.x) {
+        const float2 z = col[i];
+        const double2 vi = v[i];
+        re = fma((double)z.x, vi.x, fma((double)z.y, vi.y, re));
+        im = fma((double)z.x, vi.y, fma(-(double)z.y, vi.x, im));
+    }
+    re = block_sum_d(re, red);
+    __syncthreads();
+    im = block_sum_d(im, red);
+    if (threadIdx.x == 0) r[f] = make_double2(re, im);
+}
+
 // SPM feature list in the order of sino.cpp:70-100 / wdm_sino.cpp:47-71.
 void spm_features(int R, std::vector<Feature>& fs) {
     const int mb = R / 2;
@@ -304,10 +342,36 @@ cudaError_t fit_alloc(FitBuffers& b, const std::vector<Feature>& fs, size_t kp, 
 // z-score the feature columns, centre the responses, form the Gram matrix and
 // copy gram ((nf+1)^2 complex128, upper triangle), mean (nf+1 complex128) and
 // sd (nf doubles) to the host.
-cudaError_t fit_finish(FitBuffers& b, size_t kp, size_t ns, int nf, int nfp, double* gram, double* mean, double* sd,
-                       cudaStream_t s) {
+// z-scores the feature columns and centres the responses in place.
+void fit_stats(FitBuffers& b, size_t kp, size_t ns, int nf, int nfp, cudaStream_t s) {
     column_stats_kernel<<<nf + 1, 256, 0, s>>>(b.Z, kp, ns, nf, b.stat, b.stat + 2 * (size_t)nfp);
     count_launch();
+}
+
+// r = Z^H (y - Z x) for the prepared design (x, r: nf complex128 on the host).
+cudaError_t fit_residual(FitBuffers& b, size_t kp, size_t ns, int nf, const double* x, double* r, cudaStream_t s) {
+    double2 *dx = nullptr, *dv = nullptr, *dr = nullptr;
+    cudaError_t e = cudaMalloc(&dx, sizeof(double2) * nf);
+    if (e == cudaSuccess) e = cudaMalloc(&dv, sizeof(double2) * ns);
+    if (e == cudaSuccess) e = cudaMalloc(&dr, sizeof(double2) * nf);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x, sizeof(double2) * nf, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        design_apply_kernel<<<grid_for_(ns), 256, 0, s>>>(b.Z, kp, ns, nf, dx, dv);
+        count_launch();
+        design_adjoint_kernel<<<nf, 256, 0, s>>>(b.Z, kp, ns, dv, dr);
+        count_launch();
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r, dr, sizeof(double2) * nf, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(dx);
+    cudaFree(dv);
+    cudaFree(dr);
+    return e;
+}
+
+cudaError_t fit_finish(FitBuffers& b, size_t kp, size_t ns, int nf, int nfp, double* gram, double* mean, double* sd,
+                       cudaStream_t s) {
     // split the samples so that the upper-triangle tiles fill every SM twice
     const int tiles = (nfp / GT) * (nfp / GT + 1) / 2;
     const int chunks = (int)(kp / GK);
@@ -329,6 +393,73 @@ cudaError_t fit_finish(FitBuffers& b, size_t kp, size_t ns, int nf, int nfp, dou
     return e;
 }
 
+// The z-scored SINO design (sino.cpp:42-118) in b; returns the sizes.
+focss_status sino_design(Ctx* c, const Field* tx, const Field* rx, int R, int type, double lw_re, double lw_im,
+                         FitBuffers& b, int& nf, size_t& ns, size_t& kp, int& nfp) {
+    if (type < 0 || type > 2 || R < 0) return FOCSS_ERR_INVALID_ARG;
+    if (tx->modes != rx->modes || tx->samples != rx->samples || tx->batch != 1 || rx->batch != 1)
+        return set_error(c, FOCSS_ERR_INVALID_ARG, "sino fit: tx and rx must be single realizations of one domain");
+    const int N = tx->samples, modes = tx->modes;
+    if (N <= 2 * R + 1) return set_error(c, FOCSS_ERR_INVALID_ARG, "sino fit: field shorter than the radius");
+    std::vector<Feature> fs;
+    spm_features(R, fs);
+    if (type == 0) fs.push_back({0, 0, 4});
+    nf = (int)fs.size();
+    ns = (size_t)modes * (N - 2 * R);
+    kp = (ns + GK - 1) / GK * GK;
+    nfp = (nf + 1 + GT - 1) / GT * GT;  // features + responses, padded
+    cudaStream_t s = c->stream;
+    cudaError_t e = fit_alloc(b, fs, kp, nfp, s);
+    if (e == cudaSuccess) {
+        dim3 grid((unsigned)std::min<size_t>((ns + 255) / 256, 1024), nf);
+        features_kernel<<<grid, 256, 0, s>>>(tx->d, modes, N, R, b.fs, nf, b.Z, kp);
+        count_launch();
+        responses_kernel<<<grid_for_(ns), 256, 0, s>>>(tx->d, rx->d, modes, N, R,
+                                                        make_float2((float)lw_re, (float)lw_im), type == 1,
+                                                        b.Z + (size_t)nf * kp);
+        count_launch();
+        fit_stats(b, kp, ns, nf, nfp, s);
+        e = cudaGetLastError();
+    }
+    return cuda_check(c, e, "sino fit design");
+}
+
+// The z-scored WdmPPE design (wdm_sino.cpp:28-93) in b.
+focss_status wdm_design(Ctx* c, const Field* tx, const Field* rx, int c_radius, int d_radius, FitBuffers& b,
+                        int& nf, size_t& ns, size_t& kp, int& nfp) {
+    if (c_radius < -1 || d_radius < -1) return FOCSS_ERR_INVALID_ARG;
+    if (tx->modes != 6 || (rx->modes != 6 && rx->modes != 2) || tx->samples != rx->samples || tx->batch != 1 ||
+        rx->batch != 1)
+        return set_error(c, FOCSS_ERR_INVALID_ARG,
+                         "wdm_ppe fit: tx must be one 6-row realization (3 channels x 2 polarizations), rx 6 or 2 rows");
+    const int N = tx->samples, R = std::max(c_radius, d_radius);
+    if (R < 0 || N <= 2 * R + 1) return set_error(c, FOCSS_ERR_INVALID_ARG, "wdm_ppe fit: radius vs field length");
+    // feature order of wdm_sino.cpp:43-80
+    std::vector<Feature> fs;
+    if (c_radius >= 0) spm_features(c_radius, fs);
+    for (int m = -d_radius; m <= d_radius; ++m) {
+        const int nb = d_radius - std::abs(m);
+        for (int n = -nb; n <= nb; ++n) fs.push_back({m, n, 5});
+    }
+    fs.push_back({0, 0, 4});
+    nf = (int)fs.size();
+    ns = 2 * (size_t)(N - 2 * R);
+    kp = (ns + GK - 1) / GK * GK;
+    nfp = (nf + 1 + GT - 1) / GT * GT;
+    cudaStream_t s = c->stream;
+    cudaError_t e = fit_alloc(b, fs, kp, nfp, s);
+    if (e == cudaSuccess) {
+        dim3 grid((unsigned)std::min<size_t>((ns + 255) / 256, 1024), nf);
+        wdm_features_kernel<<<grid, 256, 0, s>>>(tx->d, N, R, b.fs, nf, b.Z, kp);
+        count_launch();
+        wdm_responses_kernel<<<grid_for_(ns), 256, 0, s>>>(rx->d, rx->modes == 6 ? 2 : 0, N, R, b.Z + (size_t)nf * kp);
+        count_launch();
+        fit_stats(b, kp, ns, nf, nfp, s);
+        e = cudaGetLastError();
+    }
+    return cuda_check(c, e, "wdm_ppe fit design");
+}
+
 }  // namespace
 }  // namespace fg
 
@@ -342,34 +473,25 @@ FOCSS_API int focss_sino_num_features(int radius, int type) {
 FOCSS_API focss_status focss_sino_gram(focss_ctx* c, const focss_field* tx, const focss_field* rx, int radius,
                                        int type, double lw_re, double lw_im, double* gram, double* mean, double* sd) {
     using namespace fg;
-    if (!c || !tx || !rx || !gram || !mean || !sd || radius < 0 || type < 0 || type > 2)
-        return FOCSS_ERR_INVALID_ARG;
-    if (tx->modes != rx->modes || tx->samples != rx->samples || tx->batch != 1 || rx->batch != 1)
-        return set_error(c, FOCSS_ERR_INVALID_ARG, "sino_gram: tx and rx must be single realizations of one domain");
-    const int N = tx->samples, modes = tx->modes, R = radius;
-    if (N <= 2 * R + 1) return set_error(c, FOCSS_ERR_INVALID_ARG, "sino_gram: field shorter than the radius");
-    std::vector<Feature> fs;
-    spm_features(R, fs);
-    if (type == 0) fs.push_back({0, 0, 4});
-    const int nf = (int)fs.size();
-    if (nf != focss_sino_num_features(R, type)) return set_error(c, FOCSS_ERR_INVALID_ARG, "sino_gram: feature count");
-    const size_t ns = (size_t)modes * (N - 2 * R);
-    const size_t kp = (ns + GK - 1) / GK * GK;
-    const int nfp = (nf + 1 + GT - 1) / GT * GT;  // features + responses, padded
-    cudaStream_t s = c->stream;
+    if (!c || !tx || !rx || !gram || !mean || !sd) return FOCSS_ERR_INVALID_ARG;
     FitBuffers b;
-    cudaError_t e = fit_alloc(b, fs, kp, nfp, s);
-    if (e == cudaSuccess) {
-        dim3 grid((unsigned)std::min<size_t>((ns + 255) / 256, 1024), nf);
-        features_kernel<<<grid, 256, 0, s>>>(tx->d, modes, N, R, b.fs, nf, b.Z, kp);
-        count_launch();
-        responses_kernel<<<grid_for_(ns), 256, 0, s>>>(tx->d, rx->d, modes, N, R,
-                                                        make_float2((float)lw_re, (float)lw_im), type == 1,
-                                                        b.Z + (size_t)nf * kp);
-        count_launch();
-        e = fit_finish(b, kp, ns, nf, nfp, gram, mean, sd, s);
-    }
-    return cuda_check(c, e, "sino_gram");
+    int nf, nfp;
+    size_t ns, kp;
+    focss_status st = sino_design(c, tx, rx, radius, type, lw_re, lw_im, b, nf, ns, kp, nfp);
+    if (st != FOCSS_OK) return st;
+    return cuda_check(c, fit_finish(b, kp, ns, nf, nfp, gram, mean, sd, c->stream), "sino_gram");
+}
+
+FOCSS_API focss_status focss_sino_residual(focss_ctx* c, const focss_field* tx, const focss_field* rx, int radius,
+                                           int type, double lw_re, double lw_im, const double* x, double* r) {
+    using namespace fg;
+    if (!c || !tx || !rx || !x || !r) return FOCSS_ERR_INVALID_ARG;
+    FitBuffers b;
+    int nf, nfp;
+    size_t ns, kp;
+    focss_status st = sino_design(c, tx, rx, radius, type, lw_re, lw_im, b, nf, ns, kp, nfp);
+    if (st != FOCSS_OK) return st;
+    return cuda_check(c, fit_residual(b, kp, ns, nf, x, r, c->stream), "sino_residual");
 }
 
 FOCSS_API int focss_wdm_ppe_num_features(int c_radius, int d_radius) {
@@ -382,39 +504,25 @@ FOCSS_API int focss_wdm_ppe_num_features(int c_radius, int d_radius) {
 FOCSS_API focss_status focss_wdm_ppe_gram(focss_ctx* c, const focss_field* tx, const focss_field* rx, int c_radius,
                                           int d_radius, double* gram, double* mean, double* sd) {
     using namespace fg;
-    if (!c || !tx || !rx || !gram || !mean || !sd || c_radius < -1 || d_radius < -1) return FOCSS_ERR_INVALID_ARG;
-    if (tx->modes != 6 || (rx->modes != 6 && rx->modes != 2) || tx->samples != rx->samples || tx->batch != 1 ||
-        rx->batch != 1)
-        return set_error(c, FOCSS_ERR_INVALID_ARG,
-                         "wdm_ppe_gram: tx must be one 6-row realization (3 channels x 2 polarizations), rx 6 or 2 rows");
-    const int N = tx->samples, R = std::max(c_radius, d_radius);
-    if (R < 0 || N <= 2 * R + 1) return set_error(c, FOCSS_ERR_INVALID_ARG, "wdm_ppe_gram: radius vs field length");
-    // feature order of wdm_sino.cpp:43-80
-    std::vector<Feature> fs;
-    if (c_radius >= 0) spm_features(c_radius, fs);
-    for (int m = -d_radius; m <= d_radius; ++m) {
-        const int nb = d_radius - std::abs(m);
-        for (int n = -nb; n <= nb; ++n) fs.push_back({m, n, 5});
-    }
-    fs.push_back({0, 0, 4});
-    const int nf = (int)fs.size();
-    if (nf != focss_wdm_ppe_num_features(c_radius, d_radius))
-        return set_error(c, FOCSS_ERR_INVALID_ARG, "wdm_ppe_gram: feature count");
-    const size_t ns = 2 * (size_t)(N - 2 * R);
-    const size_t kp = (ns + GK - 1) / GK * GK;
-    const int nfp = (nf + 1 + GT - 1) / GT * GT;
-    cudaStream_t s = c->stream;
+    if (!c || !tx || !rx || !gram || !mean || !sd) return FOCSS_ERR_INVALID_ARG;
     FitBuffers b;
-    cudaError_t e = fit_alloc(b, fs, kp, nfp, s);
-    if (e == cudaSuccess) {
-        dim3 grid((unsigned)std::min<size_t>((ns + 255) / 256, 1024), nf);
-        wdm_features_kernel<<<grid, 256, 0, s>>>(tx->d, N, R, b.fs, nf, b.Z, kp);
-        count_launch();
-        wdm_responses_kernel<<<grid_for_(ns), 256, 0, s>>>(rx->d, rx->modes == 6 ? 2 : 0, N, R, b.Z + (size_t)nf * kp);
-        count_launch();
-        e = fit_finish(b, kp, ns, nf, nfp, gram, mean, sd, s);
-    }
-    return cuda_check(c, e, "wdm_ppe_gram");
+    int nf, nfp;
+    size_t ns, kp;
+    focss_status st = wdm_design(c, tx, rx, c_radius, d_radius, b, nf, ns, kp, nfp);
+    if (st != FOCSS_OK) return st;
+    return cuda_check(c, fit_finish(b, kp, ns, nf, nfp, gram, mean, sd, c->stream), "wdm_ppe_gram");
+}
+
+FOCSS_API focss_status focss_wdm_ppe_residual(focss_ctx* c, const focss_field* tx, const focss_field* rx,
+                                              int c_radius, int d_radius, const double* x, double* r) {
+    using namespace fg;
+    if (!c || !tx || !rx || !x || !r) return FOCSS_ERR_INVALID_ARG;
+    FitBuffers b;
+    int nf, nfp;
+    size_t ns, kp;
+    focss_status st = wdm_design(c, tx, rx, c_radius, d_radius, b, nf, ns, kp, nfp);
+    if (st != FOCSS_OK) return st;
+    return cuda_check(c, fit_residual(b, kp, ns, nf, x, r, c->stream), "wdm_ppe_residual");
 }
 
 }  // extern "C"

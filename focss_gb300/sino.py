@@ -25,6 +25,28 @@ class SinoType(IntEnum):
     HOMOGENEOUS = 2
 
 
+def solve_normal_equations(gram, nf, residual=None, refinements=2):
+    """x = G^-1 g for the (nf+1)^2 Gram matrix [Z y]^H [Z y] returned by the
+    GPU (upper triangle valid): Cholesky in FP64 on the host, then
+    `refinements` steps of iterative refinement x += G^-1 residual(x) with
+    residual(x) = Z^H (y - Z x) evaluated in FP64 on the GPU, which removes
+    the effect of the Gram matrix's FP32 chunk sums on ill-conditioned fits."""
+    Gu = np.triu(gram)
+    G = Gu + np.conj(np.triu(Gu, 1)).T              # Hermitian from the upper triangle
+    A, g = G[:nf, :nf], G[:nf, nf]
+    try:
+        from scipy.linalg import cho_factor, cho_solve
+        fac = cho_factor(A)
+        solve = lambda b: cho_solve(fac, b)  # noqa: E731
+    except Exception:  # not positive definite to working precision, or no scipy
+        solve = lambda b: np.linalg.solve(A, b)  # noqa: E731
+    x = solve(g)
+    if residual is not None:
+        for _ in range(refinements):
+            x = x + solve(residual(x))
+    return x
+
+
 def diamond_terms(weights, radius, prune=0.0):
     """(m, n, C) for |m| + |n| <= radius from a (2R+1)^2 matrix W[m+R, n+R]
     (the summation domain of SINO::cubic, sino.cpp:206-214); optionally drop
@@ -110,6 +132,15 @@ class SINO:
         return self
 
     # ---- sino.cpp:42-159 with the normal equations formed on the GPU
+    def _residual(self, transmitted, received, x):
+        lw = complex(self.linear_weight)
+        x = np.ascontiguousarray(x, np.complex128)
+        r = np.zeros_like(x)
+        check(lib().focss_sino_residual(transmitted.ctx.h, transmitted.h, received.h, self.radius, int(self.type),
+                                        lw.real, lw.imag, x.ctypes.data_as(C.c_void_p),
+                                        r.ctypes.data_as(C.c_void_p)), transmitted.ctx.h)
+        return r
+
     def _train_gpu(self, transmitted, received):
         from .api import Domain
         if not isinstance(transmitted, Field):
@@ -126,9 +157,7 @@ class SINO:
         check(lib().focss_sino_gram(transmitted.ctx.h, transmitted.h, received.h, R, int(self.type), lw.real, lw.imag,
                                     gram.ctypes.data_as(C.c_void_p), mean.ctypes.data_as(C.c_void_p),
                                     sd.ctypes.data_as(C.c_void_p)), transmitted.ctx.h)
-        Gu = np.triu(gram)
-        G = Gu + np.conj(np.triu(Gu, 1)).T          # Hermitian from the upper triangle
-        raw = np.linalg.solve(G[:nf, :nf], G[:nf, nf])
+        raw = solve_normal_equations(gram, nf, lambda x: self._residual(transmitted, received, x))
         raw = raw / sd
         x_mean, y_mean = mean[:nf], mean[nf]
         return raw, x_mean, y_mean

@@ -18,6 +18,7 @@ import numpy as np
 
 from ._lib import check, lib
 from .api import Domain, Field
+from .sino import solve_normal_equations
 
 
 def _vp(a):
@@ -66,6 +67,7 @@ class WdmPPE:
         return self
 
     # ---- wdm_sino.cpp:28-142: the normal equations on the GPU, FP64 solve
+    # with iterative refinement against the FP64 residual of the design
     def train(self, tx, rx):
         t = _field(tx)
         r = _field(rx, ctx=t.ctx)
@@ -75,9 +77,14 @@ class WdmPPE:
         mean = np.zeros(nf + 1, np.complex128)
         sd = np.zeros(nf, np.float64)
         check(lib().focss_wdm_ppe_gram(t.ctx.h, t.h, r.h, c, d, _vp(gram), _vp(mean), _vp(sd)), t.ctx.h)
-        Gu = np.triu(gram)
-        G = Gu + np.conj(np.triu(Gu, 1)).T
-        raw = np.linalg.solve(G[:nf, :nf], G[:nf, nf]) / sd
+
+        def residual(x):
+            x = np.ascontiguousarray(x, np.complex128)
+            out = np.zeros_like(x)
+            check(lib().focss_wdm_ppe_residual(t.ctx.h, t.h, r.h, c, d, _vp(x), _vp(out)), t.ctx.h)
+            return out
+
+        raw = solve_normal_equations(gram, nf, residual) / sd
         self.intercept = complex(mean[nf] - np.sum(raw * mean[:nf]))
         return self.install(raw)
 

@@ -349,6 +349,14 @@ FOCSS_API focss_status focss_sino_equalize(focss_ctx* ctx, const focss_field* rx
 FOCSS_API int focss_sino_num_features(int radius, int type);
 FOCSS_API focss_status focss_sino_gram(focss_ctx* ctx, const focss_field* tx, const focss_field* rx, int radius,
                                        int type, double lw_re, double lw_im, double* gram, double* mean, double* sd);
+/* Iterative refinement of that fit: r = Z^H (y - Z x) in FP64 for the same
+ * z-scored design Z and centred responses y that focss_sino_gram forms
+ * (rebuilt deterministically), x and r nf complex128 in the z-scored basis.
+ * Solving G d = r with the Gram matrix and taking x + d converges to the
+ * FP64 normal-equations solution of the design even where the Gram matrix's
+ * FP32 chunk sums are too coarse for an ill-conditioned fit. */
+FOCSS_API focss_status focss_sino_residual(focss_ctx* ctx, const focss_field* tx, const focss_field* rx, int radius,
+                                           int type, double lw_re, double lw_im, const double* x, double* r);
 
 /* WdmPPE (src/focss/equalizer/wdm_sino.h:8-71, wdm_sino.cpp): the
  * dual-polarization WDM perturbation equalizer.  Its fields are 6-row
@@ -375,6 +383,9 @@ FOCSS_API focss_status focss_sino_gram(focss_ctx* ctx, const focss_field* tx, co
 FOCSS_API int focss_wdm_ppe_num_features(int c_radius, int d_radius);
 FOCSS_API focss_status focss_wdm_ppe_gram(focss_ctx* ctx, const focss_field* tx, const focss_field* rx,
                                           int c_radius, int d_radius, double* gram, double* mean, double* sd);
+/* The same refinement residual for the WdmPPE design. */
+FOCSS_API focss_status focss_wdm_ppe_residual(focss_ctx* ctx, const focss_field* tx, const focss_field* rx,
+                                              int c_radius, int d_radius, const double* x, double* r);
 FOCSS_API focss_status focss_wdm_ppe_apply(focss_ctx* ctx, const focss_field* spm_in, const focss_field* xpm_in,
                                            const focss_field* rx, const focss_field* lin_in, int c_radius,
                                            const double* C, int d_radius, const double* D, double lw_re,

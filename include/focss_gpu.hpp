@@ -45,6 +45,7 @@
 #include <cstdint>
 #include <cstdlib>
 #include <fstream>
+#include <functional>
 #include <istream>
 #include <ostream>
 #include <random>
@@ -770,15 +771,20 @@ namespace detail {
 /* x = G^-1 g for the fit's normal equations: gram is the (nf+1)^2 row-major
  * complex matrix [Z y]^H [Z y] (upper triangle valid), G its leading nf x nf
  * block, g its last column.  Right-looking Cholesky G = U^H U in FP64 on
- * the upper triangle (contiguous inner loops), then U^H w = g and U x = w. */
-inline ComplexVector solve_normal_equations(const ComplexVector& gram, int nf) {
+ * the upper triangle (contiguous inner loops), then U^H w = g and U x = w;
+ * with a residual function r(x) = Z^H (y - Z x) (evaluated in FP64 on the
+ * GPU), `refinements` steps of iterative refinement x += G^-1 r(x). */
+inline ComplexVector solve_normal_equations(const ComplexVector& gram, int nf,
+                                            const std::function<ComplexVector(const ComplexVector&)>& residual = {},
+                                            int refinements = 2) {
     const size_t n = (size_t)nf, w = n + 1;
     ComplexVector U(n * n);
     for (size_t i = 0; i < n; ++i)
         for (size_t j = i; j < n; ++j) U[i * n + j] = gram[i * w + j];
     for (size_t k = 0; k < n; ++k) {
         const double d = U[k * n + k].real();
-        if (!(d > 0)) throw gpu_error(FOCSS_ERR_INVALID_ARG, "focss: normal equations are not positive definite (rank-deficient design)");
+        if (!(d > 0))
+            throw gpu_error(FOCSS_ERR_INVALID_ARG, "focss: normal equations are not positive definite (rank-deficient design)");
         const double r = std::sqrt(d);
         U[k * n + k] = r;
         for (size_t j = k + 1; j < n; ++j) U[k * n + j] /= r;
@@ -789,17 +795,26 @@ inline ComplexVector solve_normal_equations(const ComplexVector& gram, int nf) {
             for (size_t j = i; j < n; ++j) row[j] -= a * top[j];
         }
     }
-    ComplexVector x(n);
-    for (size_t i = 0; i < n; ++i) x[i] = gram[i * w + n];
-    for (size_t p = 0; p < n; ++p) {  // U^H w = g
-        x[p] /= U[p * n + p].real();
-        for (size_t i = p + 1; i < n; ++i) x[i] -= std::conj(U[p * n + i]) * x[p];
-    }
-    for (size_t i = n; i-- > 0;) {  // U x = w
-        complex_t acc = x[i];
-        for (size_t j = i + 1; j < n; ++j) acc -= U[i * n + j] * x[j];
-        x[i] = acc / U[i * n + i].real();
-    }
+    auto solve = [&](ComplexVector x) {
+        for (size_t p = 0; p < n; ++p) {  // U^H w = b
+            x[p] /= U[p * n + p].real();
+            for (size_t i = p + 1; i < n; ++i) x[i] -= std::conj(U[p * n + i]) * x[p];
+        }
+        for (size_t i = n; i-- > 0;) {  // U x = w
+            complex_t acc = x[i];
+            for (size_t j = i + 1; j < n; ++j) acc -= U[i * n + j] * x[j];
+            x[i] = acc / U[i * n + i].real();
+        }
+        return x;
+    };
+    ComplexVector g(n);
+    for (size_t i = 0; i < n; ++i) g[i] = gram[i * w + n];
+    ComplexVector x = solve(g);
+    if (residual)
+        for (int it = 0; it < refinements; ++it) {
+            const ComplexVector d = solve(residual(x));
+            for (size_t i = 0; i < n; ++i) x[i] += d[i];
+        }
     return x;
 }
 
@@ -861,7 +876,14 @@ class SINO {
                                       linear_weight_.real(), linear_weight_.imag(), detail::cplx(gram),
                                       detail::cplx(mean), sd.data()),
                       gpu_context());
-        ComplexVector raw = detail::solve_normal_equations(gram, nf);
+        ComplexVector raw = detail::solve_normal_equations(gram, nf, [&](const ComplexVector& x) {
+            ComplexVector r(x.size());
+            detail::check(focss_sino_residual(gpu_context(), transmitted.handle(), received.handle(), radius_,
+                                              (int)type_, linear_weight_.real(), linear_weight_.imag(),
+                                              detail::cplx(x), detail::cplx(r)),
+                          gpu_context());
+            return r;
+        });
         complex_t dot = 0;
         for (int i = 0; i < nf; ++i) {
             raw[(size_t)i] /= sd[(size_t)i];
@@ -977,7 +999,13 @@ class WdmPPE {
         detail::check(focss_wdm_ppe_gram(gpu_context(), tx.handle(), rx.handle(), c_, d_, detail::cplx(gram),
                                          detail::cplx(mean), sd.data()),
                       gpu_context());
-        ComplexVector raw = detail::solve_normal_equations(gram, nf);
+        ComplexVector raw = detail::solve_normal_equations(gram, nf, [&](const ComplexVector& x) {
+            ComplexVector r(x.size());
+            detail::check(focss_wdm_ppe_residual(gpu_context(), tx.handle(), rx.handle(), c_, d_, detail::cplx(x),
+                                                 detail::cplx(r)),
+                          gpu_context());
+            return r;
+        });
         complex_t dot = 0;
         for (int i = 0; i < nf; ++i) {
             raw[(size_t)i] /= sd[(size_t)i];
