@@ -350,8 +350,12 @@ FOCSS_API focss_status focss_span_loop(focss_ctx* c, int n_fields, focss_field* 
     for (int i = 0; i < n_fields; ++i) {
         if (ctr[fg::kCtr * i + 2])
             return fg::set_error(c, FOCSS_ERR_NOT_CONVERGED, "span_loop: step cap reached (field " + std::to_string(i) + ")");
-        if (ctr[fg::kCtr * i + 3])
+        if (ctr[fg::kCtr * i + 3]) {
+            // a single-CTA run stops a realization at the step cap, unfinished
+            if (fg::ssfm_single_cta(c, fs[i]))
+                return fg::set_error(c, FOCSS_ERR_NOT_CONVERGED, "span_loop: step cap reached (field " + std::to_string(i) + ")");
             return fg::set_error(c, FOCSS_ERR_TIMEOUT, "span_loop: a realization did not finish (field " + std::to_string(i) + ")");
+        }
     }
     if (steps_out) std::copy(steps.begin(), steps.end(), steps_out);
     return FOCSS_OK;

@@ -250,7 +250,9 @@ focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ss
     if (ssfm_single_cta(ctx, f)) {
         st = cuda_check(ctx, launch_block(*p, a, f->batch, (int)std::min<long long>(cap, 1 << 30), s), "ssfm block");
         if (st != FOCSS_OK) return st;
-        return ssfm_finish(ctx, f, o, steps_out);
+        st = ssfm_finish(ctx, f, o, steps_out);
+        // the kernel stops a realization at the cap, leaving it unfinished
+        return st == FOCSS_ERR_TIMEOUT ? set_error(ctx, FOCSS_ERR_NOT_CONVERGED, "ssfm_run: step cap reached") : st;
     }
     const int chunk = 16;
     long long launched = 0;
