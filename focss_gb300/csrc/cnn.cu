@@ -4,8 +4,10 @@
 //     relu(conv1(x0))))))), x0 = [Re y / s, Im y / s] (2 channels, padded to
 // 16), 64 channels, kernel 9, zero padding at the sequence ends.  Weights are
 // BF16 (FP32 master copy for Adam), activations BF16 channels-last, all
-// products accumulate in FP32 on the tensor cores (warp-level
-// mma.sync.m16n8k16 BF16 implicit GEMMs).  Loss L = mean |z - tx|^2.
+// products accumulate in FP32 on the tensor cores: the hidden 64 -> 64 layers
+// (forward and input gradient) as tcgen05 MMAs with tensor-memory
+// accumulators, the narrow first/last layers and the weight gradients as
+// warp-level mma.sync.m16n8k16 BF16 implicit GEMMs.  Loss L = mean |z - tx|^2.
 //
 // Forward conv: out[p][co] = b[co] + sum_{kk<9, ci} W[co][kk][ci] in[p+kk-4][ci]
 //   GEMM D[co][p], M = COUT, N = positions, K = 9*CIN.
@@ -124,6 +126,157 @@ __global__ void __launch_bounds__(128) conv_fwd_kernel(const bf16* __restrict__ 
             }
 }
 
+// ------------------------------------------------------------ tcgen05 forward conv (64 -> 64)
+// The hidden 64 -> 64 layers (forward and input gradient) as a tcgen05
+// implicit GEMM: D[p][co] with M = 128 positions (the CTA's tile), N = 64
+// output channels, K = 9 taps x 64 input channels, accumulated in tensor
+// memory (64 FP32 columns); one thread issues the 36 MMAs of K = 16 and
+// commits them to an mbarrier, then each warp reads its 32 rows back with
+// tcgen05.ld for the epilogue (bias, ReLU, mask, BF16).
+// Shared-memory operands use the no-swizzle K-major canonical layout: rows of
+// 8 consecutive K elements (16 bytes), 8-row core matrices SBO = 128 B apart
+// along M/N, core matrices LBO apart along K.  Activations are stored
+// [k group][row][8] with 136 rows (the tile plus the 4-sample halo on each
+// side), so the operand of tap kk is the same layout starting kk rows
+// (kk x 16 B) further: the im2col is an address offset.  Weights are stored
+// [tap][k group][co][8].
+namespace tc {
+constexpr int M = 128, N = 64, ROWS = M + 2 * HALF;
+constexpr uint32_t LBO_A = ROWS * 16, LBO_B = N * 16, SBO = 128;
+constexpr size_t SMEM_B = (size_t)KW * 8 * N * 16;   // 73 728 bytes
+constexpr size_t SMEM_A = (size_t)8 * ROWS * 16;     // 17 408 bytes
+constexpr long long kWaitCap = 1ll << 22;            // mbarrier polls before giving up
+
+// Shared-memory matrix descriptor: start address, LBO and SBO in 16-byte
+// units, the descriptor version 1 at bit 46, base offset 0, no swizzling.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+           (1ull << 46);
+}
+// kind::f16 instruction descriptor: FP32 accumulator (bits 4-5 = 1), BF16 A
+// and B (bits 7-9 and 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at
+// bit 24.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void ld_x16(uint32_t taddr, float (&r)[16]) {
+    uint32_t u[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]),
+          "=r"(u[8]), "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; ++i) r[i] = __uint_as_float(u[i]);
+}
+}  // namespace tc
+
+// in: [B][L][64] bf16, W: [64][KW][64] bf16, bias: [64] f32 or null, out [B][L][64] bf16.
+// If the MMAs do not complete within the poll cap the tile is written as NaN.
+__global__ void __launch_bounds__(128) conv_fwd_tc_kernel(const bf16* __restrict__ in, const bf16* __restrict__ W,
+                                                          const float* __restrict__ bias, bf16* __restrict__ out,
+                                                          int L, int relu, const bf16* __restrict__ mask) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    bf16* Bs = reinterpret_cast<bf16*>(smem_raw);                 // [tap][kgroup][co][8]
+    bf16* As = reinterpret_cast<bf16*>(smem_raw + tc::SMEM_B);    // [kgroup][row][8]
+    __shared__ __align__(8) unsigned long long bar;
+    __shared__ uint32_t tmem_base;
+    const int b = blockIdx.y;
+    const int p0 = blockIdx.x * tc::M;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bf16* inb = in + (size_t)b * L * CW;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(tc::smem_addr(&tmem_base)),
+                     "r"(tc::N));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(tc::smem_addr(&bar)), "r"(1));
+        asm volatile("fence.mbarrier_init.release.cluster;\n");
+    }
+    // weights: 16-byte rows W[co][kk][8g .. 8g+7] -> Bs[(kk*8 + g)*64 + co]
+    const uint4* W4 = reinterpret_cast<const uint4*>(W);
+    uint4* B4 = reinterpret_cast<uint4*>(Bs);
+    for (int i = threadIdx.x; i < KW * 8 * tc::N; i += 128) {
+        const int co = i % tc::N, kg = i / tc::N;   // kg = kk*8 + g
+        const int kk = kg / 8, g = kg % 8;
+        B4[i] = W4[((size_t)co * KW + kk) * 8 + g];
+    }
+    // activations: As[g][r] = in[p0 - 4 + r][8g .. 8g+7] (zero outside [0, L))
+    uint4* A4 = reinterpret_cast<uint4*>(As);
+    const uint4* in4 = reinterpret_cast<const uint4*>(inb);
+    for (int i = threadIdx.x; i < 8 * tc::ROWS; i += 128) {
+        const int g = i / tc::ROWS, r = i % tc::ROWS;
+        const int p = p0 - HALF + r;
+        A4[i] = (p >= 0 && p < L) ? in4[(size_t)p * 8 + g] : make_uint4(0u, 0u, 0u, 0u);
+    }
+    // make the operands visible to the tensor core's (async) proxy
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = tmem_base;
+
+    if (threadIdx.x == 0) {
+        const uint32_t a0 = tc::smem_addr(As), b0 = tc::smem_addr(Bs);
+        for (int kk = 0; kk < KW; ++kk)
+#pragma unroll
+            for (int kc = 0; kc < 4; ++kc) {  // 16 input channels = 2 K core matrices per MMA
+                const uint64_t ad = tc::smem_desc(a0 + kk * 16 + kc * 2 * tc::LBO_A, tc::LBO_A, tc::SBO);
+                const uint64_t bd = tc::smem_desc(b0 + (kk * 8 + kc * 2) * tc::LBO_B, tc::LBO_B, tc::SBO);
+                const uint32_t acc = (kk | kc) ? 1u : 0u;
+                asm volatile(
+                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(tc::IDESC), "r"(acc));
+            }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+            tc::smem_addr(&bar)));
+    }
+    // bounded wait for the MMAs (phase 0 of the barrier)
+    uint32_t done = 0;
+    for (long long it = 0; it < tc::kWaitCap && !done; ++it)
+        asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.b32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done)
+                     : "r"(tc::smem_addr(&bar)), "r"(0));
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+
+    const int row = 32 * warp + lane;
+    const int p = p0 + row;
+    const size_t ob = (size_t)b * L * CW;
+#pragma unroll
+    for (int c0 = 0; c0 < tc::N; c0 += 16) {
+        float v[16];
+        tc::ld_x16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        if (p < L) {
+            uint32_t packed[8];
+#pragma unroll
+            for (int j = 0; j < 16; j += 2) {
+                float x0 = v[j] + (bias ? bias[c0 + j] : 0.f), x1 = v[j + 1] + (bias ? bias[c0 + j + 1] : 0.f);
+                if (relu) {
+                    x0 = fmaxf(x0, 0.f);
+                    x1 = fmaxf(x1, 0.f);
+                }
+                if (mask) {
+                    if (!(__bfloat162float(mask[ob + (size_t)p * CW + c0 + j]) > 0.f)) x0 = 0.f;
+                    if (!(__bfloat162float(mask[ob + (size_t)p * CW + c0 + j + 1]) > 0.f)) x1 = 0.f;
+                }
+                if (!done) x0 = x1 = __int_as_float(0x7fc00000);
+                packed[j / 2] = pack2(__float2bfloat16(x0), __float2bfloat16(x1));
+            }
+            uint4* o = reinterpret_cast<uint4*>(out + ob + (size_t)p * CW + c0);
+            o[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+            o[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(tc::N));
+}
+
 // ------------------------------------------------------------ weight gradient
 // gW[co][kk][ci] += sum_p g[p][co] in[p+kk-4][ci] over the CTA's position
 // chunk; grid = (KW, chunks, B).  Tiles of 64 positions are staged transposed
@@ -192,19 +345,36 @@ __global__ void __launch_bounds__(128) conv_wgrad_kernel(const bf16* __restrict_
             }
 }
 
-// bias gradient: gb[co] += sum_p g[p][co]
+// bias gradient: gb[co] += sum_p g[p][co].  Each lane sums one channel pair
+// over a slot of positions, so a warp reads whole 128-byte rows; warps and
+// then CTAs combine in shared memory and one atomic per channel per CTA.
 template <int C>
-__global__ void bias_grad_kernel(const bf16* __restrict__ g, size_t positions, float* __restrict__ gb) {
-    float acc[C];
-#pragma unroll
-    for (int c = 0; c < C; ++c) acc[c] = 0.f;
-    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < positions; p += (size_t)gridDim.x * blockDim.x)
-#pragma unroll
-        for (int c = 0; c < C; ++c) acc[c] += __bfloat162float(g[p * C + c]);
-#pragma unroll
-    for (int c = 0; c < C; ++c) {
-        const float v = warp_sum(acc[c]);
-        if ((threadIdx.x & 31) == 0) atomicAdd(&gb[c], v);
+__global__ void __launch_bounds__(256) bias_grad_kernel(const bf16* __restrict__ g, size_t positions,
+                                                        float* __restrict__ gb) {
+    constexpr int HC = C / 2, PW = 32 / HC;  // channel pairs; positions per warp step
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int cp = lane % HC, po = lane / HC;
+    float a0 = 0.f, a1 = 0.f;
+    const size_t step = (size_t)gridDim.x * nw * PW;
+    for (size_t p = ((size_t)blockIdx.x * nw + warp) * PW + po; p < positions; p += step) {
+        const __nv_bfloat162 v = reinterpret_cast<const __nv_bfloat162*>(g + p * C)[cp];
+        a0 += __low2float(v);
+        a1 += __high2float(v);
+    }
+    for (int o = HC; o < 32; o <<= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+    }
+    __shared__ float sh[8][C];
+    if (po == 0) {
+        sh[warp][2 * cp] = a0;
+        sh[warp][2 * cp + 1] = a1;
+    }
+    __syncthreads();
+    if (threadIdx.x < C) {
+        float t = 0.f;
+        for (int w = 0; w < nw; ++w) t += sh[w][threadIdx.x];
+        atomicAdd(&gb[threadIdx.x], t);
     }
 }
 
@@ -273,6 +443,15 @@ inline int gridn(size_t n) { return (int)std::max<size_t>(1, std::min<size_t>((n
 template <int CIN, int COUT, bool F32>
 cudaError_t conv_fwd(const bf16* in, const bf16* W, const float* bias, void* out, int L, int B, int relu,
                      const bf16* mask, cudaStream_t s) {
+    if constexpr (CIN == CW && COUT == CW && !F32) {
+        const size_t smem = tc::SMEM_B + tc::SMEM_A;
+        cudaError_t e = cudaFuncSetAttribute(conv_fwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        conv_fwd_tc_kernel<<<dim3((L + tc::M - 1) / tc::M, B), 128, smem, s>>>(in, W, bias,
+                                                                              reinterpret_cast<bf16*>(out), L, relu, mask);
+        count_launch();
+        return cudaGetLastError();
+    }
     const size_t smem = sizeof(bf16) * ((size_t)COUT * (KW * CIN + 8) + (size_t)(NP + 2 * HALF) * (CIN + 8));
     cudaError_t e = cudaFuncSetAttribute(conv_fwd_kernel<CIN, COUT, F32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
@@ -487,7 +666,7 @@ FOCSS_API focss_status focss_cnn_loss_grad(focss_cnn* m, const focss_field* y, c
     // layer 4 (no activation): weights, bias, input gradient masked by out3 > 0
     if (e == cudaSuccess) e = fg::conv_wgrad<fg::CW, fg::COUT4>(m->g16, m->act[3], G + Y.w[3], L, B, s);
     if (e == cudaSuccess) {
-        fg::bias_grad_kernel<fg::COUT4><<<fg::gridn(n), 256, 0, s>>>(m->g16, n, G + Y.b[3]);
+        fg::bias_grad_kernel<fg::COUT4><<<152 * 4, 256, 0, s>>>(m->g16, n, G + Y.b[3]);
         fg::count_launch();
         e = cudaGetLastError();
     }
@@ -499,7 +678,7 @@ FOCSS_API focss_status focss_cnn_loss_grad(focss_cnn* m, const focss_field* y, c
     for (int l = 2; l >= 1 && e == cudaSuccess; --l) {
         e = fg::conv_wgrad<fg::CW, fg::CW>(g, m->act[l], G + Y.w[l], L, B, s);
         if (e == cudaSuccess) {
-            fg::bias_grad_kernel<fg::CW><<<fg::gridn(n), 256, 0, s>>>(g, n, G + Y.b[l]);
+            fg::bias_grad_kernel<fg::CW><<<152 * 4, 256, 0, s>>>(g, n, G + Y.b[l]);
             fg::count_launch();
             e = cudaGetLastError();
         }
@@ -509,7 +688,7 @@ FOCSS_API focss_status focss_cnn_loss_grad(focss_cnn* m, const focss_field* y, c
     // layer 1: weights and bias only
     if (e == cudaSuccess) e = fg::conv_wgrad<fg::CIN0, fg::CW>(g, m->act[0], G + Y.w[0], L, B, s);
     if (e == cudaSuccess) {
-        fg::bias_grad_kernel<fg::CW><<<fg::gridn(n), 256, 0, s>>>(g, n, G + Y.b[0]);
+        fg::bias_grad_kernel<fg::CW><<<152 * 4, 256, 0, s>>>(g, n, G + Y.b[0]);
         fg::count_launch();
         e = cudaGetLastError();
     }
