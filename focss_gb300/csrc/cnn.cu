@@ -4,10 +4,10 @@
 //     relu(conv1(x0))))))), x0 = [Re y / s, Im y / s] (2 channels, padded to
 // 16), 64 channels, kernel 9, zero padding at the sequence ends.  Weights are
 // BF16 (FP32 master copy for Adam), activations BF16 channels-last, all
-// products accumulate in FP32 on the tensor cores: the hidden 64 -> 64 layers
-// (forward and input gradient) as tcgen05 MMAs with tensor-memory
-// accumulators, the narrow first/last layers and the weight gradients as
-// warp-level mma.sync.m16n8k16 BF16 implicit GEMMs.  Loss L = mean |z - tx|^2.
+// products accumulate in FP32 on the tensor cores: the convolutions (forward
+// and input gradient) as tcgen05 MMAs with tensor-memory accumulators, the
+// weight gradients as warp-level mma.sync.m16n8k16 BF16 GEMMs.  Loss
+// L = mean |z - tx|^2.
 //
 // Forward conv: out[p][co] = b[co] + sum_{kk<9, ci} W[co][kk][ci] in[p+kk-4][ci]
 //   GEMM D[co][p], M = COUT, N = positions, K = 9*CIN.
@@ -30,7 +30,6 @@ namespace {
 typedef __nv_bfloat16 bf16;
 constexpr int KW = 9;       // kernel width
 constexpr int HALF = 4;     // (KW - 1) / 2
-constexpr int NP = 128;     // positions per forward CTA (4 warps x 32)
 constexpr int CW = 64;      // hidden channels
 constexpr int CIN0 = 16;    // padded input channels (2 used)
 constexpr int COUT4 = 16;   // padded output channels (2 used)
@@ -48,91 +47,14 @@ __device__ __forceinline__ uint32_t pack2(bf16 lo, bf16 hi) {
     return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
 }
 
-// ------------------------------------------------------------ forward conv
-// in: [B][L][CIN] bf16, W: [COUT][KW][CIN] bf16, bias: [COUT] f32.
-// out: [B][L][COUT] (bf16, or f32 when OUT_F32).  relu: apply max(0, .).
-// mask (optional, [B][L][COUT] bf16): multiply the result by (mask > 0).
-template <int CIN, int COUT, bool OUT_F32>
-__global__ void __launch_bounds__(128) conv_fwd_kernel(const bf16* __restrict__ in, const bf16* __restrict__ W,
-                                                       const float* __restrict__ bias, void* __restrict__ out,
-                                                       int L, int relu, const bf16* __restrict__ mask) {
-    constexpr int KS = KW * CIN + 8;   // padded weight row (bank spread)
-    constexpr int AS = CIN + 8;        // padded activation row
-    constexpr int MT = COUT / 16;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    bf16* Ws = reinterpret_cast<bf16*>(smem_raw);
-    bf16* As = Ws + COUT * KS;
-    const int b = blockIdx.y;
-    const int p0 = blockIdx.x * NP;
-    const bf16* inb = in + (size_t)b * L * CIN;
-    for (int i = threadIdx.x; i < COUT * KW * CIN; i += blockDim.x) {
-        const int co = i / (KW * CIN), k = i % (KW * CIN);
-        Ws[co * KS + k] = W[i];
-    }
-    for (int i = threadIdx.x; i < (NP + 2 * HALF) * CIN; i += blockDim.x) {
-        const int r = i / CIN, ci = i % CIN;
-        const int p = p0 - HALF + r;
-        As[r * AS + ci] = (p >= 0 && p < L) ? inb[(size_t)p * CIN + ci] : __float2bfloat16(0.f);
-    }
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    float acc[MT][4][4];
-#pragma unroll
-    for (int mt = 0; mt < MT; ++mt)
-#pragma unroll
-        for (int nt = 0; nt < 4; ++nt)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) acc[mt][nt][q] = 0.f;
-#pragma unroll 1
-    for (int kk = 0; kk < KW; ++kk) {
-#pragma unroll
-        for (int c0 = 0; c0 < CIN; c0 += 16) {
-            uint32_t af[MT][4];
-#pragma unroll
-            for (int mt = 0; mt < MT; ++mt) {
-                const bf16* w0 = Ws + (16 * mt + g) * KS + kk * CIN + c0 + 2 * t;
-                af[mt][0] = ld32(w0);
-                af[mt][1] = ld32(w0 + 8 * KS);
-                af[mt][2] = ld32(w0 + 8);
-                af[mt][3] = ld32(w0 + 8 * KS + 8);
-            }
-#pragma unroll
-            for (int nt = 0; nt < 4; ++nt) {
-                const int n = 32 * warp + 8 * nt + g;
-                const bf16* a0 = As + (n + kk) * AS + c0 + 2 * t;
-                const uint32_t bfr[2] = {ld32(a0), ld32(a0 + 8)};
-#pragma unroll
-                for (int mt = 0; mt < MT; ++mt) mma_bf16(acc[mt][nt], af[mt], bfr);
-            }
-        }
-    }
-    const size_t ob = (size_t)b * L * COUT;
-#pragma unroll
-    for (int mt = 0; mt < MT; ++mt)
-#pragma unroll
-        for (int nt = 0; nt < 4; ++nt)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int co = 16 * mt + g + (q >= 2 ? 8 : 0);
-                const int p = p0 + 32 * warp + 8 * nt + 2 * t + (q & 1);
-                if (p >= L) continue;
-                float v = acc[mt][nt][q] + (bias ? bias[co] : 0.f);
-                if (relu) v = fmaxf(v, 0.f);
-                if (mask && !(__bfloat162float(mask[ob + (size_t)p * COUT + co]) > 0.f)) v = 0.f;
-                if (OUT_F32)
-                    reinterpret_cast<float*>(out)[ob + (size_t)p * COUT + co] = v;
-                else
-                    reinterpret_cast<bf16*>(out)[ob + (size_t)p * COUT + co] = __float2bfloat16(v);
-            }
-}
-
-// ------------------------------------------------------------ tcgen05 forward conv (64 -> 64)
-// The hidden 64 -> 64 layers (forward and input gradient) as a tcgen05
-// implicit GEMM: D[p][co] with M = 128 positions (the CTA's tile), N = 64
-// output channels, K = 9 taps x 64 input channels, accumulated in tensor
-// memory (64 FP32 columns); one thread issues the 36 MMAs of K = 16 and
+// ------------------------------------------------------------ tcgen05 forward conv
+// Every forward-type convolution (the four layers, and the input gradients)
+// as a tcgen05 implicit GEMM: D[p][co] with M = 128 positions per tile,
+// N = COUT output channels, K = 9 taps x CIN input channels, accumulated in
+// tensor memory (FP32 columns); one thread issues the MMAs of K = 16 and
 // commits them to an mbarrier, then each warp reads its 32 rows back with
-// tcgen05.ld for the epilogue (bias, ReLU, mask, BF16).
+// tcgen05.ld for the epilogue (bias, ReLU, mask, BF16 or FP32).  A CTA stages
+// the weights once and then runs `tiles` consecutive position tiles.
 // Shared-memory operands use the no-swizzle K-major canonical layout: rows of
 // 8 consecutive K elements (16 bytes), 8-row core matrices SBO = 128 B apart
 // along M/N, core matrices LBO apart along K.  Activations are stored
@@ -141,11 +63,17 @@ __global__ void __launch_bounds__(128) conv_fwd_kernel(const bf16* __restrict__ 
 // (kk x 16 B) further: the im2col is an address offset.  Weights are stored
 // [tap][k group][co][8].
 namespace tc {
-constexpr int M = 128, N = 64, ROWS = M + 2 * HALF;
-constexpr uint32_t LBO_A = ROWS * 16, LBO_B = N * 16, SBO = 128;
-constexpr size_t SMEM_B = (size_t)KW * 8 * N * 16;   // 73 728 bytes
-constexpr size_t SMEM_A = (size_t)8 * ROWS * 16;     // 17 408 bytes
-constexpr long long kWaitCap = 1ll << 22;            // mbarrier polls before giving up
+constexpr int M = 128, ROWS = M + 2 * HALF;
+constexpr uint32_t SBO = 128;
+constexpr long long kWaitCap = 1ll << 22;  // mbarrier polls before giving up
+
+template <int CIN, int COUT>
+struct Shape {
+    static constexpr uint32_t LBO_A = ROWS * 16, LBO_B = COUT * 16;
+    static constexpr size_t SMEM_B = (size_t)KW * (CIN / 8) * COUT * 16;
+    static constexpr size_t SMEM_A = (size_t)(CIN / 8) * ROWS * 16;
+    static constexpr uint32_t TMEM_COLS = COUT < 32 ? 32 : COUT;  // allocation: a power of two >= 32
+};
 
 // Shared-memory matrix descriptor: start address, LBO and SBO in 16-byte
 // units, the descriptor version 1 at bit 46, base offset 0, no swizzling.
@@ -156,7 +84,9 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
 // kind::f16 instruction descriptor: FP32 accumulator (bits 4-5 = 1), BF16 A
 // and B (bits 7-9 and 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at
 // bit 24.
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+__host__ __device__ constexpr uint32_t idesc(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -172,109 +102,125 @@ __device__ __forceinline__ void ld_x16(uint32_t taddr, float (&r)[16]) {
 }
 }  // namespace tc
 
-// in: [B][L][64] bf16, W: [64][KW][64] bf16, bias: [64] f32 or null, out [B][L][64] bf16.
-// If the MMAs do not complete within the poll cap the tile is written as NaN.
+// in: [B][L][CIN] bf16, W: [COUT][KW][CIN] bf16, bias: [COUT] f32 or null,
+// out [B][L][COUT] (bf16, or f32 when OUT_F32); mask (optional, [B][L][COUT]
+// bf16): multiply the result by (mask > 0).  If the MMAs do not complete
+// within the poll cap the tile is written as NaN.
+template <int CIN, int COUT, bool OUT_F32>
 __global__ void __launch_bounds__(128) conv_fwd_tc_kernel(const bf16* __restrict__ in, const bf16* __restrict__ W,
-                                                          const float* __restrict__ bias, bf16* __restrict__ out,
-                                                          int L, int relu, const bf16* __restrict__ mask) {
+                                                          const float* __restrict__ bias, void* __restrict__ out,
+                                                          int L, int relu, const bf16* __restrict__ mask, int tiles) {
+    using S = tc::Shape<CIN, COUT>;
+    constexpr int KG = CIN / 8;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    bf16* Bs = reinterpret_cast<bf16*>(smem_raw);                 // [tap][kgroup][co][8]
-    bf16* As = reinterpret_cast<bf16*>(smem_raw + tc::SMEM_B);    // [kgroup][row][8]
+    bf16* Bs = reinterpret_cast<bf16*>(smem_raw);              // [tap][kgroup][co][8]
+    bf16* As = reinterpret_cast<bf16*>(smem_raw + S::SMEM_B);  // [kgroup][row][8]
     __shared__ __align__(8) unsigned long long bar;
     __shared__ uint32_t tmem_base;
     const int b = blockIdx.y;
-    const int p0 = blockIdx.x * tc::M;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const bf16* inb = in + (size_t)b * L * CW;
+    const bf16* inb = in + (size_t)b * L * CIN;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(tc::smem_addr(&tmem_base)),
-                     "r"(tc::N));
+                     "r"(S::TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
     }
     if (threadIdx.x == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(tc::smem_addr(&bar)), "r"(1));
         asm volatile("fence.mbarrier_init.release.cluster;\n");
     }
-    // weights: 16-byte rows W[co][kk][8g .. 8g+7] -> Bs[(kk*8 + g)*64 + co]
+    // weights: 16-byte rows W[co][kk][8g .. 8g+7] -> Bs[(kk*KG + g)*COUT + co]
     const uint4* W4 = reinterpret_cast<const uint4*>(W);
     uint4* B4 = reinterpret_cast<uint4*>(Bs);
-    for (int i = threadIdx.x; i < KW * 8 * tc::N; i += 128) {
-        const int co = i % tc::N, kg = i / tc::N;   // kg = kk*8 + g
-        const int kk = kg / 8, g = kg % 8;
-        B4[i] = W4[((size_t)co * KW + kk) * 8 + g];
+    for (int i = threadIdx.x; i < KW * KG * COUT; i += 128) {
+        const int co = i % COUT, kg = i / COUT;  // kg = kk*KG + g
+        B4[i] = W4[((size_t)co * KW + kg / KG) * KG + kg % KG];
     }
-    // activations: As[g][r] = in[p0 - 4 + r][8g .. 8g+7] (zero outside [0, L))
-    uint4* A4 = reinterpret_cast<uint4*>(As);
-    const uint4* in4 = reinterpret_cast<const uint4*>(inb);
-    for (int i = threadIdx.x; i < 8 * tc::ROWS; i += 128) {
-        const int g = i / tc::ROWS, r = i % tc::ROWS;
-        const int p = p0 - HALF + r;
-        A4[i] = (p >= 0 && p < L) ? in4[(size_t)p * 8 + g] : make_uint4(0u, 0u, 0u, 0u);
-    }
-    // make the operands visible to the tensor core's (async) proxy
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    const uint32_t tmem = tmem_base;
-
-    if (threadIdx.x == 0) {
-        const uint32_t a0 = tc::smem_addr(As), b0 = tc::smem_addr(Bs);
-        for (int kk = 0; kk < KW; ++kk)
-#pragma unroll
-            for (int kc = 0; kc < 4; ++kc) {  // 16 input channels = 2 K core matrices per MMA
-                const uint64_t ad = tc::smem_desc(a0 + kk * 16 + kc * 2 * tc::LBO_A, tc::LBO_A, tc::SBO);
-                const uint64_t bd = tc::smem_desc(b0 + (kk * 8 + kc * 2) * tc::LBO_B, tc::LBO_B, tc::SBO);
-                const uint32_t acc = (kk | kc) ? 1u : 0u;
-                asm volatile(
-                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-                    "l"(ad), "l"(bd), "r"(tc::IDESC), "r"(acc));
-            }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-            tc::smem_addr(&bar)));
-    }
-    // bounded wait for the MMAs (phase 0 of the barrier)
-    uint32_t done = 0;
-    for (long long it = 0; it < tc::kWaitCap && !done; ++it)
-        asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.b32 %0, 1, 0, p;\n}\n"
-                     : "=r"(done)
-                     : "r"(tc::smem_addr(&bar)), "r"(0));
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-
-    const int row = 32 * warp + lane;
-    const int p = p0 + row;
-    const size_t ob = (size_t)b * L * CW;
-#pragma unroll
-    for (int c0 = 0; c0 < tc::N; c0 += 16) {
-        float v[16];
-        tc::ld_x16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
-        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-        if (p < L) {
-            uint32_t packed[8];
-#pragma unroll
-            for (int j = 0; j < 16; j += 2) {
-                float x0 = v[j] + (bias ? bias[c0 + j] : 0.f), x1 = v[j + 1] + (bias ? bias[c0 + j + 1] : 0.f);
-                if (relu) {
-                    x0 = fmaxf(x0, 0.f);
-                    x1 = fmaxf(x1, 0.f);
-                }
-                if (mask) {
-                    if (!(__bfloat162float(mask[ob + (size_t)p * CW + c0 + j]) > 0.f)) x0 = 0.f;
-                    if (!(__bfloat162float(mask[ob + (size_t)p * CW + c0 + j + 1]) > 0.f)) x1 = 0.f;
-                }
-                if (!done) x0 = x1 = __int_as_float(0x7fc00000);
-                packed[j / 2] = pack2(__float2bfloat16(x0), __float2bfloat16(x1));
-            }
-            uint4* o = reinterpret_cast<uint4*>(out + ob + (size_t)p * CW + c0);
-            o[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-            o[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+    uint32_t tmem = 0;
+    bool ok = true;
+    for (int t = 0; t < tiles; ++t) {
+        const int p0 = (blockIdx.x * tiles + t) * tc::M;
+        if (p0 >= L) break;
+        // activations: As[g][r] = in[p0 - 4 + r][8g .. 8g+7] (zero outside [0, L))
+        uint4* A4 = reinterpret_cast<uint4*>(As);
+        const uint4* in4 = reinterpret_cast<const uint4*>(inb);
+        for (int i = threadIdx.x; i < KG * tc::ROWS; i += 128) {
+            const int g = i / tc::ROWS, r = i % tc::ROWS;
+            const int p = p0 - HALF + r;
+            A4[i] = (p >= 0 && p < L) ? in4[(size_t)p * KG + g] : make_uint4(0u, 0u, 0u, 0u);
         }
+        // make the operands visible to the tensor core's (async) proxy
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        tmem = tmem_base;
+        if (threadIdx.x == 0) {
+            const uint32_t a0 = tc::smem_addr(As), b0 = tc::smem_addr(Bs);
+            for (int kk = 0; kk < KW; ++kk)
+#pragma unroll
+                for (int kc = 0; kc < CIN / 16; ++kc) {  // 16 input channels = 2 K core matrices per MMA
+                    const uint64_t ad = tc::smem_desc(a0 + kk * 16 + kc * 2 * S::LBO_A, S::LBO_A, tc::SBO);
+                    const uint64_t bd = tc::smem_desc(b0 + (kk * KG + kc * 2) * S::LBO_B, S::LBO_B, tc::SBO);
+                    const uint32_t acc = (kk | kc) ? 1u : 0u;
+                    asm volatile(
+                        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                        "l"(ad), "l"(bd), "r"(tc::idesc(COUT)), "r"(acc));
+                }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                tc::smem_addr(&bar)));
+        }
+        // bounded wait for this tile's MMAs (barrier phase t)
+        uint32_t done = 0;
+        for (long long it = 0; it < tc::kWaitCap && !done; ++it)
+            asm volatile(
+                "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.b32 %0, 1, 0, p;\n}\n"
+                : "=r"(done)
+                : "r"(tc::smem_addr(&bar)), "r"((uint32_t)(t & 1)));
+        ok = ok && done;
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+
+        const int p = p0 + 32 * warp + lane;
+        const size_t ob = (size_t)b * L * COUT;
+#pragma unroll
+        for (int c0 = 0; c0 < COUT; c0 += 16) {
+            float v[16];
+            tc::ld_x16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            if (p < L) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    float x = v[j] + (bias ? bias[c0 + j] : 0.f);
+                    if (relu) x = fmaxf(x, 0.f);
+                    if (mask && !(__bfloat162float(mask[ob + (size_t)p * COUT + c0 + j]) > 0.f)) x = 0.f;
+                    v[j] = ok ? x : __int_as_float(0x7fc00000);
+                }
+                if (OUT_F32) {
+                    float4* o = reinterpret_cast<float4*>(reinterpret_cast<float*>(out) + ob + (size_t)p * COUT + c0);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                } else {
+                    uint32_t packed[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) packed[j] = pack2(__float2bfloat16(v[2 * j]), __float2bfloat16(v[2 * j + 1]));
+                    uint4* o = reinterpret_cast<uint4*>(reinterpret_cast<bf16*>(out) + ob + (size_t)p * COUT + c0);
+                    o[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                    o[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+                }
+            }
+        }
+        // every warp's reads of the accumulator and of the activation tile
+        // are done before the next tile's MMAs and staging
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     }
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(tc::N));
+    if (warp == 0) {
+        tmem = tmem_base;
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(S::TMEM_COLS));
+    }
 }
 
 // ------------------------------------------------------------ weight gradient
@@ -443,20 +389,18 @@ inline int gridn(size_t n) { return (int)std::max<size_t>(1, std::min<size_t>((n
 template <int CIN, int COUT, bool F32>
 cudaError_t conv_fwd(const bf16* in, const bf16* W, const float* bias, void* out, int L, int B, int relu,
                      const bf16* mask, cudaStream_t s) {
-    if constexpr (CIN == CW && COUT == CW && !F32) {
-        const size_t smem = tc::SMEM_B + tc::SMEM_A;
-        cudaError_t e = cudaFuncSetAttribute(conv_fwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        conv_fwd_tc_kernel<<<dim3((L + tc::M - 1) / tc::M, B), 128, smem, s>>>(in, W, bias,
-                                                                              reinterpret_cast<bf16*>(out), L, relu, mask);
-        count_launch();
-        return cudaGetLastError();
-    }
-    const size_t smem = sizeof(bf16) * ((size_t)COUT * (KW * CIN + 8) + (size_t)(NP + 2 * HALF) * (CIN + 8));
-    cudaError_t e = cudaFuncSetAttribute(conv_fwd_kernel<CIN, COUT, F32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    using S = tc::Shape<CIN, COUT>;
+    const size_t smem = S::SMEM_B + S::SMEM_A;
+    cudaError_t e = cudaFuncSetAttribute(conv_fwd_tc_kernel<CIN, COUT, F32>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    conv_fwd_kernel<CIN, COUT, F32><<<dim3((L + NP - 1) / NP, B), 128, smem, s>>>(in, W, bias, out, L, relu, mask);
+    // about two waves of CTAs, each running several position tiles on one
+    // staged copy of the weights
+    const int ntiles = (L + tc::M - 1) / tc::M;
+    const int per_item = std::max(1, (152 * 4 + B - 1) / B);
+    const int tiles = std::max(1, (ntiles + per_item - 1) / per_item);
+    conv_fwd_tc_kernel<CIN, COUT, F32><<<dim3((ntiles + tiles - 1) / tiles, B), 128, smem, s>>>(in, W, bias, out, L,
+                                                                                                 relu, mask, tiles);
     count_launch();
     return cudaGetLastError();
 }
