@@ -54,7 +54,9 @@ __device__ __forceinline__ uint32_t pack2(bf16 lo, bf16 hi) {
 // tensor memory (FP32 columns); one thread issues the MMAs of K = 16 and
 // commits them to an mbarrier, then each warp reads its 32 rows back with
 // tcgen05.ld for the epilogue (bias, ReLU, mask, BF16 or FP32).  A CTA stages
-// the weights once and then runs `tiles` consecutive position tiles.
+// the weights once and then runs `tiles` consecutive position tiles, the
+// activations of the next tile copied asynchronously (cp.async) into the
+// second of two buffers while the current tile's MMAs and epilogue run.
 // Shared-memory operands use the no-swizzle K-major canonical layout: rows of
 // 8 consecutive K elements (16 bytes), 8-row core matrices SBO = 128 B apart
 // along M/N, core matrices LBO apart along K.  Activations are stored
@@ -71,7 +73,7 @@ template <int CIN, int COUT>
 struct Shape {
     static constexpr uint32_t LBO_A = ROWS * 16, LBO_B = COUT * 16;
     static constexpr size_t SMEM_B = (size_t)KW * (CIN / 8) * COUT * 16;
-    static constexpr size_t SMEM_A = (size_t)(CIN / 8) * ROWS * 16;
+    static constexpr size_t SMEM_A = (size_t)(CIN / 8) * ROWS * 16;  // one activation buffer (two are used)
     static constexpr uint32_t TMEM_COLS = COUT < 32 ? 32 : COUT;  // allocation: a power of two >= 32
 };
 
@@ -89,6 +91,11 @@ __host__ __device__ constexpr uint32_t idesc(int n) {
 }
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// 16-byte asynchronous copy global -> shared; `bytes` = 0 writes zeros.
+__device__ __forceinline__ void cp16(uint32_t dst, const void* src, uint32_t bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
+}
 
 __device__ __forceinline__ void ld_x16(uint32_t taddr, float (&r)[16]) {
     uint32_t u[16];
@@ -114,12 +121,14 @@ __global__ void __launch_bounds__(128) conv_fwd_tc_kernel(const bf16* __restrict
     constexpr int KG = CIN / 8;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     bf16* Bs = reinterpret_cast<bf16*>(smem_raw);              // [tap][kgroup][co][8]
-    bf16* As = reinterpret_cast<bf16*>(smem_raw + S::SMEM_B);  // [kgroup][row][8]
+    bf16* As = reinterpret_cast<bf16*>(smem_raw + S::SMEM_B);  // 2 x [kgroup][row][8]
     __shared__ __align__(8) unsigned long long bar;
     __shared__ uint32_t tmem_base;
+    __shared__ float s_bias[COUT];
     const int b = blockIdx.y;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const bf16* inb = in + (size_t)b * L * CIN;
+    for (int i = threadIdx.x; i < COUT; i += 128) s_bias[i] = bias ? bias[i] : 0.f;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(tc::smem_addr(&tmem_base)),
@@ -130,34 +139,47 @@ __global__ void __launch_bounds__(128) conv_fwd_tc_kernel(const bf16* __restrict
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(tc::smem_addr(&bar)), "r"(1));
         asm volatile("fence.mbarrier_init.release.cluster;\n");
     }
-    // weights: 16-byte rows W[co][kk][8g .. 8g+7] -> Bs[(kk*KG + g)*COUT + co]
+    // weights: 16-byte rows W[co][kk][8g .. 8g+7] -> Bs[(kk*KG + g)*COUT + co],
+    // asynchronous copies committed with the first activation tile
     const uint4* W4 = reinterpret_cast<const uint4*>(W);
-    uint4* B4 = reinterpret_cast<uint4*>(Bs);
+    const uint32_t bs0 = tc::smem_addr(Bs);
     for (int i = threadIdx.x; i < KW * KG * COUT; i += 128) {
         const int co = i % COUT, kg = i / COUT;  // kg = kk*KG + g
-        B4[i] = W4[((size_t)co * KW + kg / KG) * KG + kg % KG];
+        tc::cp16(bs0 + 16u * i, W4 + ((size_t)co * KW + kg / KG) * KG + kg % KG, 16u);
     }
-    uint32_t tmem = 0;
-    bool ok = true;
-    for (int t = 0; t < tiles; ++t) {
+    // activation tile t -> buffer t & 1: As[g][r] = in[p0 - 4 + r][8g .. 8g+7]
+    // (zero outside [0, L)), as asynchronous copies that overlap the previous
+    // tile's MMAs and epilogue
+    const uint4* in4 = reinterpret_cast<const uint4*>(inb);
+    auto stage = [&](int t) {
         const int p0 = (blockIdx.x * tiles + t) * tc::M;
-        if (p0 >= L) break;
-        // activations: As[g][r] = in[p0 - 4 + r][8g .. 8g+7] (zero outside [0, L))
-        uint4* A4 = reinterpret_cast<uint4*>(As);
-        const uint4* in4 = reinterpret_cast<const uint4*>(inb);
+        const uint32_t base = tc::smem_addr(As) + (uint32_t)((t & 1) * S::SMEM_A);
         for (int i = threadIdx.x; i < KG * tc::ROWS; i += 128) {
             const int g = i / tc::ROWS, r = i % tc::ROWS;
             const int p = p0 - HALF + r;
-            A4[i] = (p >= 0 && p < L) ? in4[(size_t)p * KG + g] : make_uint4(0u, 0u, 0u, 0u);
+            const bool in_range = p >= 0 && p < L;
+            tc::cp16(base + 16u * i, in_range ? (const void*)(in4 + (size_t)p * KG + g) : (const void*)in4,
+                     in_range ? 16u : 0u);
         }
-        // make the operands visible to the tensor core's (async) proxy
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+    const int rem = (L - (int)blockIdx.x * tiles * tc::M + tc::M - 1) / tc::M;  // tiles left from this CTA's first
+    const int n_here = rem < tiles ? rem : tiles;
+    if (n_here > 0) stage(0);
+    uint32_t tmem = 0;
+    bool ok = true;
+    for (int t = 0; t < n_here; ++t) {
+        const int p0 = (blockIdx.x * tiles + t) * tc::M;
+        // this tile's rows (and, for the first, the weights) have landed: the
+        // only group in flight; make them visible to the tensor core's proxy
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         tmem = tmem_base;
         if (threadIdx.x == 0) {
-            const uint32_t a0 = tc::smem_addr(As), b0 = tc::smem_addr(Bs);
+            const uint32_t a0 = tc::smem_addr(As) + (uint32_t)((t & 1) * S::SMEM_A), b0 = tc::smem_addr(Bs);
             for (int kk = 0; kk < KW; ++kk)
 #pragma unroll
                 for (int kc = 0; kc < CIN / 16; ++kc) {  // 16 input channels = 2 K core matrices per MMA
@@ -172,6 +194,9 @@ __global__ void __launch_bounds__(128) conv_fwd_tc_kernel(const bf16* __restrict
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
                 tc::smem_addr(&bar)));
         }
+        // the other buffer was read by the MMAs of tile t - 1, complete before
+        // that tile's epilogue: refill it with tile t + 1
+        if (t + 1 < n_here) stage(t + 1);
         // bounded wait for this tile's MMAs (barrier phase t)
         uint32_t done = 0;
         for (long long it = 0; it < tc::kWaitCap && !done; ++it)
@@ -192,7 +217,7 @@ __global__ void __launch_bounds__(128) conv_fwd_tc_kernel(const bf16* __restrict
             if (p < L) {
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
-                    float x = v[j] + (bias ? bias[c0 + j] : 0.f);
+                    float x = v[j] + s_bias[c0 + j];
                     if (relu) x = fmaxf(x, 0.f);
                     if (mask && !(__bfloat162float(mask[ob + (size_t)p * COUT + c0 + j]) > 0.f)) x = 0.f;
                     v[j] = ok ? x : __int_as_float(0x7fc00000);
@@ -390,7 +415,7 @@ template <int CIN, int COUT, bool F32>
 cudaError_t conv_fwd(const bf16* in, const bf16* W, const float* bias, void* out, int L, int B, int relu,
                      const bf16* mask, cudaStream_t s) {
     using S = tc::Shape<CIN, COUT>;
-    const size_t smem = S::SMEM_B + S::SMEM_A;
+    const size_t smem = S::SMEM_B + 2 * S::SMEM_A;
     cudaError_t e = cudaFuncSetAttribute(conv_fwd_tc_kernel<CIN, COUT, F32>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
