@@ -210,6 +210,27 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------- GPU arm
+def replica_seed(rank: int, seed: int) -> int:
+    """ASE seed of one propagation on `rank`: every replica draws independent
+    noise, so N GPUs run N independent batches of realizations (weak scaling,
+    no data exchanged between ranks)."""
+    return seed + 100003 * rank
+
+
+def reduce_over_ranks(dist, device, elapsed, work):
+    """(max elapsed over ranks, summed work): the whole-job aggregate of the
+    replicas, whose throughput is the total work over the slowest rank's
+    time.  Single process (dist None): the local values."""
+    if dist is None:
+        return float(elapsed), float(work)
+    import torch
+    mx = torch.tensor([float(elapsed)], dtype=torch.float64, device=device)
+    tt = torch.tensor([float(work)], dtype=torch.float64, device=device)
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    dist.all_reduce(tt, op=dist.ReduceOp.SUM)
+    return float(mx[0]), float(tt[0])
+
+
 def run_ours(args):
     import focss_gb300 as fg
     if not os.path.exists(fg.LIB_PATH):
@@ -264,7 +285,7 @@ def run_ours(args):
 
     for w in range(args.warmup):
         field.assign(pristine)
-        propagate(field, 1000 + w)
+        propagate(field, replica_seed(rank, 1000 + w))
     ctx.sync()
 
     clocks = ClockSampler(local)
@@ -278,7 +299,7 @@ def run_ours(args):
         field.assign(pristine)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        total_steps += propagate(field, 2000 + k)
+        total_steps += propagate(field, replica_seed(rank, 2000 + k))
         e1.record(stream)
         e1.synchronize()
         total_ms += e0.elapsed_time(e1)
@@ -289,15 +310,7 @@ def run_ours(args):
     clk = clocks.stop()
     sample_steps = total_steps * N
 
-    t_max = total_ms
-    total_samples = sample_steps
-    if dist is not None:
-        tt = torch.tensor([total_ms, float(sample_steps)], dtype=torch.float64, device="cuda")
-        mx = tt.clone()
-        dist.all_reduce(mx[:1], op=dist.ReduceOp.MAX)
-        dist.all_reduce(tt[1:], op=dist.ReduceOp.SUM)
-        t_max = float(mx[0])
-        total_samples = float(tt[1])
+    t_max, total_samples = reduce_over_ranks(dist, "cuda", total_ms, sample_steps)
     value = total_samples / (t_max / 1e3) / 1e9
 
     # ---- roofline probe: the split-step passes alone on the full batch
@@ -356,16 +369,11 @@ def run_ours(args):
         ctx.sync()
         t0 = time.perf_counter()
         check(lib().focss_field_upload_c64(field.h, hin.ctypes.data_as(C.c_void_p), hin.size), ctx.h)
-        e2e_steps += propagate(field, 3000 + k)
+        e2e_steps += propagate(field, replica_seed(rank, 3000 + k))
         check(lib().focss_field_download_c64(field.h, hout.ctypes.data_as(C.c_void_p), hout.size), ctx.h)
         t_e2e += time.perf_counter() - t0
-    e2e_val = e2e_steps * N / t_e2e / 1e9
-    if dist is not None:
-        tt = torch.tensor([t_e2e, float(e2e_steps * N)], dtype=torch.float64, device="cuda")
-        mx = tt.clone()
-        dist.all_reduce(mx[:1], op=dist.ReduceOp.MAX)
-        dist.all_reduce(tt[1:], op=dist.ReduceOp.SUM)
-        e2e_val = float(tt[1]) / float(mx[0]) / 1e9
+    t_e2e_max, e2e_total = reduce_over_ranks(dist, "cuda", t_e2e, e2e_steps * N)
+    e2e_val = e2e_total / t_e2e_max / 1e9
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
