@@ -4,16 +4,15 @@
 //     relu(conv1(x0))))))), x0 = [Re y / s, Im y / s] (2 channels, padded to
 // 16), 64 channels, kernel 9, zero padding at the sequence ends.  Weights are
 // BF16 (FP32 master copy for Adam), activations BF16 channels-last, all
-// products accumulate in FP32 on the tensor cores: the convolutions (forward
-// and input gradient) as tcgen05 MMAs with tensor-memory accumulators, the
-// weight gradients as warp-level mma.sync.m16n8k16 BF16 GEMMs.  Loss
-// L = mean |z - tx|^2.
+// products accumulate in FP32 on the tensor cores as tcgen05 MMAs with
+// tensor-memory accumulators (the convolutions, forward and input gradient,
+// and the weight gradients).  Loss L = mean |z - tx|^2.
 //
 // Forward conv: out[p][co] = b[co] + sum_{kk<9, ci} W[co][kk][ci] in[p+kk-4][ci]
-//   GEMM D[co][p], M = COUT, N = positions, K = 9*CIN.
+//   GEMM D[p][co], M = 128 positions per tile, N = COUT, K = 9*CIN.
 // Input gradient: the same conv with W'[ci][kk][co] = W[co][8-kk][ci].
 // Weight gradient: gW[co][kk][ci] = sum_p g[p][co] in[p+kk-4][ci]
-//   GEMM M = COUT, N = CIN per tap, K = positions (chunked, atomics).
+//   GEMM per tap, K = positions (chunked, atomics).
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -34,15 +33,6 @@ constexpr int CW = 64;      // hidden channels
 constexpr int CIN0 = 16;    // padded input channels (2 used)
 constexpr int COUT4 = 16;   // padded output channels (2 used)
 
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-__device__ __forceinline__ uint32_t ld32(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
 __device__ __forceinline__ uint32_t pack2(bf16 lo, bf16 hi) {
     return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
 }
@@ -248,72 +238,158 @@ __global__ void __launch_bounds__(128) conv_fwd_tc_kernel(const bf16* __restrict
     }
 }
 
-// ------------------------------------------------------------ weight gradient
-// gW[co][kk][ci] += sum_p g[p][co] in[p+kk-4][ci] over the CTA's position
-// chunk; grid = (KW, chunks, B).  Tiles of 64 positions are staged transposed
-// (channel-major) so fragments are 32-bit shared loads.
-constexpr int WG_TILE = 64;
+// ------------------------------------------------------------ tcgen05 weight gradient
+// gW[co][kk][ci] += sum_p g[p][co] in[p+kk-4][ci]: per tap a GEMM with
+// M = 64 (the 64-channel side: output channels when COUT = 64, else input
+// channels with the result transposed), N = the other side (64 or 16),
+// K = positions.  Both operands are MN-major (channels contiguous, as
+// stored), no-swizzle canonical layout: 16-byte rows of 8 channels, one row
+// per position, 8-row core matrices LBO = 128 B apart along K (positions),
+// channel groups SBO apart.  The input operand of tap kk is the same buffer
+// starting kk rows further (kk x 16 B), so the tap shift along K is an
+// address offset.  A CTA accumulates three taps in tensor memory over its
+// chunk of positions in tiles of 128, the next tile copied asynchronously
+// while the current tile's MMAs run; each buffer has its own mbarrier so a
+// wait never sees two completed phases.  With M = 64 the accumulator row m
+// sits in tensor-memory lane 32 (m / 16) + m % 16.
+namespace tcw {
+constexpr int P = 128;                // positions per tile
+constexpr int PR = P + 2 * HALF;      // input rows per tile (halo)
+constexpr int TAPS = 3;               // taps per CTA
+constexpr uint32_t LBO = 128;
+template <int COUT, int CIN>
+struct Shape {
+    static constexpr bool G_IS_A = COUT == 64;           // M side = output-gradient channels
+    static constexpr int NC = G_IS_A ? CIN : COUT;        // N
+    static constexpr size_t SMEM_G = (size_t)(COUT / 8) * P * 16;
+    static constexpr size_t SMEM_I = (size_t)(CIN / 8) * PR * 16;
+    static constexpr size_t STAGE = (SMEM_G + SMEM_I + 127) / 128 * 128;
+    static constexpr size_t SMEM = 2 * STAGE + 32 * 1024;  // the tail caps residency at 2 CTAs per SM
+    static constexpr uint32_t TMEM_COLS = TAPS * NC <= 64 ? 64 : 256;
+    // kind::f16: FP32 D, BF16 A/B, both MN-major (bits 15, 16), N = NC, M = 64.
+    static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) |
+                                      ((uint32_t)(NC >> 3) << 17) | ((uint32_t)(64 >> 4) << 24);
+    static_assert((COUT == 64 && (CIN == 64 || CIN == 16)) || (COUT == 16 && CIN == 64), "wgrad shapes");
+};
+}  // namespace tcw
+
 template <int CIN, int COUT>
-__global__ void __launch_bounds__(128) conv_wgrad_kernel(const bf16* __restrict__ gout, const bf16* __restrict__ in,
-                                                         float* __restrict__ gW, int L, int chunk) {
-    constexpr int PS = WG_TILE + 8;   // padded position stride
-    constexpr int MT = COUT / 16;     // m16 tiles (COUT)
-    constexpr int NT = CIN / 8;       // n8 tiles (CIN)
-    constexpr int WM = MT >= 4 ? MT / 4 : 1;   // m tiles per warp
-    constexpr int WN = MT >= 4 ? NT : NT / 4;  // n tiles per warp (split N when COUT < 64)
-    __shared__ __align__(16) bf16 gT[COUT][PS];
-    __shared__ __align__(16) bf16 iT[CIN][PS];
-    const int kk = blockIdx.x, b = blockIdx.z;
-    const int pstart = blockIdx.y * chunk, pend = min(L, pstart + chunk);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const int m_base = MT >= 4 ? warp * WM : 0;
-    const int n_base = MT >= 4 ? 0 : warp * WN;
-    float acc[WM][WN][4];
-#pragma unroll
-    for (int i = 0; i < WM; ++i)
-#pragma unroll
-        for (int j = 0; j < WN; ++j)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
-    const bf16* gb = gout + (size_t)b * L * COUT;
-    const bf16* ib = in + (size_t)b * L * CIN;
-    for (int p0 = pstart; p0 < pend; p0 += WG_TILE) {
-        __syncthreads();
-        for (int i = threadIdx.x; i < WG_TILE * COUT; i += blockDim.x) {
-            const int pp = i / COUT, co = i % COUT, p = p0 + pp;
-            gT[co][pp] = (p < pend) ? gb[(size_t)p * COUT + co] : __float2bfloat16(0.f);
+__global__ void __launch_bounds__(128) conv_wgrad_tc_kernel(const bf16* __restrict__ gout, const bf16* __restrict__ in,
+                                                            float* __restrict__ gW, int L, int chunk) {
+    using S = tcw::Shape<COUT, CIN>;
+    constexpr int GG = COUT / 8, IG = CIN / 8;  // 16-byte channel groups
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ __align__(8) unsigned long long bar[2];
+    __shared__ uint32_t tmem_base;
+    const int tap0 = blockIdx.x * tcw::TAPS;
+    const int b = blockIdx.z;
+    const int c0 = blockIdx.y * chunk;
+    const int c1 = min(L, c0 + chunk);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint4* g4 = reinterpret_cast<const uint4*>(gout + (size_t)b * L * COUT);
+    const uint4* i4 = reinterpret_cast<const uint4*>(in + (size_t)b * L * CIN);
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(tc::smem_addr(&tmem_base)),
+                     "r"(S::TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(tc::smem_addr(&bar[0])), "r"(1));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(tc::smem_addr(&bar[1])), "r"(1));
+        asm volatile("fence.mbarrier_init.release.cluster;\n");
+    }
+    // tile t -> stage t & 1: G[cg][r] = g[p0 + r][8cg ..], I[cg][r] = in[p0 - 4 + r][8cg ..]
+    // (zero outside [c0, c1) / [0, L))
+    auto stage = [&](int t) {
+        const int p0 = c0 + t * tcw::P;
+        const uint32_t base = tc::smem_addr(smem_raw) + (uint32_t)((t & 1) * S::STAGE);
+        for (int i = threadIdx.x; i < GG * tcw::P; i += 128) {
+            const int cg = i / tcw::P, r = i % tcw::P;
+            const int p = p0 + r;
+            const bool ok = p < c1;
+            tc::cp16(base + 16u * i, ok ? (const void*)(g4 + (size_t)p * GG + cg) : (const void*)g4, ok ? 16u : 0u);
         }
-        for (int i = threadIdx.x; i < WG_TILE * CIN; i += blockDim.x) {
-            const int pp = i / CIN, ci = i % CIN, p = p0 + pp, s = p + kk - HALF;
-            iT[ci][pp] = (p < pend && s >= 0 && s < L) ? ib[(size_t)s * CIN + ci] : __float2bfloat16(0.f);
+        for (int i = threadIdx.x; i < IG * tcw::PR; i += 128) {
+            const int cg = i / tcw::PR, r = i % tcw::PR;
+            const int p = p0 - HALF + r;
+            const bool ok = p >= 0 && p < L;
+            tc::cp16(base + (uint32_t)S::SMEM_G + 16u * i, ok ? (const void*)(i4 + (size_t)p * IG + cg) : (const void*)i4,
+                     ok ? 16u : 0u);
         }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+    auto wait_bar = [&](int t) {  // MMAs of tile t (buffer t & 1, its (t / 2)-th phase)
+        uint32_t done = 0;
+        for (long long it = 0; it < tc::kWaitCap && !done; ++it)
+            asm volatile(
+                "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.b32 %0, 1, 0, p;\n}\n"
+                : "=r"(done)
+                : "r"(tc::smem_addr(&bar[t & 1])), "r"((uint32_t)((t >> 1) & 1)));
+        return done != 0;
+    };
+    const int n = c1 > c0 ? (c1 - c0 + tcw::P - 1) / tcw::P : 0;
+    if (n > 0) stage(0);
+    bool ok = true;
+    uint32_t tmem = 0;
+    for (int t = 0; t < n; ++t) {
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
         __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        tmem = tmem_base;
+        if (threadIdx.x == 0) {
+            const uint32_t gb = tc::smem_addr(smem_raw) + (uint32_t)((t & 1) * S::STAGE);
+            const uint32_t ib = gb + (uint32_t)S::SMEM_G;
+            for (int j = 0; j < tcw::TAPS; ++j) {
+                const int kk = tap0 + j;
 #pragma unroll
-        for (int k0 = 0; k0 < WG_TILE; k0 += 16) {
-#pragma unroll
-            for (int i = 0; i < WM; ++i) {
-                const int m0 = 16 * (m_base + i);
-                uint32_t af[4] = {ld32(&gT[m0 + g][k0 + 2 * t]), ld32(&gT[m0 + g + 8][k0 + 2 * t]),
-                                  ld32(&gT[m0 + g][k0 + 2 * t + 8]), ld32(&gT[m0 + g + 8][k0 + 2 * t + 8])};
-#pragma unroll
-                for (int j = 0; j < WN; ++j) {
-                    const int n0 = 8 * (n_base + j);
-                    const uint32_t bfr[2] = {ld32(&iT[n0 + g][k0 + 2 * t]), ld32(&iT[n0 + g][k0 + 2 * t + 8])};
-                    mma_bf16(acc[i][j], af, bfr);
+                for (int ks = 0; ks < tcw::P / 16; ++ks) {  // 16 positions = 2 K core matrices per MMA
+                    const uint64_t gd = tc::smem_desc(gb + ks * 2 * tcw::LBO, tcw::LBO, tcw::P * 16);
+                    const uint64_t id = tc::smem_desc(ib + kk * 16 + ks * 2 * tcw::LBO, tcw::LBO, tcw::PR * 16);
+                    const uint32_t acc = (t | ks) ? 1u : 0u;
+                    asm volatile(
+                        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem + (uint32_t)(S::NC * j)),
+                        "l"(S::G_IS_A ? gd : id), "l"(S::G_IS_A ? id : gd), "r"(S::IDESC), "r"(acc));
                 }
             }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                tc::smem_addr(&bar[t & 1])));
         }
+        // buffer (t + 1) & 1 was read by the MMAs of tile t - 1
+        if (t >= 1) ok = wait_bar(t - 1) && ok;
+        if (t + 1 < n) stage(t + 1);
     }
+    if (n > 0) ok = wait_bar(n - 1) && ok;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    // epilogue: lanes 0-15 of warp w hold M-side channel m = 16 w + lane
+    if (n > 0) {
+        tmem = tmem_base;
+        const int m = 16 * warp + lane;
+        for (int j = 0; j < tcw::TAPS; ++j)
 #pragma unroll
-    for (int i = 0; i < WM; ++i)
+            for (int q = 0; q < S::NC; q += 16) {
+                float v[16];
+                tc::ld_x16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(S::NC * j + q), v);
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                if (lane < 16) {
 #pragma unroll
-        for (int j = 0; j < WN; ++j)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int co = 16 * (m_base + i) + g + (q >= 2 ? 8 : 0);
-                const int ci = 8 * (n_base + j) + 2 * t + (q & 1);
-                atomicAdd(&gW[((size_t)co * KW + kk) * CIN + ci], acc[i][j][q]);
+                    for (int e = 0; e < 16; ++e) {
+                        const int nn = q + e;
+                        const int co = S::G_IS_A ? m : nn, ci = S::G_IS_A ? nn : m;
+                        atomicAdd(gW + ((size_t)co * KW + tap0 + j) * CIN + ci, ok ? v[e] : __int_as_float(0x7fc00000));
+                    }
+                }
             }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        tmem = tmem_base;
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(S::TMEM_COLS));
+    }
 }
 
 // bias gradient: gb[co] += sum_p g[p][co].  Each lane sums one channel pair
@@ -432,8 +508,14 @@ cudaError_t conv_fwd(const bf16* in, const bf16* W, const float* bias, void* out
 
 template <int CIN, int COUT>
 cudaError_t conv_wgrad(const bf16* g, const bf16* in, float* gW, int L, int B, cudaStream_t s) {
+    using S = tcw::Shape<COUT, CIN>;
+    static_assert(KW % tcw::TAPS == 0, "taps per CTA");
     const int chunk = 2048;
-    conv_wgrad_kernel<CIN, COUT><<<dim3(KW, (L + chunk - 1) / chunk, B), 128, 0, s>>>(g, in, gW, L, chunk);
+    cudaError_t e = cudaFuncSetAttribute(conv_wgrad_tc_kernel<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)S::SMEM);
+    if (e != cudaSuccess) return e;
+    conv_wgrad_tc_kernel<CIN, COUT><<<dim3(KW / tcw::TAPS, (L + chunk - 1) / chunk, B), 128, S::SMEM, s>>>(g, in, gW, L,
+                                                                                                          chunk);
     count_launch();
     return cudaGetLastError();
 }
