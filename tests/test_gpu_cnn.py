@@ -1,5 +1,6 @@
-"""Correction CNN on the GPU (mma.sync BF16 implicit GEMMs): outputs, loss and
-gradients against the numpy restatement with the same BF16 rounding points
+"""Correction CNN on the GPU (tcgen05 BF16 implicit GEMMs with tensor-memory
+accumulators): outputs, loss and gradients against the numpy restatement
+with the same BF16 rounding points
 (oracle/cnn_ref.py), and training on a structured distortion.  BF16 weights
 and activations: 1e-3 relative on outputs and loss, 1e-2 on gradients."""
 import numpy as np
