@@ -150,12 +150,14 @@ def test_bright_soliton_kat(ctx, oracle_cpu):
     assert rel_l2(got, exact) < 1e-4
 
 
-def test_dispersion_only_closed_form_full_size(ctx):
-    """Linear propagation at N = 2^19 (the WDM configuration's length):
-    A_hat(L) = A_hat(0) exp(i beta2/2 L w^2) exactly (ssfm.cpp:142-150 sign)."""
-    n = 1 << 19
+@pytest.mark.parametrize("lg", [19, 20])
+def test_dispersion_only_closed_form_full_size(ctx, lg):
+    """Linear propagation at N = 2^19 (the WDM configuration's length) and at
+    the largest supported length 2^20: A_hat(L) = A_hat(0) exp(i beta2/2 L w^2)
+    exactly (ssfm.cpp:142-150 sign)."""
+    n = 1 << lg
     dt = 1 / 512e9
-    rng = np.random.default_rng(19)
+    rng = np.random.default_rng(lg)
     x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) * 0.01
     L = 80e3
     f = make_field(x, dt, ctx=ctx)
@@ -193,3 +195,33 @@ def test_forward_then_dbp_round_trip_full_size(ctx):
     fg.forward_propagation(f, fib, s, fg.Amplifier(G), spans=3)
     fg.backward_propagation(f, fib, s, G, spans=3)
     assert rel_l2(f.numpy()[:, 0], x) < 2e-5
+
+
+@pytest.mark.parametrize("single_cta", [False, True])
+def test_zero_and_mixed_power_realizations(ctx, oracle_cpu, single_cta):
+    """A realization with no power takes the step bound (peak 0 => the
+    maximum step: 80 steps of 1 km for 80 km) and stays zero, next to a
+    powered one in the same batch that follows the FP64 oracle
+    (ssfm.cpp:136-140; both passes and the single-CTA kernel)."""
+    n, dt = 1 << 12, 1 / 256e9
+    rng = np.random.default_rng(12)
+    x = np.zeros((2, 1, n), np.complex128)
+    x[1, 0] = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) * 0.03
+    x = x.astype(np.complex64).astype(np.complex128)
+    f = fg.Field(fg.Domain(1, n, dt, 193.1e12), data=x, batch=2, ctx=ctx)
+    s = fg.SSFM(fg.Fiber(ALPHA, BETA2, GAMMA, 80e3))
+    s.set_grid(fg.SSFM.ADAPTIVE)
+    s.set_maximum_phase_shift(0.005)
+    s.set_maximum_step_size(1000.0)
+    if single_cta:
+        fg.set_fft_split(n, fg.SPLIT_SINGLE_CTA, ctx=ctx)
+    try:
+        steps = s.run(f)
+    finally:
+        fg.set_fft_split(n, 0, ctx=ctx)
+    out = f.numpy()
+    assert int(steps[0]) == 80 and np.all(out[0] == 0)
+    want, wsteps = oracle_cpu.ssfm_run(x[1, 0], dt, oracle_cpu.Fiber(ALPHA, BETA2, GAMMA, 80e3, 1.55e-6, 1.0),
+                                       oracle_cpu.ADAPTIVE, 1, 0.005, 1000.0)
+    assert int(steps[1]) == wsteps and wsteps > 80
+    assert rel_l2(out[1, 0], want) < 1e-5
