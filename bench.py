@@ -695,6 +695,10 @@ def run_ncu_case(args):
     ldbp  learned-DBP forward + backward, 20 spans x 2 steps, 63/255 taps,
           8 x 2^16 samples;
     cnn   correction-CNN forward + backward, 8 x 2^15 symbols;
+    dsp   transmitter / receiver DSP chain on 4 x 2^17 16QAM symbols at 8
+          samples/symbol (2^20 samples): map, RRC shaping, channel selection,
+          decimation, matched filter, phase search, decisions, certainty,
+          error counts, Q;
     block single-CTA split-step kernel, 304 realizations of N = 2^14 (2 CTAs
           per SM of work, 40 MB), UNIFORM 10 steps in one launch;
     fit   SINO normal equations (features, z-scores, FP64-accumulated Gram),
@@ -752,6 +756,21 @@ def run_ncu_case(args):
         f = fg.Field(fg.Domain(1, n, DT, F0), data=x.astype(np.complex64), batch=B, ctx=ctx)
         fg.set_fft_split(n, fg.SPLIT_SINGLE_CTA, ctx=ctx)
         fg.SSFM(fib, 10).run(f)
+    elif kind == "dsp":
+        ns, osf, B = 2 ** 17, 8, 4
+        codes = rng.integers(0, 16, (B, 1, ns))
+        sym = dsp.qam16_map(codes, fg.Domain(1, ns, 1 / 32e9, F0), batch=B, ctx=ctx)
+        sig = dsp.rrc_shaping(sym, osf, 0.1)
+        sel = dsp.wdm_select(sig, 0, 50e9)
+        dec = dsp.decimate(sel, osf // 2)
+        y = dsp.rrc_sampling(sig, osf, 0.1)
+        y = dsp.PhaseShiftEqualizer(720).train_equalize(sym, y)
+        dsp.hard_decision_16qam(y)
+        dsp.soft_decision_16qam(y, 0.05)
+        dsp.certainty_decision(y, float(dsp.find_certainty(sym, y)[0]))
+        dsp.error_counts(sym, y, 100)
+        dsp.q2_factor(sym, y, 100)
+        del dec
     elif kind == "fit":
         from focss_gb300 import sino
         ns = 2 ** 17
@@ -780,7 +799,7 @@ def run_ncu_case(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ncu-case", nargs="?", const="ssfm", default=None,
-                    help="small fixed case for ncu captures: ssfm (default), ppe, ldbp, cnn, block, fit, wdmppe")
+                    help="small fixed case for ncu captures: ssfm (default), ppe, ldbp, cnn, dsp, block, fit, wdmppe")
     ap.add_argument("--ncu-batch", type=int, default=40)
     ap.add_argument("--split", type=int, default=0, help="ncu case: log2 N1 of the FFT split (0: balanced)")
     ap.add_argument("--gpus", type=int, default=1)
