@@ -17,14 +17,11 @@ int block_split(int N) {
 namespace {
 template <int N1, int N2>
 cudaError_t launch_block_t(const PassArgs& a, int batch, int cap, cudaStream_t s) {
-    static bool attr = false;
     const size_t smem = BlockShape<N1, N2>::SMEM;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute((const void*)block_kernel<N1, N2>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    // set on every launch: the attribute is per device, and the call is cheap
+    cudaError_t e = cudaFuncSetAttribute((const void*)block_kernel<N1, N2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
     block_kernel<N1, N2><<<batch, kBlockThreads, smem, s>>>(a, cap);
     count_launch();
     return cudaGetLastError();
