@@ -1,6 +1,7 @@
 // ssfm_block.cu -- single-CTA split-step runs for N <= 2^14 (block_kernel in
 // ssfm_kernels.cuh): one CTA per realization, the field in shared memory for
-// the whole run.  Splits: 2^12 = 64 x 64, 2^13 = 64 x 128, 2^14 = 128 x 128.
+// the whole run.  Splits: 2^12 = 64 x 64, 2^13 = 128 x 64 (112 KB: two CTAs
+// per SM), 2^14 = 128 x 128.
 #include "ssfm_kernels.cuh"
 
 namespace fg {
@@ -8,7 +9,7 @@ namespace fg {
 int block_split(int N) {
     switch (N) {
         case 1 << 12: return 6;
-        case 1 << 13: return 6;
+        case 1 << 13: return 7;
         case 1 << 14: return 7;
         default: return 0;
     }
@@ -38,7 +39,7 @@ cudaError_t launch_block(const Plan& p, PassArgs a, int batch, int cap, cudaStre
     a.batch = batch;
     switch (p.N) {
         case 1 << 12: return launch_block_t<64, 64>(a, batch, cap, s);
-        case 1 << 13: return launch_block_t<64, 128>(a, batch, cap, s);
+        case 1 << 13: return launch_block_t<128, 64>(a, batch, cap, s);
         case 1 << 14: return launch_block_t<128, 128>(a, batch, cap, s);
         default: return cudaErrorInvalidValue;
     }

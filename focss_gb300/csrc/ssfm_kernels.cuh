@@ -413,7 +413,8 @@ struct BlockShape {
 };
 
 template <int N1, int N2>
-__global__ void __launch_bounds__(kBlockThreads, 1) block_kernel(const PassArgs a, int cap) {
+__global__ void __launch_bounds__(kBlockThreads, BlockShape<N1, N2>::SMEM <= 113 * 1024 ? 2 : 1)
+    block_kernel(const PassArgs a, int cap) {
     using S = BlockShape<N1, N2>;
     constexpr int C = S::C, G = S::G, RPI = S::RPI;
     constexpr int Pc = ColFFT<N1>::P, Qc = ColFFT<N1>::Q, Pr = PQ<N2>::P;

@@ -19,7 +19,7 @@ pytestmark = pytest.mark.gpu
 
 G = 10 ** (0.2 * 80 / 10)
 NF = 10 ** 0.5
-SPLIT = {1 << 12: 6, 1 << 13: 6, 1 << 14: 7}
+SPLIT = {1 << 12: 6, 1 << 13: 7, 1 << 14: 7}
 
 
 def _field(ctx, n, batch, seed, power_dbm=4.0, modes=1, dt=1 / 256e9):
