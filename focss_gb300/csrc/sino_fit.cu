@@ -18,7 +18,9 @@
 // The Gram product is a tiled complex kernel on the CUDA
 // cores (64 x 64 output tiles, 4 x 4 complex outputs per thread, the samples
 // split over the grid's z dimension) reading the FP32 features, summing runs
-// of 16 samples in FP32 and accumulating those sums in FP64.
+// of 16 samples in FP32 and accumulating those sums in FP64.  The residual
+// entry points rebuild the same design and return Z^H (y - Z x) in FP64, so
+// the caller can refine its solve to the FP64 normal-equations solution.
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
