@@ -397,6 +397,8 @@ def run_ours(args):
         line["ppe"] = ppe_section(fg, ctx, stream)
     if not args.no_wdm_ppe:
         line["wdm_ppe"] = wdm_ppe_section(fg, ctx, stream)
+    if args.dbp_sweep:
+        line["dbp_sweep"] = dbp_sweep_section(fg, ctx)
     if world == 1 and rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         n_steps = CPU_BASELINE_STEPS
@@ -636,6 +638,48 @@ def ppe_section(fg, ctx, stream):
     return out
 
 
+DBP_SWEEP = dict(
+    workload="learned_dbp_sweep_wdm5_centre_2^20sym_-2..+4dBm",
+    powers_dbm=[-2, -1, 0, 1, 2, 3, 4], realizations=32, symbols_per_realization=2 ** 15, steps_per_span=4,
+    taps=63, mf_taps=255, iters=300, lr=3e-4, cnn_iters=200, cnn_lr=1e-3,
+)
+
+
+def dbp_sweep_section(fg, ctx):
+    """Learned DBP at 4 steps/span against plain DBP at 1 / 4 / 100 steps/span
+    over the launch-power sweep of the WDM link (centre channel, 2 samples/
+    symbol): per power an independent training set and test set of 32
+    realizations x 2^15 symbols (2^20 symbols each), the learned DBP trained
+    on the training set (300 Adam steps), then the correction CNN."""
+    from focss_gb300 import links
+    c = DBP_SWEEP
+    link = links.Link(spans=W["spans"], span_m=W["span_m"], noise_figure_db=W["noise_figure_db"],
+                      max_phase=W["max_phase_shift"], max_step=W["max_step_m"], channels=W["channels"],
+                      spacing=W["spacing_hz"], osf=W["samples_per_symbol"], roll_off=W["roll_off"])
+    B, ns = c["realizations"], c["symbols_per_realization"]
+    rows = []
+    for i, p in enumerate(c["powers_dbm"]):
+        a, ta = links.wdm_transmitter(link, ns, B, p, seed=1000 + 2 * i, ctx=ctx)
+        b, tb = links.wdm_transmitter(link, ns, B, p, seed=1001 + 2 * i, ctx=ctx)
+        links.propagate(link, a, seed=500 + 2 * i)
+        links.propagate(link, b, seed=501 + 2 * i)
+        ra, rb = links.centre_channel(link, a), links.centre_channel(link, b)
+        del a, b
+        row = {"power_dbm": p}
+        for k in (1, 4, 100):
+            q, ms = links.plain_dbp_q(link, rb, tb, k)
+            row["plain_%d" % k] = {"q_db": float(np.mean(q)), "ms": ms}
+        r = links.learned_dbp(link, ra, ta, rb, tb, steps_per_span=c["steps_per_span"], taps=c["taps"],
+                              mf_taps=c["mf_taps"], iters=c["iters"], lr=c["lr"], cnn_iters=c["cnn_iters"],
+                              cnn_lr=c["cnn_lr"])
+        row["learned_%d" % c["steps_per_span"]] = {"q_db": float(np.mean(r["q_learned"])), "ms": r["ms_learned"],
+                                                   "train_s": r["train_s"]}
+        row["learned_%d_cnn" % c["steps_per_span"]] = {"q_db": float(np.mean(r["q_learned_cnn"])),
+                                                       "ms": r["ms_learned_cnn"], "train_s": r["cnn_train_s"]}
+        rows.append(row)
+    return {"config": c, "powers": rows}
+
+
 WDM_PPE = dict(
     workload="wdm_ppe_3ch_dualpol_16qam_32GBd_2^15sym_20x100km_2dBm",
     channels=3, polarizations=2, symbols=2 ** 15, samples_per_symbol=16, spacing_hz=37.5e9, power_index=16,
@@ -812,6 +856,8 @@ def main():
     ap.add_argument("--no-ppe", action="store_true", help="skip the perturbation-equalizer section")
     ap.add_argument("--no-wdm-ppe", action="store_true",
                     help="skip the dual-polarization WDM dataset and WdmPPE scoring section")
+    ap.add_argument("--dbp-sweep", action="store_true",
+                    help="add the learned-vs-plain DBP launch-power sweep (-2..+4 dBm, 2^20 symbols per set; minutes)")
     ap.add_argument("--host-loop", action="store_true",
                     help="drive the spans from the host (one SSFM run + EDFA per span) instead of one graph")
     args = ap.parse_args()
