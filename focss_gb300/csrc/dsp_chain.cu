@@ -39,20 +39,25 @@ inline int grid_for(size_t n, int threads) {
 __constant__ double c_gray_re[16] = {-3, -1, 3, 1, -3, -1, 3, 1, -3, -1, 3, 1, -3, -1, 3, 1};
 __constant__ double c_gray_im[16] = {-3, -3, -3, -3, -1, -1, -1, -1, 3, 3, 3, 3, 1, 1, 1, 1};
 
-__device__ __forceinline__ double inv_sqrt10() { return 0.31622776601683794; }
-
 // demodulate_16qam (modulation.cpp:98-110): argmin over the 16 points, ties
-// to the lowest code, FP64 distances exactly as the reference forms them.
+// to the lowest code, FP64 distances.  The 16 points are the products of 4
+// in-phase and 4 quadrature levels, so the 4 + 4 coordinate differences (the
+// same values the point-by-point form computes) and the 4 quadrature squares
+// are formed once and each distance is one fused multiply-add.
 __device__ __forceinline__ unsigned demod16(double re, double im) {
     const double s = 1.0 / sqrt(10.0);
+    double dr[4], qi[4];
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+        dr[l] = re - c_gray_re[l] * s;            // levels of codes l, l + 4, l + 8, l + 12
+        const double di = im - c_gray_im[4 * l] * s;  // level of codes 4l .. 4l + 3
+        qi[l] = di * di;
+    }
     unsigned arg = 0;
-    double dr = re - c_gray_re[0] * s, di = im - c_gray_im[0] * s;
-    double mn = dr * dr + di * di;
+    double mn = fma(dr[0], dr[0], qi[0]);
 #pragma unroll
     for (unsigned code = 1; code < 16; ++code) {
-        dr = re - c_gray_re[code] * s;
-        di = im - c_gray_im[code] * s;
-        const double d = dr * dr + di * di;
+        const double d = fma(dr[code & 3], dr[code & 3], qi[code >> 2]);
         if (mn > d) {
             mn = d;
             arg = code;
