@@ -749,7 +749,11 @@ def run_ncu_case(args):
           R = 32 (577 features) on 2^17 symbols x 2 modes;
     wdmppe  WdmPPE (c, d) = (30, 3): equalizer on 16 x 6-row realizations of
           2^18 symbols (201 MB in, 67 MB out), then the fit's features on one
-          6-row realization of 2^16 symbols."""
+          6-row realization of 2^16 symbols;
+    aux   the remaining kernels: field scale / power / natural-order FFT on
+          40 x 2^19, a UNIFORM span loop graph with EDFA, the allocation-free
+          entry point, WDM mux, RRC taps, hard-decision codes, one learned-DBP
+          and one CNN training step (with Adam), SINO and WdmPPE fits."""
     import focss_gb300 as fg
     from focss_gb300 import dsp
     ctx = fg.Context(0)
@@ -833,6 +837,59 @@ def run_ncu_case(args):
             ppe.equalize(tx, tx)
         t1 = dsp.qam16_map(codes[:1, :, :2 ** 16], fg.Domain(6, 2 ** 16, 1 / 32e9, F0), ctx=ctx)
         fg.WdmPPE(c, d).train(t1, t1)
+    elif kind == "aux":
+        import ctypes as C
+        from focss_gb300 import sino
+        from focss_gb300._lib import check
+        from focss_gb300.cnn import CorrectionCNN, he_init
+        from focss_gb300.ldbp import LearnedDBP, rrc_response
+        # field utilities on 40 realizations of N = 2^19 (168 MB)
+        B = 40
+        x = (synth_wdm() * np.sqrt(1e-3)).astype(np.complex64)
+        f = fg.Field(fg.Domain(1, N, DT, F0), data=np.broadcast_to(x, (B, 1, N)), batch=B, ctx=ctx)
+        f *= 0.5
+        f.power_stats()
+        f.fft_inplace()
+        f.ifft_inplace()
+        # span loop on a UNIFORM grid (no conditional node, so its kernel nodes can be profiled)
+        fg.span_loop([f], fib, fg.SSFM(fib, 2), 2, amplifier=fg.Amplifier(10 ** 1.6, 10 ** 0.5, seed=1),
+                     after=0)
+        # allocation-free entry point, 8 x 2^17 samples, 4 UNIFORM steps
+        n17 = 1 << 17
+        g = fg.Field(fg.Domain(1, n17, DT, F0), data=x[None, None, :n17].repeat(8, 0), batch=8, ctx=ctx)
+        steps = np.zeros(8, np.int32)
+        fb, op = fib.c(), fg.SSFM(fib, 4).opts()
+        check(fg.lib().focss_ssfm_run_noalloc(ctx.stream, g.device_ptr(), n17, 8, DT, C.byref(fb), C.byref(op),
+                                              1.0, steps.ctypes.data_as(C.c_void_p)), ctx.h)
+        # WDM multiplexer (5 channels of 2^19 samples), RRC taps, hard-decision codes on 16 x 2^18 symbols
+        dsp.wdm_mux(f.slice(0, 5), 50e9)
+        dsp.rrc_pulse(2 ** 12, 8, 0.1, ctx=ctx)
+        y = dsp.qam16_map(rng.integers(0, 16, (16, 1, 2 ** 18)), fg.Domain(1, 2 ** 18, 1 / 32e9, F0), batch=16,
+                          ctx=ctx)
+        dsp.hd_sequence_16qam(y)
+        # learned DBP training step (8 x 2^16 samples, 20 spans x 2 steps)
+        n2, dt2 = 2 ** 16, 1 / 64e9
+        rx = fg.Field(fg.Domain(1, n2, dt2, F0), data=(rng.standard_normal((8, 1, n2)) + 0j) * 1e-2, batch=8,
+                      ctx=ctx)
+        tx = dsp.qam16_map(rng.integers(0, 16, (8, 1, n2 // 2)), fg.Domain(1, n2 // 2, 1 / 32e9, F0), batch=8,
+                           ctx=ctx)
+        model = LearnedDBP(20, 2, 63, 255, n2, 8, 10 ** -0.8, ctx=ctx)
+        model.init_from_dbp(alpha, beta2, gamma, 1.0, W["span_m"], dt2, rrc_response(n2 // 2, 2, 0.1, ctx=ctx))
+        model.loss_grad(rx, tx)
+        model.adam_step(1e-3)
+        # correction-CNN training step (8 x 2^15 symbols)
+        y15 = dsp.qam16_map(rng.integers(0, 16, (8, 1, 2 ** 15)), fg.Domain(1, 2 ** 15, 1 / 32e9, F0), batch=8,
+                            ctx=ctx)
+        net = CorrectionCNN(2 ** 15, 8, 1.0, ctx=ctx)
+        net.set_params(he_init(rng))
+        net.loss_grad(y15, y15)
+        net.adam_step(1e-3)
+        # SINO / WdmPPE fits: responses, z-scores, residual refinement (design apply / adjoint)
+        ns = 2 ** 17
+        t2 = dsp.qam16_map(rng.integers(0, 16, (1, 2, ns)), fg.Domain(2, ns, 1 / 32e9, F0), ctx=ctx)
+        sino.SINO(16).train(t2, t2.copy(), solver="gpu")
+        t6 = dsp.qam16_map(rng.integers(0, 16, (1, 6, 2 ** 16)), fg.Domain(6, 2 ** 16, 1 / 32e9, F0), ctx=ctx)
+        fg.WdmPPE(8, 2).train(t6, t6)
     else:
         raise SystemExit("unknown ncu case %r" % kind)
     ctx.sync()

@@ -260,6 +260,9 @@ FOCSS_API focss_status focss_field_create(focss_ctx* c, const focss_domain* d, i
     // src/focss/field.cpp:25 asserts modes > 0, samples > 0, time_step > 0.
     if (d->modes <= 0 || d->samples <= 0 || !(d->time_step > 0) || batch <= 0)
         return fg::set_error(c, FOCSS_ERR_INVALID_ARG, "field_create: modes, samples, time_step, batch must be > 0");
+    // the kernels put realizations (or realization x mode rows) on a grid's y dimension
+    if ((long long)batch * d->modes > 65535)
+        return fg::set_error(c, FOCSS_ERR_INVALID_ARG, "field_create: batch x modes must be <= 65535");
     focss_field* f = new (std::nothrow) focss_field();
     if (!f) return FOCSS_ERR_OOM;
     f->ctx = c;

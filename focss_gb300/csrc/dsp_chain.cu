@@ -29,6 +29,15 @@ inline int grid_for(size_t n, int threads) {
     return (int)(g ? g : 1);
 }
 
+// Per-realization grid (x: samples of one realization, y: realization) with
+// about 8 CTAs of 256 threads per SM over the whole launch (each CTA forms
+// its realization's FP64 scale once, so fewer, longer CTAs amortize it).
+inline dim3 grid_per_realization(size_t per, int batch) {
+    const size_t by_work = (per + 255) / 256, by_fill = ((size_t)152 * 8 + batch - 1) / (size_t)batch;
+    size_t gx = by_work < by_fill ? by_work : by_fill;
+    return dim3((unsigned)(gx ? gx : 1), (unsigned)batch);
+}
+
 #define FG_LAUNCH(...)       \
     do {                     \
         __VA_ARGS__;         \
@@ -65,6 +74,39 @@ __device__ __forceinline__ unsigned demod16(double re, double im) {
     }
     return arg;
 }
+
+// The same decision from FP32 coordinates, where that is provably the same:
+// the nearest point of the square grid is the nearest level on each axis,
+// and a coordinate farther than kNear (1e-5 (1 + |v|)) from every level
+// boundary (0, +-2/sqrt 10) has that level under the FP64 argmin above as
+// well -- the FP32 coordinate is within 2e-7 |v| of the FP64 one, and the
+// FP64 distances of the two nearest points then differ by ~1e-5, far above
+// their rounding.  `near` is set when a coordinate is closer than that (or
+// NaN); the caller then decides with demod16 on its FP64 coordinates, so
+// the codes are those of the FP64 argmin for every input.
+__device__ __forceinline__ bool near_value(float v, float t) {
+    return !(fabsf(v - t) > 1e-5f * (1.0f + fabsf(v)));
+}
+__device__ __forceinline__ unsigned level4(float v, bool& near) {
+    constexpr float kB = 0.632455532f;  // 2/sqrt(10)
+    const float a = fabsf(v);
+    near = near || near_value(a, 0.0f) || near_value(a, kB);
+    // levels -3, -1, 1, 3 (/sqrt 10) are table indices 0, 1, 3, 2 on both axes
+    return v < 0.0f ? (v < -kB ? 0u : 1u) : (v < kB ? 3u : 2u);
+}
+__device__ __forceinline__ unsigned demod16_f32(float re, float im, bool& near) {
+    near = false;
+    const unsigned lr = level4(re, near);
+    const unsigned li = level4(im, near);
+    return lr | (li << 2);
+}
+
+// FP64 fallbacks as calls: kept out of line so that the compiler does not
+// if-convert them into every sample's path (GB300's FP64 pipe is narrow).
+__device__ __noinline__ unsigned demod16_div(float x, float y, double sp) {
+    return demod16((double)x / sp, (double)y / sp);
+}
+__device__ __noinline__ unsigned demod16_mul(float x, float y, double sc) { return demod16(sc * x, sc * y); }
 
 __global__ void qam_map_kernel(const int32_t* __restrict__ codes, float2* __restrict__ out, size_t n) {
     const double s = 1.0 / sqrt(10.0);
@@ -205,37 +247,95 @@ __global__ void power_sum_kernel(const float2* __restrict__ d, size_t per, doubl
 
 // hard_decision_16qam (modulation.cpp:112-120): power = avg/modes,
 // out = sqrt(power) * gray[demod(in / sqrt(power))].
+// Grid (samples, realization): the realization's scale is formed once per thread.
 __global__ void hard_decision_kernel(const float2* __restrict__ in, float2* __restrict__ out, int modes, int samples,
-                                     size_t per, int batch, const double* __restrict__ psum) {
+                                     size_t per, const double* __restrict__ psum) {
     const double s10 = 1.0 / sqrt(10.0);
-    const size_t n = per * batch;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const int b = (int)(i / per);
-        const double power = psum[b] / samples / modes;
-        const double sp = sqrt(power);
-        const unsigned c = demod16((double)in[i].x / sp, (double)in[i].y / sp);
-        out[i] = make_float2((float)(sp * (c_gray_re[c] * s10)), (float)(sp * (c_gray_im[c] * s10)));
+    const int b = blockIdx.y;
+    const double power = psum[b] / samples / modes;
+    const double sp = sqrt(power);
+    in += (size_t)b * per;
+    out += (size_t)b * per;
+    // the 16 outputs, formed once per CTA (a per-sample lookup with divergent
+    // codes would serialize in the constant cache)
+    __shared__ float2 s_out[16];
+    if (threadIdx.x < 16)
+        s_out[threadIdx.x] = make_float2((float)(sp * (c_gray_re[threadIdx.x] * s10)),
+                                         (float)(sp * (c_gray_im[threadIdx.x] * s10)));
+    __syncthreads();
+    const float inv = (float)(1.0 / sp);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < per; i += (size_t)gridDim.x * blockDim.x) {
+        const float2 z = in[i];
+        bool near;
+        unsigned c = demod16_f32(z.x * inv, z.y * inv, near);
+        if (near) c = demod16_div(z.x, z.y, sp);
+        out[i] = s_out[c];
     }
+}
+
+// The FP64 forms of one soft decision (modulation.cpp:122-146) and one
+// certainty decision (src/tasks/wdm_scoring.cpp:128-144), out of line.
+__device__ __noinline__ float2 soft_decision_fp64(float2 z, double sp, double thr) {
+    const double s10 = 1.0 / sqrt(10.0), pivot = 2.0 / sqrt(10.0);
+    const double re = (double)z.x / sp, im = (double)z.y / sp;
+    const unsigned c = demod16(re, im);
+    double gr = c_gray_re[c] * s10, gi = c_gray_im[c] * s10;
+    if (fabs(re) < thr || fabs(re - pivot) < thr || fabs(re + pivot) < thr) gr = re;
+    if (fabs(im) < thr || fabs(im - pivot) < thr || fabs(im + pivot) < thr) gi = im;
+    return make_float2((float)(sp * gr), (float)(sp * gi));
+}
+__device__ __noinline__ float2 certainty_decision_fp64(float2 z, double amp, double thr) {
+    const double s10 = 1.0 / sqrt(10.0);
+    double re = (double)z.x / amp, im = (double)z.y / amp;
+    const unsigned c = demod16(re, im);
+    const double gr = c_gray_re[c] * s10, gi = c_gray_im[c] * s10;
+    if (hypot(gr - re, gi - im) < thr) {
+        re = gr;
+        im = gi;
+    }
+    return make_float2((float)(amp * re), (float)(amp * im));
 }
 
 // soft_decision_16qam (modulation.cpp:122-146): per quadrature the hard
 // decision, unless the normalized received value lies within
 // sqrt(10)*uncertainty of a decision boundary (0, +-2/sqrt(10)); then it is kept.
 __global__ void soft_decision_kernel(const float2* __restrict__ in, float2* __restrict__ out, int modes, int samples,
-                                     size_t per, int batch, const double* __restrict__ psum, double uncertainty) {
+                                     size_t per, const double* __restrict__ psum, double uncertainty) {
     const double s10 = 1.0 / sqrt(10.0);
     const double pivot = 2.0 / sqrt(10.0), thr = sqrt(10.0) * uncertainty;
-    const size_t n = per * batch;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const int b = (int)(i / per);
-        const double power = psum[b] / samples / modes;
-        const double sp = sqrt(power);
-        const double re = (double)in[i].x / sp, im = (double)in[i].y / sp;
-        const unsigned c = demod16(re, im);
-        double gr = c_gray_re[c] * s10, gi = c_gray_im[c] * s10;
-        if (fabs(re) < thr || fabs(re - pivot) < thr || fabs(re + pivot) < thr) gr = re;
-        if (fabs(im) < thr || fabs(im - pivot) < thr || fabs(im + pivot) < thr) gi = im;
-        out[i] = make_float2((float)(sp * gr), (float)(sp * gi));
+    const int b = blockIdx.y;
+    const double power = psum[b] / samples / modes;
+    const double sp = sqrt(power);
+    in += (size_t)b * per;
+    out += (size_t)b * per;
+    // FP32 first, as in demod16_f32: a quadrature is kept when its distance
+    // to 0 or +-pivot is below thr; a distance within 1e-5 (1 + |v|) of thr
+    // goes to the FP64 form.  A kept value is written as the input itself,
+    // which is what float(sp * (x / sp)) rounds to for every FP32 x (the FP64
+    // round trip moves x by < 2^-51 |x|, below half an FP32 unit).
+    __shared__ float2 s_out[16];  // decided outputs, as in hard_decision_kernel
+    if (threadIdx.x < 16)
+        s_out[threadIdx.x] = make_float2((float)(sp * (c_gray_re[threadIdx.x] * s10)),
+                                         (float)(sp * (c_gray_im[threadIdx.x] * s10)));
+    __syncthreads();
+    const float inv = (float)(1.0 / sp), thr32 = (float)thr, pv32 = (float)pivot;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < per; i += (size_t)gridDim.x * blockDim.x) {
+        const float2 z = in[i];
+        const float r32 = z.x * inv, i32 = z.y * inv;
+        bool near;
+        unsigned c = demod16_f32(r32, i32, near);
+        const float dr0 = fabsf(r32), dr1 = fabsf(r32 - pv32), dr2 = fabsf(r32 + pv32);
+        const float di0 = fabsf(i32), di1 = fabsf(i32 - pv32), di2 = fabsf(i32 + pv32);
+        near = near || near_value(dr0, thr32) || near_value(dr1, thr32) || near_value(dr2, thr32) ||
+               near_value(di0, thr32) || near_value(di1, thr32) || near_value(di2, thr32);
+        if (!near) {
+            const bool keep_r = dr0 < thr32 || dr1 < thr32 || dr2 < thr32;
+            const bool keep_i = di0 < thr32 || di1 < thr32 || di2 < thr32;
+            const float2 d = s_out[c];
+            out[i] = make_float2(keep_r ? z.x : d.x, keep_i ? z.y : d.y);
+            continue;
+        }
+        out[i] = soft_decision_fp64(z, sp, thr);
     }
 }
 
@@ -248,13 +348,18 @@ __global__ void certainty_kernel(const float2* __restrict__ tx, const float2* __
                                  const double* __restrict__ psum_tx, unsigned long long* __restrict__ dmin) {
     const int b = blockIdx.y;
     const double scale = sqrt((double)per) / sqrt(psum_tx[b]);
+    const float sc32 = (float)scale;
     const double s10 = 1.0 / sqrt(10.0);
     double best = __longlong_as_double(0x7FF0000000000000LL);
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < per; i += (size_t)gridDim.x * blockDim.x) {
         const size_t k = (size_t)b * per + i;
-        const double rr = rx[k].x, ri = rx[k].y;
-        const unsigned tc = demod16(scale * tx[k].x, scale * tx[k].y);
-        const unsigned rc = demod16(scale * rr, scale * ri);
+        const float2 t = tx[k], r = rx[k];
+        const double rr = r.x, ri = r.y;
+        bool near;
+        unsigned tc = demod16_f32(t.x * sc32, t.y * sc32, near);
+        if (near) tc = demod16_mul(t.x, t.y, scale);
+        unsigned rc = demod16_f32(r.x * sc32, r.y * sc32, near);
+        if (near) rc = demod16_mul(r.x, r.y, scale);
         if (tc ^ rc) best = fmin(best, hypot(c_gray_re[rc] * s10 / scale - rr, c_gray_im[rc] * s10 / scale - ri));
     }
     for (int o = 16; o > 0; o >>= 1) best = fmin(best, __shfl_xor_sync(0xffffffffu, best, o));
@@ -265,32 +370,55 @@ __global__ void certainty_kernel(const float2* __restrict__ tx, const float2* __
 // sd (src/tasks/wdm_scoring.cpp:128-144): at the RMS amplitude amp, a sample
 // snaps to its decided point when closer than certainty / sqrt(5).
 __global__ void certainty_decision_kernel(const float2* __restrict__ in, float2* __restrict__ out, size_t per,
-                                          int batch, const double* __restrict__ psum, double certainty) {
+                                          const double* __restrict__ psum, double certainty) {
     const double s10 = 1.0 / sqrt(10.0);
     const double thr = certainty / sqrt(5.0);
-    const size_t n = per * batch;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const int b = (int)(i / per);
-        const double amp = sqrt(psum[b]) / sqrt((double)per);
-        double re = (double)in[i].x / amp, im = (double)in[i].y / amp;
-        const unsigned c = demod16(re, im);
-        const double gr = c_gray_re[c] * s10, gi = c_gray_im[c] * s10;
-        if (hypot(gr - re, gi - im) < thr) {
-            re = gr;
-            im = gi;
+    const int b = blockIdx.y;
+    const double amp = sqrt(psum[b]) / sqrt((double)per);
+    in += (size_t)b * per;
+    out += (size_t)b * per;
+    // FP32 first (demod16_f32; the distance to the decided point against thr
+    // with the same 1e-5 (1 + d) guard band); a kept sample is written as the
+    // input itself, which float(amp * (x / amp)) rounds to for every FP32 x.
+    __shared__ float2 s_pt[16], s_out[16];  // normalized points (FP32) and snapped outputs
+    if (threadIdx.x < 16) {
+        s_pt[threadIdx.x] = make_float2((float)(c_gray_re[threadIdx.x] * s10), (float)(c_gray_im[threadIdx.x] * s10));
+        s_out[threadIdx.x] = make_float2((float)(amp * (c_gray_re[threadIdx.x] * s10)),
+                                         (float)(amp * (c_gray_im[threadIdx.x] * s10)));
+    }
+    __syncthreads();
+    const float inv = (float)(1.0 / amp), thr32 = (float)thr;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < per; i += (size_t)gridDim.x * blockDim.x) {
+        const float2 z = in[i];
+        const float r32 = z.x * inv, i32 = z.y * inv;
+        bool near;
+        unsigned c = demod16_f32(r32, i32, near);
+        if (!near) {
+            const float2 p = s_pt[c];
+            const float d = hypotf(p.x - r32, p.y - i32);
+            if (!near_value(d, thr32)) {
+                out[i] = d < thr32 ? s_out[c] : z;
+                continue;
+            }
         }
-        out[i] = make_float2((float)(amp * re), (float)(amp * im));
+        out[i] = certainty_decision_fp64(z, amp, thr);
     }
 }
 
 // hd_sequence_16qam (modulation.cpp:148-156): scale = sqrt(modes / average_power).
 __global__ void hd_codes_kernel(const float2* __restrict__ in, int32_t* __restrict__ codes, int modes, int samples,
-                                size_t per, int batch, const double* __restrict__ psum) {
-    const size_t n = per * batch;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const int b = (int)(i / per);
-        const double sc = sqrt(modes / (psum[b] / samples));
-        codes[i] = (int32_t)demod16(sc * in[i].x, sc * in[i].y);
+                                size_t per, const double* __restrict__ psum) {
+    const int b = blockIdx.y;
+    const double sc = sqrt(modes / (psum[b] / samples));
+    in += (size_t)b * per;
+    codes += (size_t)b * per;
+    const float sc32 = (float)sc;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < per; i += (size_t)gridDim.x * blockDim.x) {
+        const float2 z = in[i];
+        bool near;
+        unsigned c = demod16_f32(z.x * sc32, z.y * sc32, near);
+        if (near) c = demod16_mul(z.x, z.y, sc);
+        codes[i] = (int32_t)c;
     }
 }
 
@@ -302,6 +430,7 @@ __global__ void error_count_kernel(const float2* __restrict__ tx, const float2* 
     const int b = blockIdx.y;
     const size_t per = (size_t)modes * samples;
     const double sc = sqrt(modes / (psum_tx[b] / samples));
+    const float sc32 = (float)sc;
     const int span = samples - 2 * cut;
     unsigned long long be = 0, se = 0;
     if (span > 0) {
@@ -310,8 +439,12 @@ __global__ void error_count_kernel(const float2* __restrict__ tx, const float2* 
             const int m = (int)(i / span);
             const int s = cut + (int)(i % span);
             const size_t k = (size_t)b * per + (size_t)m * samples + s;
-            const unsigned tc = demod16(sc * tx[k].x, sc * tx[k].y);
-            const unsigned rc = demod16(sc * rx[k].x, sc * rx[k].y);
+            const float2 t = tx[k], r = rx[k];
+            bool near;
+            unsigned tc = demod16_f32(t.x * sc32, t.y * sc32, near);
+            if (near) tc = demod16_mul(t.x, t.y, sc);
+            unsigned rc = demod16_f32(r.x * sc32, r.y * sc32, near);
+            if (near) rc = demod16_mul(r.x, r.y, sc);
             const int d = __popc(tc ^ rc);
             be += d;
             se += d > 0;
@@ -673,7 +806,7 @@ FOCSS_API focss_status focss_hard_decision(focss_ctx* c, const focss_field* in, 
     if (st == FOCSS_OK) st = fg::power_sums(c, in, c->d_red);
     if (st != FOCSS_OK) return st;
     const size_t per = (size_t)in->modes * in->samples;
-    FG_LAUNCH(fg::hard_decision_kernel<<<fg::grid_for(in->n(), 256), 256, 0, c->stream>>>(in->d, out->d, in->modes, in->samples, per, in->batch, c->d_red));
+    FG_LAUNCH(fg::hard_decision_kernel<<<fg::grid_per_realization(per, in->batch), 256, 0, c->stream>>>(in->d, out->d, in->modes, in->samples, per, c->d_red));
     return fg::cuda_check(c, cudaGetLastError(), "hard_decision");
 }
 
@@ -685,7 +818,7 @@ FOCSS_API focss_status focss_soft_decision(focss_ctx* c, const focss_field* in, 
     if (st == FOCSS_OK) st = fg::power_sums(c, in, c->d_red);
     if (st != FOCSS_OK) return st;
     const size_t per = (size_t)in->modes * in->samples;
-    FG_LAUNCH(fg::soft_decision_kernel<<<fg::grid_for(in->n(), 256), 256, 0, c->stream>>>(in->d, out->d, in->modes, in->samples, per, in->batch, c->d_red, uncertainty));
+    FG_LAUNCH(fg::soft_decision_kernel<<<fg::grid_per_realization(per, in->batch), 256, 0, c->stream>>>(in->d, out->d, in->modes, in->samples, per, c->d_red, uncertainty));
     return fg::cuda_check(c, cudaGetLastError(), "soft_decision");
 }
 
@@ -730,7 +863,7 @@ FOCSS_API focss_status focss_certainty_decision(focss_ctx* c, const focss_field*
     if (st == FOCSS_OK) st = fg::power_sums(c, in, c->d_red);
     if (st != FOCSS_OK) return st;
     const size_t per = (size_t)in->modes * in->samples;
-    FG_LAUNCH(fg::certainty_decision_kernel<<<fg::grid_for(in->n(), 256), 256, 0, c->stream>>>(in->d, out->d, per, in->batch, c->d_red, certainty));
+    FG_LAUNCH(fg::certainty_decision_kernel<<<fg::grid_per_realization(per, in->batch), 256, 0, c->stream>>>(in->d, out->d, per, c->d_red, certainty));
     return fg::cuda_check(c, cudaGetLastError(), "certainty_decision");
 }
 
@@ -742,7 +875,7 @@ FOCSS_API focss_status focss_hd_codes(focss_ctx* c, const focss_field* in, int32
     int32_t* d = (int32_t*)fg::scratch_buffer(c, 1, sizeof(int32_t) * in->n());
     if (!d) return fg::set_error(c, FOCSS_ERR_OOM, "hd_codes scratch");
     const size_t per = (size_t)in->modes * in->samples;
-    FG_LAUNCH(fg::hd_codes_kernel<<<fg::grid_for(in->n(), 256), 256, 0, c->stream>>>(in->d, d, in->modes, in->samples, per, in->batch, c->d_red));
+    FG_LAUNCH(fg::hd_codes_kernel<<<fg::grid_per_realization(per, in->batch), 256, 0, c->stream>>>(in->d, d, in->modes, in->samples, per, c->d_red));
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(codes, d, sizeof(int32_t) * in->n(), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);

@@ -146,47 +146,103 @@ __global__ void wdm_responses_kernel(const float2* __restrict__ rx, int row0, in
     }
 }
 
-// Per column: mean (FP64) and, for features, the standard deviation
-// (normalized by the count); then z-score features and centre the responses.
-__global__ void column_stats_kernel(float2* __restrict__ Z, size_t kp, size_t ns, int nf, double* __restrict__ mean,
-                                   double* __restrict__ sd) {
-    __shared__ double red[64];
+// Per column: mean and, for features, the standard deviation (normalized by
+// the count), in two kernels so that every column is split over many CTAs.
+// column_moments_kernel sums the deviations from the column's first sample K
+// (S1 = sum (z - K), S2 = sum |z - K|^2: shifted sums, so a mean large against
+// the spread does not cancel), runs of 16 samples per thread in FP32 and the
+// runs in FP64; the CTAs of a column (grid.y) meet in FP64 atomics on
+// mom[5 f .. 5 f + 2] (zeroed by the caller), and CTA y = 0 stores K in
+// mom[5 f + 3 .. 5 f + 4].
+constexpr int kMom = 5;
+__global__ void column_moments_kernel(const float2* __restrict__ Z, size_t kp, size_t ns, double* __restrict__ mom) {
+    __shared__ double red[32];
     const int f = blockIdx.x;
-    float2* col = Z + (size_t)f * kp;
-    double sr = 0, si = 0;
-    for (size_t i = threadIdx.x; i < ns; i += blockDim.x) {
-        sr += col[i].x;
-        si += col[i].y;
+    const float2* col = Z + (size_t)f * kp;
+    const float2 K = col[0];
+    const size_t per = (ns + gridDim.y - 1) / gridDim.y;
+    const size_t i0 = per * blockIdx.y, i1 = i0 + per < ns ? i0 + per : ns;
+    double s1r = 0, s1i = 0, s2 = 0;
+    float pr = 0.f, pi = 0.f, p2 = 0.f;
+    int run = 0;
+    // four independent loads per iteration (bytes in flight); a sample past
+    // the range reads as K and adds nothing
+    for (size_t i = i0 + threadIdx.x; i < i1; i += 4 * (size_t)blockDim.x) {
+        float2 z[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const size_t j = i + (size_t)u * blockDim.x;
+            z[u] = j < i1 ? col[j] : K;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const float dr = z[u].x - K.x, di = z[u].y - K.y;
+            pr += dr;
+            pi += di;
+            p2 = fmaf(dr, dr, fmaf(di, di, p2));
+        }
+        if (++run == 4) {  // 16 samples per FP32 run
+            s1r += pr;
+            s1i += pi;
+            s2 += p2;
+            pr = pi = p2 = 0.f;
+            run = 0;
+        }
     }
-    sr = block_sum_d(sr, red);
+    s1r += pr;
+    s1i += pi;
+    s2 += p2;
+    s1r = block_sum_d(s1r, red);
     __syncthreads();
-    si = block_sum_d(si, red);
-    __shared__ double mu[2];
+    s1i = block_sum_d(s1i, red);
+    __syncthreads();
+    s2 = block_sum_d(s2, red);
     if (threadIdx.x == 0) {
-        mu[0] = sr / (double)ns;
-        mu[1] = si / (double)ns;
+        double* m = mom + kMom * (size_t)f;
+        atomicAdd(m, s1r);
+        atomicAdd(m + 1, s1i);
+        atomicAdd(m + 2, s2);
+        if (blockIdx.y == 0) {
+            m[3] = K.x;
+            m[4] = K.y;
+        }
     }
-    __syncthreads();
-    const double mr = mu[0], mi = mu[1];
-    double ss = 0;
-    for (size_t i = threadIdx.x; i < ns; i += blockDim.x) {
-        const double dr = col[i].x - mr, di = col[i].y - mi;
-        ss += dr * dr + di * di;
-    }
-    __syncthreads();
-    ss = block_sum_d(ss, red);
-    __shared__ double scale;
-    if (threadIdx.x == 0) {
+}
+
+// z-score the features and centre the responses in place:
+// mean = K + S1/ns, sd = sqrt(S2/ns - |S1/ns|^2), z <- (z - mean)/sd in FP64
+// (the responses, column nf, only centred); CTA (f, 0) stores mean and sd.
+__global__ void column_normalize_kernel(float2* __restrict__ Z, size_t kp, size_t ns, int nf,
+                                        const double* __restrict__ mom, double* __restrict__ mean,
+                                        double* __restrict__ sd) {
+    const int f = blockIdx.x;
+    const double* m = mom + kMom * (size_t)f;
+    const double d1r = m[0] / (double)ns, d1i = m[1] / (double)ns;
+    const double mr = m[3] + d1r, mi = m[4] + d1i;
+    const double var = m[2] / (double)ns - (d1r * d1r + d1i * d1i);
+    const double s = var > 0 ? sqrt(var) : 0.0;
+    const double sc = (f < nf && s > 0) ? 1.0 / s : 1.0;
+    if (blockIdx.y == 0 && threadIdx.x == 0) {
         mean[2 * f] = mr;
         mean[2 * f + 1] = mi;
-        const double s = sqrt(ss / (double)ns);
         if (f < nf) sd[f] = s;
-        scale = (f < nf && s > 0) ? 1.0 / s : 1.0;  // the responses are only centred
     }
-    __syncthreads();
-    const double sc = scale;
-    for (size_t i = threadIdx.x; i < ns; i += blockDim.x)
-        col[i] = make_float2((float)((col[i].x - mr) * sc), (float)((col[i].y - mi) * sc));
+    float2* col = Z + (size_t)f * kp;
+    const size_t per = (ns + gridDim.y - 1) / gridDim.y;
+    const size_t i0 = per * blockIdx.y, i1 = i0 + per < ns ? i0 + per : ns;
+    for (size_t i = i0 + threadIdx.x; i < i1; i += 4 * (size_t)blockDim.x) {
+        float2 z[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const size_t j = i + (size_t)u * blockDim.x;
+            if (j < i1) z[u] = col[j];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const size_t j = i + (size_t)u * blockDim.x;
+            if (j < i1) col[j] = make_float2((float)((z[u].x - mr) * sc), (float)((z[u].y - mi) * sc));
+        }
+    }
 }
 
 // G[a][b] += sum_i conj(Z[a][i]) Z[b][i] for the upper-triangle tiles (a <= b)
@@ -198,7 +254,7 @@ __global__ void column_stats_kernel(float2* __restrict__ Z, size_t kp, size_t ns
 // must not run in FP32, but 16-term partial sums keep their error near that
 // of the FP32 features and the multiply-adds on the FP32 pipes (GB300's FP64
 // rate is a small fraction of its FP32 rate).
-__global__ void __launch_bounds__(256) gram_kernel(const float2* __restrict__ Z, size_t kp, int nfp,
+__global__ void __launch_bounds__(256, 2) gram_kernel(const float2* __restrict__ Z, size_t kp, int nfp,
                                                    double2* __restrict__ G) {
     const int bi = blockIdx.y, bj = blockIdx.x;
     if (bi > bj) return;
@@ -277,6 +333,7 @@ __global__ void design_apply_kernel(const float2* __restrict__ Z, size_t kp, siz
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ns; i += (size_t)gridDim.x * blockDim.x) {
         const float2 y = Z[(size_t)nf * kp + i];
         double re = y.x, im = y.y;
+#pragma unroll 4
         for (int f = 0; f < nf; ++f) {
             const float2 z = Z[(size_t)f * kp + i];
             const double2 xf = __ldg(x + f);
@@ -292,17 +349,31 @@ __global__ void design_adjoint_kernel(const float2* __restrict__ Z, size_t kp, s
     __shared__ double red[32];
     const int f = blockIdx.x;
     const float2* col = Z + (size_t)f * kp;
+    const size_t per = (ns + gridDim.y - 1) / gridDim.y;
+    const size_t i0 = per * blockIdx.y, i1 = i0 + per < ns ? i0 + per : ns;
     double re = 0, im = 0;
-    for (size_t i = threadIdx.x; i < ns; i += blockDim.x) {
-        const float2 z = col[i];
-        const double2 vi = v[i];
-        re = fma((double)z.x, vi.x, fma((double)z.y, vi.y, re));
-        im = fma((double)z.x, vi.y, fma(-(double)z.y, vi.x, im));
+    for (size_t i = i0 + threadIdx.x; i < i1; i += 4 * (size_t)blockDim.x) {
+        float2 z[4];
+        double2 vi[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const size_t j = i + (size_t)u * blockDim.x;
+            z[u] = j < i1 ? col[j] : make_float2(0.f, 0.f);
+            vi[u] = j < i1 ? v[j] : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            re = fma((double)z[u].x, vi[u].x, fma((double)z[u].y, vi[u].y, re));
+            im = fma((double)z[u].x, vi[u].y, fma(-(double)z[u].y, vi[u].x, im));
+        }
     }
     re = block_sum_d(re, red);
     __syncthreads();
     im = block_sum_d(im, red);
-    if (threadIdx.x == 0) r[f] = make_double2(re, im);
+    if (threadIdx.x == 0) {  // r is zeroed by the caller; the CTAs of a column meet here
+        atomicAdd(&r[f].x, re);
+        atomicAdd(&r[f].y, im);
+    }
 }
 
 // SPM feature list in the order of sino.cpp:70-100 / wdm_sino.cpp:47-71.
@@ -322,11 +393,13 @@ struct FitBuffers {
     Feature* fs = nullptr;
     double2* G = nullptr;
     double* stat = nullptr;
+    double* mom = nullptr;
     ~FitBuffers() {
         cudaFree(Z);
         cudaFree(fs);
         cudaFree(G);
         cudaFree(stat);
+        cudaFree(mom);
     }
 };
 
@@ -336,6 +409,7 @@ cudaError_t fit_alloc(FitBuffers& b, const std::vector<Feature>& fs, size_t kp, 
     if (e == cudaSuccess) e = cudaMalloc(&b.fs, sizeof(Feature) * std::max(nf, 1));
     if (e == cudaSuccess) e = cudaMalloc(&b.G, sizeof(double2) * (size_t)nfp * nfp);
     if (e == cudaSuccess) e = cudaMalloc(&b.stat, sizeof(double) * (3 * (size_t)nfp + 2));
+    if (e == cudaSuccess) e = cudaMalloc(&b.mom, sizeof(double) * kMom * (size_t)nfp);
     if (e == cudaSuccess) e = cudaMemsetAsync(b.Z, 0, sizeof(float2) * (size_t)nfp * kp, s);
     if (e == cudaSuccess && nf) e = cudaMemcpyAsync(b.fs, fs.data(), sizeof(Feature) * nf, cudaMemcpyHostToDevice, s);
     return e;
@@ -345,9 +419,23 @@ cudaError_t fit_alloc(FitBuffers& b, const std::vector<Feature>& fs, size_t kp, 
 // copy gram ((nf+1)^2 complex128, upper triangle), mean (nf+1 complex128) and
 // sd (nf doubles) to the host.
 // z-scores the feature columns and centres the responses in place.
-void fit_stats(FitBuffers& b, size_t kp, size_t ns, int nf, int nfp, cudaStream_t s) {
-    column_stats_kernel<<<nf + 1, 256, 0, s>>>(b.Z, kp, ns, nf, b.stat, b.stat + 2 * (size_t)nfp);
+// Splits each of `cols` columns of ns samples over enough CTAs to give the
+// GPU about 8 CTAs of 256 threads per SM, at least 4096 samples per CTA.
+inline unsigned column_split(int cols, size_t ns) {
+    const size_t by_work = (ns + 4095) / 4096, by_fill = ((size_t)152 * 8 + cols - 1) / (size_t)cols;
+    const size_t y = std::min(by_work, by_fill);
+    return (unsigned)std::max<size_t>(1, std::min<size_t>(y, 65535));
+}
+
+cudaError_t fit_stats(FitBuffers& b, size_t kp, size_t ns, int nf, int nfp, cudaStream_t s) {
+    const dim3 grid(nf + 1, column_split(nf + 1, ns));
+    cudaError_t e = cudaMemsetAsync(b.mom, 0, sizeof(double) * kMom * (size_t)(nf + 1), s);
+    if (e != cudaSuccess) return e;
+    column_moments_kernel<<<grid, 256, 0, s>>>(b.Z, kp, ns, b.mom);
     count_launch();
+    column_normalize_kernel<<<grid, 256, 0, s>>>(b.Z, kp, ns, nf, b.mom, b.stat, b.stat + 2 * (size_t)nfp);
+    count_launch();
+    return cudaGetLastError();
 }
 
 // r = Z^H (y - Z x) for the prepared design (x, r: nf complex128 on the host).
@@ -357,10 +445,11 @@ cudaError_t fit_residual(FitBuffers& b, size_t kp, size_t ns, int nf, const doub
     if (e == cudaSuccess) e = cudaMalloc(&dv, sizeof(double2) * ns);
     if (e == cudaSuccess) e = cudaMalloc(&dr, sizeof(double2) * nf);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x, sizeof(double2) * nf, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dr, 0, sizeof(double2) * nf, s);
     if (e == cudaSuccess) {
         design_apply_kernel<<<grid_for_(ns), 256, 0, s>>>(b.Z, kp, ns, nf, dx, dv);
         count_launch();
-        design_adjoint_kernel<<<nf, 256, 0, s>>>(b.Z, kp, ns, dv, dr);
+        design_adjoint_kernel<<<dim3(nf, column_split(nf, ns)), 256, 0, s>>>(b.Z, kp, ns, dv, dr);
         count_launch();
         e = cudaGetLastError();
     }
@@ -374,10 +463,18 @@ cudaError_t fit_residual(FitBuffers& b, size_t kp, size_t ns, int nf, const doub
 
 cudaError_t fit_finish(FitBuffers& b, size_t kp, size_t ns, int nf, int nfp, double* gram, double* mean, double* sd,
                        cudaStream_t s) {
-    // split the samples so that the upper-triangle tiles fill every SM twice
+    // Split the samples over grid.z so that the upper-triangle tiles fill
+    // whole waves of 2 CTAs per SM: the GPU time goes as waves(ks) / ks, and
+    // the smallest split within 5 % of the best one keeps the FP64 atomics
+    // that merge the splits few.
     const int tiles = (nfp / GT) * (nfp / GT + 1) / 2;
-    const int chunks = (int)(kp / GK);
-    const int ks = std::max(1, std::min({(2 * 152 + tiles - 1) / tiles, 32, chunks}));
+    const int kmax = std::max(1, std::min(256, (int)(kp / GK)));
+    constexpr int kWave = 152 * 2;
+    auto per_wave = [&](int k) { return (double)k / (double)((tiles * k + kWave - 1) / kWave); };
+    double best = 0.0;
+    for (int k = 1; k <= kmax; ++k) best = std::max(best, per_wave(k));
+    int ks = 1;
+    while (ks < kmax && per_wave(ks) < 0.95 * best) ++ks;
     dim3 g2(nfp / GT, nfp / GT, ks);
     cudaError_t e0 = cudaMemsetAsync(b.G, 0, sizeof(double2) * (size_t)nfp * nfp, s);
     if (e0 != cudaSuccess) return e0;
@@ -420,8 +517,7 @@ focss_status sino_design(Ctx* c, const Field* tx, const Field* rx, int R, int ty
                                                         make_float2((float)lw_re, (float)lw_im), type == 1,
                                                         b.Z + (size_t)nf * kp);
         count_launch();
-        fit_stats(b, kp, ns, nf, nfp, s);
-        e = cudaGetLastError();
+        e = fit_stats(b, kp, ns, nf, nfp, s);
     }
     return cuda_check(c, e, "sino fit design");
 }
@@ -456,8 +552,7 @@ focss_status wdm_design(Ctx* c, const Field* tx, const Field* rx, int c_radius, 
         count_launch();
         wdm_responses_kernel<<<grid_for_(ns), 256, 0, s>>>(rx->d, rx->modes == 6 ? 2 : 0, N, R, b.Z + (size_t)nf * kp);
         count_launch();
-        fit_stats(b, kp, ns, nf, nfp, s);
-        e = cudaGetLastError();
+        e = fit_stats(b, kp, ns, nf, nfp, s);
     }
     return cuda_check(c, e, "wdm_ppe fit design");
 }

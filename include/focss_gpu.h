@@ -100,7 +100,8 @@ FOCSS_API const char* focss_status_string(int status);
 FOCSS_API int focss_abi_version(void);
 
 /* ------------------------------------------------------------------ field */
-/* focss::Field(const Domain&) (src/focss/field.cpp:24-38): zero-filled.      */
+/* focss::Field(const Domain&) (src/focss/field.cpp:24-38): zero-filled;      */
+/* batch x modes <= 65535 (FOCSS_ERR_INVALID_ARG otherwise).                  */
 FOCSS_API focss_status focss_field_create(focss_ctx* ctx, const focss_domain* domain, int batch,
                                           focss_field** out);
 /* ~Field (src/focss/field.cpp:130, 543-547) */

@@ -127,6 +127,39 @@ def test_rrc_round_trip_full_size(ctx):
     np.testing.assert_array_equal(dsp.hd_sequence_16qam(back), codes)
 
 
+def test_decisions_near_level_boundaries(ctx, oracle_cpu):
+    """Samples planted on and around the level boundaries of the normalized
+    coordinates (0 and +-2/sqrt 10, offsets 0 to 1e-4 on either side, on
+    each axis): the kernels decide from FP32 coordinates only outside a
+    guard band and take the FP64 argmin inside it, so codes, error counts,
+    hard and soft decisions equal the FP64 oracle's exactly."""
+    rng = np.random.default_rng(99)
+    n = 1 << 16
+    base = f32(oracle_cpu.qam16_map(rng.integers(0, 16, n)) * 0.7)
+    b = 2 / np.sqrt(10)
+    offs = np.array([0, 1e-9, 1e-7, 1e-6, 9e-6, 1.1e-5, 3e-5, 1e-4])
+    offs = np.concatenate([offs, -offs[1:]])
+    near = (np.array([0.0, b, -b])[:, None] + offs[None, :]).ravel()
+    other = np.array([-3, -1, 1, 3]) / np.sqrt(10)
+    planted = np.concatenate([(near[:, None] + 1j * other[None, :]).ravel(),
+                              (other[None, :] + 1j * near[:, None]).ravel()])
+    idx = rng.choice(n, planted.size, replace=False)
+    x = base.copy()
+    for _ in range(4):  # the planted samples move the RMS they are scaled by
+        sp = np.sqrt(np.mean(np.abs(x) ** 2))
+        x[idx] = planted * sp
+        x = f32(x)
+    r = fld(x, 1.0, ctx)
+    np.testing.assert_array_equal(dsp.hd_sequence_16qam(r)[0, 0], oracle_cpu.hd_sequence(x))
+    np.testing.assert_array_equal(dsp.hard_decision_16qam(r).numpy(np.complex64)[0, 0],
+                                  oracle_cpu.hard_decision(x).astype(np.complex64))
+    for u in (0.05, 1e-5 / np.sqrt(10), 0.0):
+        np.testing.assert_array_equal(dsp.soft_decision_16qam(r, u).numpy(np.complex64)[0, 0],
+                                      oracle_cpu.soft_decision(x, u).astype(np.complex64))
+    be, se = dsp.error_counts(fld(base, 1.0, ctx), r, 0)
+    assert (int(be[0]), int(se[0])) == oracle_cpu.error_counts(base, x, 0)
+
+
 def test_certainty_decisions(ctx, oracle_cpu):
     """find_certainty / sd / hd (src/tasks/wdm_scoring.cpp:105-156) on
     3 realizations of a 6-row (3 channels x 2 modes) dataset-shaped field:

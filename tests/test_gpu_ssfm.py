@@ -46,6 +46,14 @@ def test_fft_rejects_unsupported_length(ctx):
     assert e.value.status == 6
 
 
+def test_field_rejects_too_many_rows(ctx):
+    """Realization rows (batch x modes) map to a grid dimension: at most 65535."""
+    with pytest.raises(fg.FocssError) as e:
+        fg.Field(fg.Domain(2, 256, 1.0), batch=40000, ctx=ctx)
+    assert e.value.status == 1
+    fg.Field(fg.Domain(1, 256, 1.0), batch=65535, ctx=ctx)
+
+
 def test_ssfm_uniform_matches_reference(ctx, golden):
     dt = float(golden["dt"][0])
     span = fg.Fiber(*golden["ssfm_span"])
