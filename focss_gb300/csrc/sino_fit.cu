@@ -18,7 +18,8 @@
 // The Gram product is a tiled complex kernel on the CUDA
 // cores (64 x 64 output tiles, 4 x 4 complex outputs per thread, the samples
 // split over the grid's z dimension) reading the FP32 features, summing runs
-// of 16 samples in FP32 and accumulating those sums in FP64.  The residual
+// of 16 samples in FP32 and accumulating those sums as double-float pairs
+// (~48 bits, converted to FP64 once per CTA).  The residual
 // entry points rebuild the same design and return Z^H (y - Z x) in FP64, so
 // the caller can refine its solve to the FP64 normal-equations solution.
 #include <algorithm>
@@ -249,11 +250,19 @@ __global__ void column_normalize_kernel(float2* __restrict__ Z, size_t kp, size_
 // over this CTA's share of the samples (grid.z splits them; G starts at zero
 // and the shares meet in FP64 atomics).  Z is zero-padded to multiples of GT
 // features and GK samples.  Each run of kFlush x GK = 16 samples is summed in
-// FP32 (products of FP32 features) and added to FP64 accumulators: the normal
-// equations square the design's condition number, so sums over ~1e5 samples
-// must not run in FP32, but 16-term partial sums keep their error near that
-// of the FP32 features and the multiply-adds on the FP32 pipes (GB300's FP64
-// rate is a small fraction of its FP32 rate).
+// FP32 (products of FP32 features) and the run sums are accumulated as
+// double-float pairs hi + lo (Knuth's two-sum, ~48 significant bits) on the
+// FP32 pipes: the normal equations square the design's condition number, so
+// sums over ~1e5 samples must not run in plain FP32, but GB300's FP64 rate
+// is a small fraction of its FP32 rate and FP64 accumulation of the run sums
+// held the kernel on the FP64 pipe.  The pairs go to FP64 once, at the end.
+__device__ __forceinline__ void df_acc(float& hi, float& lo, float x) {
+    const float s = hi + x;
+    const float bv = s - hi;
+    lo += (hi - (s - bv)) + (x - bv);
+    hi = s;
+}
+
 __global__ void __launch_bounds__(256, 2) gram_kernel(const float2* __restrict__ Z, size_t kp, int nfp,
                                                    double2* __restrict__ G) {
     const int bi = blockIdx.y, bj = blockIdx.x;
@@ -261,11 +270,11 @@ __global__ void __launch_bounds__(256, 2) gram_kernel(const float2* __restrict__
     __shared__ float2 As[GK][GT + 1];
     __shared__ float2 Bs[GK][GT + 1];
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-    double2 acc[4][4];
+    float4 acc[4][4];  // {re_hi, re_lo, im_hi, im_lo}
 #pragma unroll
     for (int r = 0; r < 4; ++r)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) acc[r][c] = make_double2(0.0, 0.0);
+        for (int c = 0; c < 4; ++c) acc[r][c] = make_float4(0.f, 0.f, 0.f, 0.f);
     const float2* Za = Z + (size_t)bi * GT * kp;
     const float2* Zb = Z + (size_t)bj * GT * kp;
     const size_t chunks = kp / GK;
@@ -306,8 +315,8 @@ __global__ void __launch_bounds__(256, 2) gram_kernel(const float2* __restrict__
             for (int r = 0; r < 4; ++r)
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
-                    acc[r][c].x += (double)part[r][c].x;
-                    acc[r][c].y += (double)part[r][c].y;
+                    df_acc(acc[r][c].x, acc[r][c].y, part[r][c].x);
+                    df_acc(acc[r][c].z, acc[r][c].w, part[r][c].y);
                     part[r][c] = make_float2(0.f, 0.f);
                 }
         }
@@ -318,8 +327,8 @@ __global__ void __launch_bounds__(256, 2) gram_kernel(const float2* __restrict__
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
             double2* g = G + (size_t)(bi * GT + ty * 4 + r) * nfp + bj * GT + tx + 16 * c;
-            atomicAdd(&g->x, acc[r][c].x);
-            atomicAdd(&g->y, acc[r][c].y);
+            atomicAdd(&g->x, (double)acc[r][c].x + (double)acc[r][c].y);
+            atomicAdd(&g->y, (double)acc[r][c].z + (double)acc[r][c].w);
         }
 }
 

@@ -342,7 +342,8 @@ FOCSS_API focss_status focss_sino_equalize(focss_ctx* ctx, const focss_field* rx
  * [R, N-R) of every mode, z-scored per feature (mean, standard deviation
  * normalized by the count), and the responses rx (type 1 = FIXED: rx - lw*tx;
  * type 2 = HOMOGENEOUS: rx) centred, appended as column nf.  Outputs:
- * gram = [Z y]^H [Z y] accumulated in FP64, (nf+1) x (nf+1) complex
+ * gram = [Z y]^H [Z y] (FP32 products, 16-sample runs accumulated to ~48
+ * bits, returned as FP64), (nf+1) x (nf+1) complex
  * (interleaved FP64) row-major, upper triangle valid; mean = nf+1 complex means (interleaved FP64, the last one the
  * responses'); sd = nf standard deviations.  nf = focss_sino_num_features.
  * tx and rx: single realizations of one domain.  The caller solves
