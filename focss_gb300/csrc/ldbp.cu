@@ -21,74 +21,167 @@
 
 namespace fg {
 
-constexpr int FIR_TILE = 1024;      // outputs per CTA
-constexpr int FIR_THREADS = 256;    // 4 outputs per thread
+constexpr int FIR_THREADS = 128;                    // fir_kernel
+constexpr int FIR_GRAD_THREADS = 256;               // fir_grad_taps_kernel: 8 warps x 8 taps
+constexpr int FIR_OUT = 4;                          // consecutive outputs per thread
+constexpr int FIR_TILE = FIR_THREADS * FIR_OUT;     // outputs per CTA of fir_kernel
+constexpr int FIR_GRAD_TILE = 2048;                 // samples per CTA of fir_grad_taps_kernel
 constexpr int FIR_MAX_TAPS = 255;
+constexpr int FIR_TAPS_PAD = (FIR_MAX_TAPS + 7) / 8 * 8;
+// Shared-memory sample windows keep one padding slot after every R samples,
+// R the run a thread reads from a multiple of R: runs of 4 (forward) start
+// 40 bytes apart across a half-warp and runs of 8 (tap gradient) 72 bytes
+// apart, both on distinct bank pairs.
+template <int R>
+__device__ __forceinline__ int fir_pad(int i) { return i + i / R; }
+constexpr int FIR_XS = (FIR_TILE + FIR_TAPS_PAD + 8) * (FIR_OUT + 1) / FIR_OUT;
+constexpr int FIR_GRAD_XS = (FIR_GRAD_TILE + FIR_TAPS_PAD + 8) * 9 / 8;
 
-// y = FIR(x, h) for every realization; conj_rev: use h'[t] = conj(h[T-1-t])
-// (the adjoint filter, for the input gradient).
-__global__ void __launch_bounds__(FIR_THREADS) fir_kernel(const float2* __restrict__ x, const float2* __restrict__ h,
-                                                          int T, int conj_rev, float2* __restrict__ y, int N) {
-    __shared__ float2 xs[FIR_TILE + FIR_MAX_TAPS];
-    __shared__ float2 hs[FIR_MAX_TAPS + 1];
-    const int b = blockIdx.y;
-    const int n0 = blockIdx.x * FIR_TILE;
-    const int c = (T - 1) / 2;
-    const float2* xb = x + (size_t)b * N;
-    for (int t = threadIdx.x; t < T; t += blockDim.x) {
-        float2 v = conj_rev ? h[T - 1 - t] : h[t];
-        if (conj_rev) v.y = -v.y;
-        hs[t] = v;
-    }
-    const int span = FIR_TILE + T - 1;
-    for (int i = threadIdx.x; i < span; i += blockDim.x) {
-        int s = n0 - c + i;
-        s %= N;
-        if (s < 0) s += N;
-        xs[i] = xb[s];
-    }
-    __syncthreads();
-    for (int o = threadIdx.x; o < FIR_TILE && n0 + o < N; o += blockDim.x) {
-        float2 acc = make_float2(0.f, 0.f);
-        for (int t = 0; t < T; ++t) {
-            const float2 hv = hs[t], xv = xs[o + t];
-            acc.x = fmaf(hv.x, xv.x, fmaf(-hv.y, xv.y, acc.x));
-            acc.y = fmaf(hv.x, xv.y, fmaf(hv.y, xv.x, acc.y));
+// Loads samples [n0 - c, n0 - c + span) of one realization (circular) into
+// the padded window: all of a thread's loads are issued before the first
+// store (a load-store loop would wait for one load latency per iteration).
+template <int THREADS, int TILE, int R>
+__device__ __forceinline__ void fir_load_window(float2* xs, const float2* __restrict__ xb, int n0, int c, int span,
+                                                int N) {
+    constexpr int K = (TILE + FIR_TAPS_PAD + THREADS - 1) / THREADS;
+    float2 v[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int i = threadIdx.x + k * THREADS;
+        if (i < span) {
+            int s = n0 - c + i;
+            if (s < 0 || s >= N) {
+                s %= N;
+                if (s < 0) s += N;
+            }
+            v[k] = xb[s];
         }
-        y[(size_t)b * N + n0 + o] = acc;
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int i = threadIdx.x + k * THREADS;
+        if (i < span) xs[fir_pad<R>(i)] = v[k];
     }
 }
 
-// g_h[t] += sum_n g_y[n] conj(x[(n + t - c) mod N]) over all realizations.
-__global__ void __launch_bounds__(FIR_THREADS) fir_grad_taps_kernel(const float2* __restrict__ x,
-                                                                    const float2* __restrict__ gy, int T,
-                                                                    float2* __restrict__ gh, int N) {
-    __shared__ float2 xs[FIR_TILE + FIR_MAX_TAPS];
-    __shared__ float2 gs[FIR_TILE];
+// y = FIR(x, h) for every realization; conj_rev: use h'[t] = conj(h[T-1-t])
+// (the adjoint filter, for the input gradient).  Register-blocked: a thread
+// computes 4 consecutive outputs from an 11-sample register window per 8 taps
+// (taps zero-padded to a multiple of 8), so a product costs 19/32 of a
+// shared-memory load instead of two; each output still sums its taps in
+// ascending order with the same fused multiply-adds.
+//
+// Inference epilogue (both optional): the output is multiplied by `gain`
+// (the span's drop_power factor, moved past the linear filter) and then
+// rotated by exp(i xi |.|^2) (the step's nonlinear phase, as nl_kernel), so
+// one launch does a whole learned step.
+__global__ void __launch_bounds__(FIR_THREADS) fir_kernel(const float2* __restrict__ x, const float2* __restrict__ h,
+                                                          int T, int conj_rev, float2* __restrict__ y, int N,
+                                                          float gain, const float* __restrict__ xi) {
+    __shared__ float2 xs[FIR_XS];
+    __shared__ float2 hs[FIR_TAPS_PAD];
     const int b = blockIdx.y;
     const int n0 = blockIdx.x * FIR_TILE;
     const int c = (T - 1) / 2;
-    const float2* xb = x + (size_t)b * N;
-    const int span = FIR_TILE + T - 1;
-    for (int i = threadIdx.x; i < span; i += blockDim.x) {
-        int s = n0 - c + i;
-        s %= N;
-        if (s < 0) s += N;
-        xs[i] = xb[s];
+    const int Tp = (T + 7) & ~7;
+    for (int t = threadIdx.x; t < Tp; t += blockDim.x) {
+        float2 v = make_float2(0.f, 0.f);
+        if (t < T) {
+            v = conj_rev ? h[T - 1 - t] : h[t];
+            if (conj_rev) v.y = -v.y;
+        }
+        hs[t] = v;
     }
-    for (int i = threadIdx.x; i < FIR_TILE; i += blockDim.x)
-        gs[i] = (n0 + i < N) ? gy[(size_t)b * N + n0 + i] : make_float2(0.f, 0.f);
+    fir_load_window<FIR_THREADS, FIR_TILE, FIR_OUT>(xs, x + (size_t)b * N, n0, c, FIR_TILE + Tp, N);
     __syncthreads();
-    // warp w handles taps t = w, w + 8, ...; lanes stride over n
+    const int o0 = threadIdx.x * FIR_OUT;
+    float2 acc[FIR_OUT];
+#pragma unroll
+    for (int i = 0; i < FIR_OUT; ++i) acc[i] = make_float2(0.f, 0.f);
+    for (int tb = 0; tb < Tp; tb += 8) {
+        constexpr int WN = FIR_OUT + 7;  // window of 8 taps x FIR_OUT outputs
+        float2 w[WN], hv[8];
+        const int base = ((o0 + tb) / FIR_OUT) * (FIR_OUT + 1);
+#pragma unroll
+        for (int j = 0; j < WN; ++j) w[j] = xs[base + j + j / FIR_OUT];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) hv[u] = hs[tb + u];
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+#pragma unroll
+            for (int i = 0; i < FIR_OUT; ++i) {
+                const float2 xv = w[i + u];
+                acc[i].x = fmaf(hv[u].x, xv.x, fmaf(-hv[u].y, xv.y, acc[i].x));
+                acc[i].y = fmaf(hv[u].x, xv.y, fmaf(hv[u].y, xv.x, acc[i].y));
+            }
+    }
+    if (gain != 1.0f) {
+#pragma unroll
+        for (int i = 0; i < FIR_OUT; ++i) acc[i] = cscale(acc[i], gain);
+    }
+    if (xi) {
+        const float k = *xi;
+#pragma unroll
+        for (int i = 0; i < FIR_OUT; ++i) acc[i] = cmul(acc[i], phase_rotation(k * cnorm(acc[i])));
+    }
+    float2* yb = y + (size_t)b * N + n0 + o0;
+#pragma unroll
+    for (int i = 0; i < FIR_OUT; ++i)
+        if (n0 + o0 + i < N) yb[i] = acc[i];
+}
+
+// g_h[t] += sum_n g_y[n] conj(x[(n + t - c) mod N]) over all realizations.
+// Warp w takes taps 8w .. 8w + 7 (+ 64 per round for longer filters), lane l
+// the 8 consecutive samples 8l .. 8l + 7 of each 256-sample chunk of the
+// 2048-sample tile: per (chunk, 8 taps) a 15-sample register window and 8 gradient
+// samples give 64 products; lanes meet in a warp sum, CTAs in atomics.
+__global__ void __launch_bounds__(FIR_GRAD_THREADS) fir_grad_taps_kernel(const float2* __restrict__ x,
+                                                                         const float2* __restrict__ gy, int T,
+                                                                         float2* __restrict__ gh, int N) {
+    __shared__ float2 xs[FIR_GRAD_XS];
+    __shared__ float2 gs[FIR_GRAD_TILE * 9 / 8];
+    const int b = blockIdx.y;
+    const int n0 = blockIdx.x * FIR_GRAD_TILE;
+    const int c = (T - 1) / 2;
+    const int Tp = (T + 7) & ~7;
+    fir_load_window<FIR_GRAD_THREADS, FIR_GRAD_TILE, 8>(xs, x + (size_t)b * N, n0, c, FIR_GRAD_TILE + Tp, N);
+    {
+        constexpr int K = FIR_GRAD_TILE / FIR_GRAD_THREADS;
+        float2 v[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int i = threadIdx.x + k * FIR_GRAD_THREADS;
+            v[k] = (n0 + i < N) ? gy[(size_t)b * N + n0 + i] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) gs[fir_pad<8>(threadIdx.x + k * FIR_GRAD_THREADS)] = v[k];
+    }
+    __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int t = warp; t < T; t += FIR_THREADS / 32) {
-        float2 acc = make_float2(0.f, 0.f);
-        for (int o = lane; o < FIR_TILE; o += 32) acc = cadd(acc, cmulc(gs[o], xs[o + t]));
-        acc.x = warp_sum(acc.x);
-        acc.y = warp_sum(acc.y);
-        if (lane == 0) {
-            atomicAdd(&gh[t].x, acc.x);
-            atomicAdd(&gh[t].y, acc.y);
+    for (int t0 = warp * 8; t0 < Tp; t0 += 64) {
+        float2 acc[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[j] = make_float2(0.f, 0.f);
+        for (int q = 0; q < FIR_GRAD_TILE; q += 256) {
+            const int nl = q + 8 * lane;  // first local sample of this lane
+            float2 g[8], w[16];
+            const int gb = (nl >> 3) * 9, xb = ((nl + t0) >> 3) * 9;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) g[i] = gs[gb + i];
+#pragma unroll
+            for (int k = 0; k < 15; ++k) w[k] = xs[xb + k + (k >> 3)];
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+#pragma unroll
+                for (int i = 0; i < 8; ++i) acc[j] = cadd(acc[j], cmulc(g[i], w[i + j]));
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const float sx = warp_sum(acc[j].x), sy = warp_sum(acc[j].y);
+            if (lane == 0 && t0 + j < T) {
+                atomicAdd(&gh[t0 + j].x, sx);
+                atomicAdd(&gh[t0 + j].y, sy);
+            }
         }
     }
 }
@@ -209,15 +302,38 @@ using fg::count_launch;
 
 static focss_status ldbp_err(focss_ctx* c, cudaError_t e, const char* what) { return fg::cuda_check(c, e, what); }
 
-static cudaError_t fir(const LdbpModel& M, const float2* x, const float2* h, int T, int conj_rev, float2* y) {
+static cudaError_t fir(const LdbpModel& M, const float2* x, const float2* h, int T, int conj_rev, float2* y,
+                       float gain = 1.0f, const float* xi = nullptr) {
     dim3 g((M.samples + fg::FIR_TILE - 1) / fg::FIR_TILE, M.batch);
-    fg::fir_kernel<<<g, fg::FIR_THREADS, 0, M.ctx->stream>>>(x, h, T, conj_rev, y, M.samples);
+    fg::fir_kernel<<<g, fg::FIR_THREADS, 0, M.ctx->stream>>>(x, h, T, conj_rev, y, M.samples, gain, xi);
     count_launch();
     return cudaGetLastError();
 }
 
+// Inference forward pass: one launch per learned step (FIR, the span's
+// drop_power factor applied to the filter output, nonlinear phase), reading
+// the input field directly, then the matched filter into work[1].
+static cudaError_t ldbp_infer(LdbpModel& M, const float2* in) {
+    const size_t n = M.field_n();
+    float2* bufs[2] = {M.work, M.work + n};
+    const int layers = M.spans * M.steps;
+    int w = (layers - 1) & 1;  // the last step lands in work[0]
+    const float2* src = in;
+    cudaError_t e = cudaSuccess;
+    for (int sp = 0; sp < M.spans && e == cudaSuccess; ++sp)
+        for (int st = 0; st < M.steps && e == cudaSuccess; ++st) {
+            const int k = sp * M.steps + st;
+            e = fir(M, src, M.h(k), M.taps, 0, bufs[w], st == 0 ? M.span_scale : 1.0f, M.xi(k));
+            src = bufs[w];
+            w ^= 1;
+        }
+    if (e == cudaSuccess) e = fir(M, src, M.hmf(), M.mf_taps, 0, M.work + n);
+    return e;
+}
+
 // Forward pass; keeps every layer input in M.acts when `keep`.
 static cudaError_t ldbp_forward(LdbpModel& M, const float2* in, bool keep) {
+    if (!keep && M.steps > 0) return ldbp_infer(M, in);
     cudaStream_t s = M.ctx->stream;
     const size_t n = M.field_n();
     float2* cur = M.work;
@@ -367,10 +483,10 @@ FOCSS_API focss_status focss_ldbp_loss_grad(focss_ldbp* m, const focss_field* in
     }
     const int L = m->spans * m->steps;
     int a = 2 * L;  // index of the matched filter's input activation
-    dim3 gg((m->samples + fg::FIR_TILE - 1) / fg::FIR_TILE, m->batch);
+    dim3 gg((m->samples + fg::FIR_GRAD_TILE - 1) / fg::FIR_GRAD_TILE, m->batch);
     // matched filter
     if (e == cudaSuccess) {
-        fg::fir_grad_taps_kernel<<<gg, fg::FIR_THREADS, 0, s>>>(m->acts + (size_t)a * n, g, m->mf_taps, m->ghmf(), m->samples);
+        fg::fir_grad_taps_kernel<<<gg, fg::FIR_GRAD_THREADS, 0, s>>>(m->acts + (size_t)a * n, g, m->mf_taps, m->ghmf(), m->samples);
         count_launch();
         e = cudaGetLastError();
     }
@@ -386,7 +502,7 @@ FOCSS_API focss_status focss_ldbp_loss_grad(focss_ldbp* m, const focss_field* in
             std::swap(g, g2);
             --a;  // FIR input
             if (e == cudaSuccess) {
-                fg::fir_grad_taps_kernel<<<gg, fg::FIR_THREADS, 0, s>>>(m->acts + (size_t)a * n, g, m->taps, m->gh(k), m->samples);
+                fg::fir_grad_taps_kernel<<<gg, fg::FIR_GRAD_THREADS, 0, s>>>(m->acts + (size_t)a * n, g, m->taps, m->gh(k), m->samples);
                 count_launch();
                 e = cudaGetLastError();
             }
