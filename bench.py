@@ -399,6 +399,8 @@ def run_ours(args):
         line["wdm_ppe"] = wdm_ppe_section(fg, ctx, stream)
     if args.dbp_sweep:
         line["dbp_sweep"] = dbp_sweep_section(fg, ctx)
+    if args.single_channel:
+        line["single_channel"] = single_channel_section(fg, ctx, stream)
     if world == 1 and rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         n_steps = CPU_BASELINE_STEPS
@@ -460,6 +462,69 @@ def _stream_ms(torch, stream, fn):
     e1.record(stream)
     e1.synchronize()
     return out, e0.elapsed_time(e1)
+
+
+SINGLE = dict(
+    workload="single_channel_16qam_32GBd_2^14sym_8sps_n2^17_10x80km_uniform_1km_2dBm",
+    symbols=2 ** 14, samples_per_symbol=8, roll_off=0.1, spans=10, span_m=80e3, step_m=1000.0,
+    power_dbm=2.0, batches=[1, 152], seed=7,
+)
+
+
+def single_channel_section(fg, ctx, stream):
+    """Plain single-channel SSFM: 2^14 16QAM symbols at 8 samples/symbol
+    (N = 2^17), 10 x 80 km SSMF with fixed 1 km steps and a lossless,
+    noise-free EDFA after every span, 2 dBm.  GPU throughput of the span-loop
+    graph for one realization (the reference's unit of work) and for 152
+    copies (one per SM), the FP32 field error against the FP64 oracle after
+    the first span, and the oracle's single-thread time for that span."""
+    import torch
+    from focss_gb300 import dsp
+    sc = SINGLE
+    alpha, beta2, gamma = fiber_params()
+    fib = fg.Fiber(alpha, beta2, gamma, sc["span_m"])
+    G = 10 ** (W["alpha_db_per_km"] * sc["span_m"] / 1e3 / 10)
+    ns, osf = sc["symbols"], sc["samples_per_symbol"]
+    n = ns * osf
+    steps_per_span = int(round(sc["span_m"] / sc["step_m"]))
+    rng = np.random.default_rng(sc["seed"])
+    sym = dsp.qam16_map(rng.integers(0, 16, (1, 1, ns)), fg.Domain(1, ns, 1 / 32e9, F0), ctx=ctx)
+    dsp.scale_each(sym, np.array([np.sqrt(1e-3 * 10 ** (sc["power_dbm"] / 10))]))
+    sig = dsp.rrc_shaping(sym, osf, sc["roll_off"])
+    x = sig.numpy()
+    ssfm = fg.SSFM(fib, steps_per_span)
+    out = {"config": sc, "samples": n, "runs": {}}
+    for B in sc["batches"]:
+        f = fg.Field(sig.domain, data=np.broadcast_to(x, (B, 1, n)), batch=B, ctx=ctx)
+        amp = fg.Amplifier(G, 0.0)
+        fg.span_loop([f], fib, ssfm, sc["spans"], after=fg.Amplifier.AMPLIFY, amplifier=amp)  # warm-up
+        ms = []
+        for _ in range(3):
+            f.upload(np.broadcast_to(x, (B, 1, n)))
+            ctx.sync()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fg.span_loop([f], fib, ssfm, sc["spans"], after=fg.Amplifier.AMPLIFY, amplifier=amp)
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        t = statistics.median(ms)
+        out["runs"]["batch_%d" % B] = {"ms": t, "gsample_steps_per_s": B * n * steps_per_span * sc["spans"] / t / 1e6}
+    # one span against the FP64 oracle (checker), timed on one host thread
+    from oracle import build as obuild
+    from oracle import cpu
+    obuild.build_oracle()
+    g = fg.Field(sig.domain, data=x, ctx=ctx)
+    ssfm.run(g)
+    got = g.numpy()[0, 0]
+    t0 = time.perf_counter()
+    ofib = cpu.Fiber(alpha, beta2, gamma, sc["span_m"], 1.55e-6, 1.0)
+    want, _ = cpu.ssfm_run(x[0, 0], sig.domain.time_step, ofib, cpu.UNIFORM, steps_per_span)
+    t_cpu = time.perf_counter() - t0
+    out["field_rel_l2_one_span"] = float(np.linalg.norm(got - want) / np.linalg.norm(want))
+    out["cpu_oracle_one_thread"] = {"s_per_span": t_cpu,
+                                    "gsample_steps_per_s": n * steps_per_span / t_cpu / 1e9}
+    return out
 
 
 def sweep_section(fg, ctx, stream):
@@ -915,6 +980,9 @@ def main():
                     help="skip the dual-polarization WDM dataset and WdmPPE scoring section")
     ap.add_argument("--dbp-sweep", action="store_true",
                     help="add the learned-vs-plain DBP launch-power sweep (-2..+4 dBm, 2^20 symbols per set; minutes)")
+    ap.add_argument("--single-channel", action="store_true",
+                    help="add the plain single-channel link (N=2^17, 10 x 80 km, 1 km steps): GPU throughput at "
+                         "batch 1 and 152, FP32 field error and single-thread FP64 oracle time for one span")
     ap.add_argument("--host-loop", action="store_true",
                     help="drive the spans from the host (one SSFM run + EDFA per span) instead of one graph")
     args = ap.parse_args()
