@@ -309,6 +309,27 @@ __global__ void __launch_bounds__(2 * C * ColFFT<N1>::P, 1) col_kernel(const Pas
 // first sample (global or shared memory), rows `ld` samples apart.  ROW_SSFM
 // applies exp(-alpha hl/2)/N (FP32 gain g) times the dispersion phase from the
 // 96-bit fraction dhi/dlo.
+// a k'^2 in turns as the 96-bit fixed-point product of the step's fraction
+// a (a96 = dhi 2^32 + the low 32 bits) and k'^2, carried exactly (mod 2^128)
+// along an arithmetic progression k' = k0 + delta i by second differences:
+// P_i = a k_i'^2, P_{i+1} = P_i + dP_i, dP_{i+1} = dP_i + 2 a delta^2.  next()
+// returns bits 32..95 of P_i, which equal dhi k'^2 + umulhi(dlo 2^32, k'^2)
+// mod 2^64.  |k0|, |delta| <= 2^19, so the integer factors fit in 64 bits.
+struct PhaseRun {
+    unsigned __int128 P, dP, C2;
+    __device__ __forceinline__ PhaseRun(unsigned __int128 a, long long k0, long long delta) {
+        P = a * (unsigned __int128)(unsigned long long)(k0 * k0);
+        dP = a * (unsigned __int128)(__int128)(2 * delta * k0 + delta * delta);
+        C2 = a * (unsigned __int128)(unsigned long long)(2 * delta * delta);
+    }
+    __device__ __forceinline__ unsigned long long next() {
+        const unsigned long long X = (unsigned long long)(P >> 32);
+        P += dP;
+        dP += C2;
+        return X;
+    }
+};
+
 template <int N2>
 __device__ __forceinline__ void row_work(const PassArgs& a, int op, float2* data, int k1, int rl, int t,
                                          const float4* s_tw, const float4* s_T, float2* sx, float g,
@@ -328,16 +349,28 @@ __device__ __forceinline__ void row_work(const PassArgs& a, int op, float2* data
         // The thread's own bins go through its column of the exchange buffer
         // so that this long per-bin body is emitted once (a rolled loop), not
         // Q times: the unrolled kernel overflowed the instruction cache.
+        //
+        // The thread's bins k = s0 + D j (s0 = k1 + N1 t, D = N1 P) fold to
+        // k' = s0 + D j for j < Q/2 and k' = N - s0 - D j above: two
+        // arithmetic progressions, along which a k'^2 is carried exactly by
+        // second differences (PhaseRun) instead of a 64 x 64-bit product per
+        // bin -- the same bits, so the same rotation.
         float2* mine = sx + lay(0, t);
 #pragma unroll
         for (int j = 0; j < Q; ++j) mine[j * (P + 1)] = v[j];
+        const unsigned __int128 a96 = ((unsigned __int128)dhi << 32) | (unsigned __int128)(dlo >> 32);
+        const long long s0 = (long long)k1 + (long long)N1 * t, D = (long long)N1 * P;
+        {
+            PhaseRun run(a96, s0, D);
 #pragma unroll 1
-        for (int j = 0; j < Q; ++j) {
-            const int k = k1 + N1 * (t + P * j);
-            const unsigned long long kp = (unsigned long long)(k <= (N >> 1) ? k : N - k);
-            const unsigned long long kk = kp * kp;
-            const unsigned long long X = dhi * kk + __umul64hi(dlo, kk);
-            mine[j * (P + 1)] = turns_rotate(cscale(mine[j * (P + 1)], g), X, s_T);
+            for (int j = 0; j < Q / 2; ++j)
+                mine[j * (P + 1)] = turns_rotate(cscale(mine[j * (P + 1)], g), run.next(), s_T);
+        }
+        {
+            PhaseRun run(a96, (long long)(N >> 1) - s0, -D);
+#pragma unroll 1
+            for (int j = Q / 2; j < Q; ++j)
+                mine[j * (P + 1)] = turns_rotate(cscale(mine[j * (P + 1)], g), run.next(), s_T);
         }
 #pragma unroll
         for (int j = 0; j < Q; ++j) v[j] = mine[j * (P + 1)];
