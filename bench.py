@@ -7,8 +7,8 @@ Workload (one bench step = one forward propagation of the whole batch):
   samples per realization; 20 x 80 km SSMF (alpha 0.2 dB/km, D 17 ps/nm/km,
   gamma 1.3 /W/km), ADAPTIVE split step (max nonlinear phase 0.005 rad/step,
   max step 1 km), EDFA after every span (gain = span loss, NF 5 dB, seeded
-  ASE).  Batch = 7 launch powers (-2..+4 dBm per channel) x 8 ASE seeds = 56
-  realizations (235 MB of complex64, larger than the 129 MB L2).
+  ASE).  Batch = 7 launch powers (-2..+4 dBm per channel) x 18 ASE seeds = 126
+  realizations (528 MB of complex64, 4.1x the 129 MB L2).
   One sample-step = one complex sample advanced by one split step.
 
 Arms:
@@ -43,7 +43,7 @@ W = dict(
     channels=5, symbols_per_channel=2 ** 15, samples_per_symbol=16, spacing_hz=50e9, baud=32e9,
     roll_off=0.1, spans=20, span_m=80e3, alpha_db_per_km=0.2, dispersion_ps_nm_km=17.0, gamma_per_w_km=1.3,
     max_phase_shift=0.005, max_step_m=1000.0, noise_figure_db=5.0,
-    powers_dbm=[-2, -1, 0, 1, 2, 3, 4], ase_seeds=8,
+    powers_dbm=[-2, -1, 0, 1, 2, 3, 4], ase_seeds=18,
 )
 N = W["symbols_per_channel"] * W["samples_per_symbol"]
 DT = 1.0 / (W["baud"] * W["samples_per_symbol"])
@@ -354,8 +354,9 @@ def run_ours(args):
         for ln in open(traffic_file):
             f = ln.split()
             if len(f) == 2 and f[0] == dom_kernel:
-                roofline["traffic"] = int(f[1])
-                roofline["traffic_source"] = "profiles/ssfm_traffic_wdm5_n2e19.txt (ncu, 40 realizations x 56/40)"
+                roofline["traffic"] = int(int(f[1]) * B / 40)
+                roofline["traffic_source"] = ("profiles/ssfm_traffic_wdm5_n2e19.txt (ncu, 40 realizations, "
+                                              "scaled x %d/40)" % B)
 
     # ---- end to end through the public API with host buffers (pinned)
     pin_in = torch.from_numpy(host.view(np.float32)).pin_memory()
@@ -379,7 +380,8 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / max(1, args.steps), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": dict(W, batch=B, samples=N, l2="batch of 235 MB complex64 exceeds the 129 MB L2",
+        "config": dict(W, batch=B, samples=N,
+                       l2="batch of %d MB complex64, %.1fx the 129 MB L2" % (B * N * 8 >> 20, B * N * 8 / 129e6),
                        fft_split="%d x %d (autotuned)" % (1 << split, N >> split),
                        parallelism="replicas" if world > 1 else "single GPU",
                        sample_steps_per_step=sample_steps / max(1, args.steps)),
@@ -467,7 +469,7 @@ def _stream_ms(torch, stream, fn):
 SINGLE = dict(
     workload="single_channel_16qam_32GBd_2^14sym_8sps_n2^17_10x80km_uniform_1km_2dBm",
     symbols=2 ** 14, samples_per_symbol=8, roll_off=0.1, spans=10, span_m=80e3, step_m=1000.0,
-    power_dbm=2.0, batches=[1, 152], seed=7,
+    power_dbm=2.0, batches=[1, 512], seed=7,
 )
 
 
@@ -475,8 +477,8 @@ def single_channel_section(fg, ctx, stream):
     """Plain single-channel SSFM: 2^14 16QAM symbols at 8 samples/symbol
     (N = 2^17), 10 x 80 km SSMF with fixed 1 km steps and a lossless,
     noise-free EDFA after every span, 2 dBm.  GPU throughput of the span-loop
-    graph for one realization (the reference's unit of work) and for 152
-    copies (one per SM), the FP32 field error against the FP64 oracle after
+    graph for one realization (the reference's unit of work) and for 512
+    copies (512 MB, 4x the L2), the FP32 field error against the FP64 oracle after
     the first span, and the oracle's single-thread time for that span."""
     import torch
     from focss_gb300 import dsp
@@ -982,7 +984,7 @@ def main():
                     help="add the learned-vs-plain DBP launch-power sweep (-2..+4 dBm, 2^20 symbols per set; minutes)")
     ap.add_argument("--single-channel", action="store_true",
                     help="add the plain single-channel link (N=2^17, 10 x 80 km, 1 km steps): GPU throughput at "
-                         "batch 1 and 152, FP32 field error and single-thread FP64 oracle time for one span")
+                         "batch 1 and 512, FP32 field error and single-thread FP64 oracle time for one span")
     ap.add_argument("--host-loop", action="store_true",
                     help="drive the spans from the host (one SSFM run + EDFA per span) instead of one graph")
     args = ap.parse_args()
