@@ -497,6 +497,7 @@ def single_channel_section(fg, ctx, stream):
     ssfm = fg.SSFM(fib, steps_per_span)
     out = {"config": sc, "samples": n, "runs": {}}
     for B in sc["batches"]:
+        split = fg.autotune(n, B, ctx=ctx)[0]  # the split the library's autotuner picks for this batch
         f = fg.Field(sig.domain, data=np.broadcast_to(x, (B, 1, n)), batch=B, ctx=ctx)
         amp = fg.Amplifier(G, 0.0)
         fg.span_loop([f], fib, ssfm, sc["spans"], after=fg.Amplifier.AMPLIFY, amplifier=amp)  # warm-up
@@ -511,7 +512,8 @@ def single_channel_section(fg, ctx, stream):
             e1.synchronize()
             ms.append(e0.elapsed_time(e1))
         t = statistics.median(ms)
-        out["runs"]["batch_%d" % B] = {"ms": t, "gsample_steps_per_s": B * n * steps_per_span * sc["spans"] / t / 1e6}
+        out["runs"]["batch_%d" % B] = {"ms": t, "gsample_steps_per_s": B * n * steps_per_span * sc["spans"] / t / 1e6,
+                                       "log2_n1": split}
     # one span against the FP64 oracle (checker), timed on one host thread
     from oracle import build as obuild
     from oracle import cpu
