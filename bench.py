@@ -478,8 +478,9 @@ def single_channel_section(fg, ctx, stream):
     (N = 2^17), 10 x 80 km SSMF with fixed 1 km steps and a lossless,
     noise-free EDFA after every span, 2 dBm.  GPU throughput of the span-loop
     graph for one realization (the reference's unit of work) and for 512
-    copies (512 MB, 4x the L2), the FP32 field error against the FP64 oracle after
-    the first span, and the oracle's single-thread time for that span."""
+    copies (512 MB, 4x the L2); then the whole link, CDC, matched filter,
+    phase search, Q and decisions for one realization against the FP64
+    oracle, and the oracle's single-thread time for the propagation."""
     import torch
     from focss_gb300 import dsp
     sc = SINGLE
@@ -514,20 +515,39 @@ def single_channel_section(fg, ctx, stream):
         t = statistics.median(ms)
         out["runs"]["batch_%d" % B] = {"ms": t, "gsample_steps_per_s": B * n * steps_per_span * sc["spans"] / t / 1e6,
                                        "log2_n1": split}
-    # one span against the FP64 oracle (checker), timed on one host thread
+    # The whole link once more on one realization, then CDC, matched filter,
+    # phase search (3600 angles), Q and decisions, against the FP64 oracle
+    # (checker) running the same chain on one host thread.
     from oracle import build as obuild
     from oracle import cpu
     obuild.build_oracle()
+    dt, cut = sig.domain.time_step, 100
     g = fg.Field(sig.domain, data=x, ctx=ctx)
-    ssfm.run(g)
+    fg.span_loop([g], fib, ssfm, sc["spans"], after=fg.Amplifier.AMPLIFY, amplifier=fg.Amplifier(G, 0.0))
     got = g.numpy()[0, 0]
-    t0 = time.perf_counter()
+    fg.cd_compensation(g, fib, sc["spans"])
+    y = dsp.PhaseShiftEqualizer(3600).train_equalize(sym, dsp.rrc_sampling(g, osf, sc["roll_off"]))
+    q_gpu = float(dsp.q2_factor(sym, y, cut)[0])
+    be, se = dsp.error_counts(sym, y, cut)
+    codes = dsp.hd_sequence_16qam(y)[0, 0]
     ofib = cpu.Fiber(alpha, beta2, gamma, sc["span_m"], 1.55e-6, 1.0)
-    want, _ = cpu.ssfm_run(x[0, 0], sig.domain.time_step, ofib, cpu.UNIFORM, steps_per_span)
+    t0 = time.perf_counter()
+    xo = x[0, 0].copy()
+    for _ in range(sc["spans"]):
+        xo, _ = cpu.ssfm_run(xo, dt, ofib, cpu.UNIFORM, steps_per_span)
+        xo = cpu.amplify(xo, dt, F0, G, 0.0)
     t_cpu = time.perf_counter() - t0
-    out["field_rel_l2_one_span"] = float(np.linalg.norm(got - want) / np.linalg.norm(want))
-    out["cpu_oracle_one_thread"] = {"s_per_span": t_cpu,
-                                    "gsample_steps_per_s": n * steps_per_span / t_cpu / 1e9}
+    field_err = float(np.linalg.norm(got - xo) / np.linalg.norm(xo))
+    yo = cpu.rrc_sampling(cpu.cd_compensation(xo, dt, ofib, sc["spans"]), osf, sc["roll_off"])
+    tx = sym.numpy()[0, 0]
+    yo = cpu.rotate(yo, cpu.pse_estimate(tx, yo, 3600))
+    q_o = float(cpu.q2(tx, yo, cut))
+    out["link_vs_fp64_oracle"] = {
+        "field_rel_l2_after_10_spans": field_err, "q_db_gpu": q_gpu, "q_db_fp64": q_o,
+        "q_delta_db": q_gpu - q_o, "bit_errors_gpu": int(be[0]), "bit_errors_fp64": cpu.error_counts(tx, yo, cut)[0],
+        "decisions_equal": int(np.sum(codes == cpu.hd_sequence(yo))), "symbols": int(codes.size)}
+    out["cpu_oracle_one_thread"] = {"s_10_spans": t_cpu,
+                                    "gsample_steps_per_s": n * steps_per_span * sc["spans"] / t_cpu / 1e9}
     return out
 
 
@@ -986,7 +1006,7 @@ def main():
                     help="add the learned-vs-plain DBP launch-power sweep (-2..+4 dBm, 2^20 symbols per set; minutes)")
     ap.add_argument("--single-channel", action="store_true",
                     help="add the plain single-channel link (N=2^17, 10 x 80 km, 1 km steps): GPU throughput at "
-                         "batch 1 and 512, FP32 field error and single-thread FP64 oracle time for one span")
+                         "batch 1 and 512, then field, Q and decisions against the FP64 oracle (about 10 s of CPU)")
     ap.add_argument("--host-loop", action="store_true",
                     help="drive the spans from the host (one SSFM run + EDFA per span) instead of one graph")
     args = ap.parse_args()
