@@ -1,7 +1,7 @@
 """End-to-end chains on the GPU.
 
-Single channel (the single-channel configuration's chain at 2^11 symbols so
-the FP64 oracle finishes in seconds): 16QAM -> RRC 0.1 at 8 sps -> 10 x 80 km
+Single channel (the single-channel configuration's chain, at 2^11 symbols
+and at its own 2^14): 16QAM -> RRC 0.1 at 8 sps -> 10 x 80 km
 SSMF at 1 km uniform steps with lossless EDFAs (noise off) -> CDC -> matched
 filter -> phase-shift equalizer -> Q and BER, against the same chain in the
 FP64 oracle: field within 1e-5 relative L2, Q within 0.05 dB, decisions equal.
@@ -20,10 +20,13 @@ from conftest import ALPHA, BETA2, F0, GAMMA, rel_l2
 pytestmark = pytest.mark.gpu
 
 
-def test_single_channel_chain_matches_oracle(ctx, oracle_cpu):
+@pytest.mark.parametrize("log2_symbols", [11, 14])
+def test_single_channel_chain_matches_oracle(ctx, oracle_cpu, log2_symbols):
+    """2^11 symbols, and the configuration's own 2^14 (N = 2^17; the FP64
+    oracle takes a few seconds for its 800 steps)."""
     cpu = oracle_cpu
     rng = np.random.default_rng(1)
-    ns, osf, spans = 1 << 11, 8, 10
+    ns, osf, spans = 1 << log2_symbols, 8, 10
     dt = 1 / (32e9 * osf)
     p = fg.dbm_to_watts(2.0)
     codes = rng.integers(0, 16, ns)
