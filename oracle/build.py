@@ -4,8 +4,9 @@
   ``oracle/libfocss_oracle.so`` (gcc, portable flags, OpenMP over realizations).
   It runs on every machine that runs the tests or the CPU baseline.
 * ``build_ref()`` compiles the reference's own unmodified sources, where they
-  lie, together with the FFTW-API shim (``fftw_shim/``) and the C bridge
-  (``ref_bridge.cpp``) into ``oracle/_ref/libfocss_ref.so``.  It needs the
+  lie, together with the FFTW-API shim (``fftw_shim/``), the Armadillo
+  stand-in (``arma_shim/``) and the C bridges (``ref_bridge.cpp``,
+  ``ref_ppe_bridge.cpp``) into ``oracle/_ref/libfocss_ref.so``.  It needs the
   reference source tree, so it only runs where that tree exists; the outputs
   are git-ignored.  Reference sources are read in place, never copied.
 """
@@ -18,7 +19,10 @@ import sys
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("FOCSS_REFERENCE_ROOT", "/root/reference")
+# The reference tree: FOCSS_REFERENCE_ROOT, else a `reference` directory beside
+# this repository's root.
+REF_ROOT = os.environ.get("FOCSS_REFERENCE_ROOT",
+                          os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 ORACLE_SO = os.path.join(HERE, "libfocss_oracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_SO = os.path.join(REF_DIR, "libfocss_ref.so")
@@ -34,6 +38,11 @@ REF_SOURCES = [
     "focss/equalizer/phase_shift_equalizer.cpp",
     "focss/equalizer/scalar_equalizer.cpp",
     "tasks/verification.cpp",
+    # perturbation equalizers and the WDM scoring task's decision helpers,
+    # against the project's Armadillo stand-in (arma_shim/)
+    "focss/equalizer/sino.cpp",
+    "focss/equalizer/wdm_sino.cpp",
+    "tasks/wdm_scoring.cpp",
 ]
 
 
@@ -71,16 +80,17 @@ def build_ref(force: bool = False) -> str | None:
     src_root = os.path.join(REF_ROOT, "src")
     sources = [os.path.join(src_root, s) for s in REF_SOURCES]
     own = [os.path.join(HERE, "ref_bridge.cpp"), os.path.join(HERE, "fftw_shim", "fftw_shim.c"),
-           os.path.join(HERE, "fftw_shim", "fftw3.h"), os.path.join(HERE, "focss_oracle.c")]
+           os.path.join(HERE, "fftw_shim", "fftw3.h"), os.path.join(HERE, "focss_oracle.c"),
+           os.path.join(HERE, "ref_ppe_bridge.cpp"), os.path.join(HERE, "arma_shim", "armadillo")]
     if not (force or _stale(REF_SO, sources + own)):
         return REF_SO
     os.makedirs(REF_DIR, exist_ok=True)
     obj_dir = os.path.join(REF_DIR, "obj")
     os.makedirs(obj_dir, exist_ok=True)
     cxx = ["g++", "-std=c++11", "-O2", "-DNDEBUG", "-fPIC", "-ffp-contract=off",
-           "-I", src_root, "-I", os.path.join(HERE, "fftw_shim")]
+           "-I", src_root, "-I", os.path.join(HERE, "fftw_shim"), "-I", os.path.join(HERE, "arma_shim")]
     jobs = []
-    for s in sources + [own[0]]:
+    for s in sources + [own[0], own[4]]:
         o = os.path.join(obj_dir, os.path.basename(s).replace(".cpp", ".o"))
         jobs.append(cxx + ["-c", s, "-o", o])
     for s in (own[1], own[3]):

@@ -69,6 +69,14 @@ def lib():
             "ref_wdm_select": (None, [I, I, D, P, I, D]),
             "ref_wdm_mux": (None, [I, I, I, D, P, D, P]),
             "ref_soliton": (None, [I, I, D, P]),
+            "ref_sino_train": (None, [I, I, P, P, I, I, D, D, P, P, P]),
+            "ref_sino_cubic": (None, [I, I, P, I, P, P]),
+            "ref_sino_equalize": (None, [I, I, P, P, I, P, D, D, P]),
+            "ref_wdm_ppe_train": (None, [I, P, P, I, I, P, P, P, P]),
+            "ref_wdm_ppe_apply": (None, [I, P, P, P, I, P, I, P, D, D, I, P]),
+            "ref_find_certainty": (D, [I, I, P, P]),
+            "ref_certainty_sd": (None, [I, I, P, D, P]),
+            "ref_hd_rms": (None, [I, I, P, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -246,3 +254,84 @@ def load_transmission(path, modes, samples):
     rx = np.zeros((modes, samples), np.complex128)
     lib().ref_load_transmission(modes, samples, str(path).encode(), _p(tx), _p(rx))
     return tx, rx
+
+
+# ---- perturbation equalizers (sino.cpp, wdm_sino.cpp) and WDM scoring decisions
+def sino_train(tx, rx, radius, type_=0, linear_weight=0j):
+    """SINO::train (sino.cpp:42-159): returns (weights (2R+1)^2, intercept, linear weight)."""
+    tx, rx = _c(np.atleast_2d(tx)), _c(np.atleast_2d(rx))
+    m, n = _shape(tx)
+    W = np.zeros((2 * radius + 1, 2 * radius + 1), np.complex128)
+    ic = np.zeros(1, np.complex128)
+    lw = np.zeros(1, np.complex128)
+    lw0 = complex(linear_weight)
+    lib().ref_sino_train(m, n, _p(tx), _p(rx), radius, type_, lw0.real, lw0.imag, _p(W), _p(ic), _p(lw))
+    return W, ic[0], lw[0]
+
+
+def sino_cubic(a, radius, weights):
+    """SINO::cubic (sino.cpp:203-220) with the weight table W[R + m, R + n]."""
+    a = _c(np.atleast_2d(a))
+    m, n = _shape(a)
+    W = _c(weights)
+    o = np.zeros_like(a)
+    lib().ref_sino_cubic(m, n, _p(a), radius, _p(W), _p(o))
+    return o
+
+
+def sino_equalize(rx, tx, radius, weights, linear_weight):
+    rx, tx = _c(np.atleast_2d(rx)), _c(np.atleast_2d(tx))
+    m, n = _shape(rx)
+    W = _c(weights)
+    o = np.zeros_like(rx)
+    lw = complex(linear_weight)
+    lib().ref_sino_equalize(m, n, _p(rx), _p(tx), radius, _p(W), lw.real, lw.imag, _p(o))
+    return o
+
+
+def wdm_ppe_train(tx, rx, c_radius, d_radius):
+    """WdmPPE::train (wdm_sino.cpp:28-142) on 6 x N datasets: (C, D, intercept, linear weight)."""
+    tx, rx = _c(tx), _c(rx)
+    assert tx.shape[0] == 6 and rx.shape == tx.shape
+    C_ = np.zeros((2 * c_radius + 1, 2 * c_radius + 1), np.complex128)
+    D_ = np.zeros((2 * d_radius + 1, 2 * d_radius + 1), np.complex128)
+    ic = np.zeros(1, np.complex128)
+    lw = np.zeros(1, np.complex128)
+    lib().ref_wdm_ppe_train(tx.shape[1], _p(tx), _p(rx), c_radius, d_radius, _p(C_), _p(D_), _p(ic), _p(lw))
+    return C_, D_, ic[0], lw[0]
+
+
+WDM_SPM, WDM_XPM, WDM_CUBIC, WDM_MODEL, WDM_EQUALIZE, WDM_EQUALIZE3 = range(6)
+
+
+def wdm_ppe_apply(what, a, C_, D_, linear_weight, b=None, rx=None):
+    """WdmPPE spm / xpm / cubic / model / equalize (wdm_sino.cpp:235-300) with given tables."""
+    a = _c(a)
+    n = a.shape[1]
+    b = _c(b) if b is not None else a
+    rx = _c(rx) if rx is not None else a
+    C_, D_ = _c(C_), _c(D_)
+    o = np.zeros((2, n), np.complex128)
+    lw = complex(linear_weight)
+    lib().ref_wdm_ppe_apply(n, _p(a), _p(b), _p(rx), (C_.shape[0] - 1) // 2, _p(C_), (D_.shape[0] - 1) // 2,
+                            _p(D_), lw.real, lw.imag, what, _p(o))
+    return o
+
+
+def find_certainty(tx, rx):
+    tx, rx = _c(np.atleast_2d(tx)), _c(np.atleast_2d(rx))
+    return lib().ref_find_certainty(tx.shape[0], tx.shape[1], _p(tx), _p(rx))
+
+
+def certainty_sd(field, certainty):
+    f = _c(np.atleast_2d(field))
+    o = np.zeros_like(f)
+    lib().ref_certainty_sd(f.shape[0], f.shape[1], _p(f), certainty, _p(o))
+    return o
+
+
+def hd_rms(field):
+    f = _c(np.atleast_2d(field))
+    o = np.zeros_like(f)
+    lib().ref_hd_rms(f.shape[0], f.shape[1], _p(f), _p(o))
+    return o

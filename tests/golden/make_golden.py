@@ -1,8 +1,10 @@
 """Generate the golden vectors in tests/golden/*.npz from the reference's own
 sources (oracle/_ref: the unmodified focss sources compiled against the
-FFTW-API shim).  Run where the reference tree exists:
+FFTW-API shim and the Armadillo stand-in).  Run where the reference tree
+exists:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py              # both files
+    python tests/golden/make_golden.py --ppe-only   # ppe_golden.npz only
 
 Inputs are seeded synthetic signals shaped like the benchmark configurations
 (16QAM, RRC, SSMF) at sizes the FP64 CPU code finishes in seconds.
@@ -155,5 +157,78 @@ def main():
     print("wrote", len(g), "arrays")
 
 
+def main_ppe():
+    """Perturbation equalizers and certainty decisions, from the reference's own
+    sino.cpp, wdm_sino.cpp and wdm_scoring.cpp (compiled against the project's
+    Armadillo stand-in, whose least-squares solve is Householder QR)."""
+    assert ref.available(), "reference build unavailable"
+    rng = np.random.default_rng(20261204)
+    g = {}
+    pts = gray()
+
+    def cn(shape, s=1.0):
+        return s * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+
+    # SINO::cubic (sino.cpp:203-220) with random weights, 1 and 2 modes
+    R = 12
+    g["cubic_R"] = np.array([R])
+    g["cubic_w"] = cn((2 * R + 1, 2 * R + 1), 1e-2)
+    g["cubic_in1"] = pts[rng.integers(0, 16, (1, 400))] * 0.05
+    g["cubic_in2"] = pts[rng.integers(0, 16, (2, 400))] * 0.05
+    g["cubic_out1"] = ref.sino_cubic(g["cubic_in1"], R, g["cubic_w"])
+    g["cubic_out2"] = ref.sino_cubic(g["cubic_in2"], R, g["cubic_w"])
+    g["sino_eq_lw"] = np.array([0.93 + 0.07j])
+    g["sino_eq_rx"] = g["cubic_in1"] * 0.9 + cn((1, 400), 1e-3)
+    g["sino_eq_out"] = ref.sino_equalize(g["sino_eq_rx"], g["cubic_in1"], R, g["cubic_w"], g["sino_eq_lw"][0])
+
+    # SINO::train (sino.cpp:42-159): a synthetic link with known coefficients
+    Rt, N = 8, 3000
+    w_true = cn((2 * Rt + 1, 2 * Rt + 1), 2e-3)
+    for modes in (1, 2):
+        tx = pts[rng.integers(0, 16, (modes, N))]
+        rx = (0.9 + 0.1j) * tx + ref.sino_cubic(tx, Rt, w_true) + cn((modes, N), 0.01)
+        g["train%d_tx" % modes] = tx
+        g["train%d_rx" % modes] = rx
+        for t in (0, 1, 2):
+            if modes == 2 and t != 0:
+                continue
+            W, ic, lw = ref.sino_train(tx, rx, Rt, t, 0.9 + 0.1j)
+            g["train%d_t%d_w" % (modes, t)] = W
+            g["train%d_t%d_ic_lw" % (modes, t)] = np.array([ic, lw])
+    g["train_R"] = np.array([Rt])
+
+    # WdmPPE::train and its operators (wdm_sino.cpp:28-300), (c, d) = (8, 2)
+    c, d, N = 8, 2, 1500
+    tx6 = pts[rng.integers(0, 16, (6, N))] * 0.1
+    rx6 = 0.95 * tx6 + cn((6, N), 2e-3)
+    rx6[2:4] += 50.0 * ref.wdm_ppe_apply(ref.WDM_CUBIC, tx6, cn((2 * c + 1, 2 * c + 1), 1e-1),
+                                         cn((2 * d + 1, 2 * d + 1), 1e-1), 1.0)
+    g["wdm_tx"], g["wdm_rx"] = tx6, rx6
+    C_, D_, ic, lw = ref.wdm_ppe_train(tx6, rx6, c, d)
+    g["wdm_C"], g["wdm_D"], g["wdm_ic_lw"] = C_, D_, np.array([ic, lw])
+    test6 = pts[rng.integers(0, 16, (6, N))] * 0.1
+    rxt = 0.95 * test6 + cn((6, N), 2e-3)
+    g["wdm_test"], g["wdm_test_rx"] = test6, rxt
+    for name, what in (("spm", ref.WDM_SPM), ("xpm", ref.WDM_XPM), ("cubic", ref.WDM_CUBIC),
+                       ("model", ref.WDM_MODEL), ("eq", ref.WDM_EQUALIZE)):
+        g["wdm_" + name] = ref.wdm_ppe_apply(what, test6, C_, D_, lw, rx=rxt)
+    g["wdm_eq3"] = ref.wdm_ppe_apply(ref.WDM_EQUALIZE3, test6, C_, D_, lw, b=rxt, rx=rxt)
+
+    # find_certainty / sd / hd (wdm_scoring.cpp:105-156) on a noisy 2 x N matrix
+    txc = pts[rng.integers(0, 16, (2, 2000))] * 0.3
+    rxc = txc + cn((2, 2000), 0.045)
+    g["cert_tx"], g["cert_rx"] = txc, rxc
+    cert = ref.find_certainty(txc, rxc)
+    g["cert"] = np.array([cert])
+    g["cert_sd"] = ref.certainty_sd(rxc, cert)
+    g["cert_sd_05"] = ref.certainty_sd(rxc, 0.5)
+    g["cert_hd"] = ref.hd_rms(rxc)
+
+    np.savez_compressed(os.path.join(OUT, "ppe_golden.npz"), **g)
+    print("wrote", len(g), "PPE arrays; certainty", cert)
+
+
 if __name__ == "__main__":
-    main()
+    if "--ppe-only" not in sys.argv:
+        main()
+    main_ppe()
