@@ -283,6 +283,33 @@ class SSFM:
                                    steps.ctypes.data_as(C.c_void_p)), field.ctx.h)
         return steps
 
+    def run_recorded(self, field: Field, direction: float = FORWARD, capacity: int = 1 << 16):
+        """run() that also returns each realization's step sizes: (steps,
+        [array of |h_i| per realization]) (focss_ssfm_run_record)."""
+        steps = np.zeros(field.batch, np.int32)
+        hs = np.zeros((field.batch, capacity))
+        fb, op = self.fiber.c(), self.opts()
+        check(lib().focss_ssfm_run_record(field.ctx.h, field.h, C.byref(fb), C.byref(op), direction, capacity,
+                                          hs.ctypes.data_as(C.c_void_p), steps.ctypes.data_as(C.c_void_p)),
+              field.ctx.h)
+        return steps, [hs[b, :steps[b]].copy() for b in range(field.batch)]
+
+    def run_steps(self, field: Field, steps_h, direction: float = FORWARD):
+        """Propagate with the given step sizes (one sequence per realization)
+        instead of the grid rule (focss_ssfm_run_steps)."""
+        if len(steps_h) != field.batch:
+            raise FocssError(1, "run_steps: one step list per realization")
+        cap = max(len(h) for h in steps_h)
+        buf = np.zeros((field.batch, cap))
+        n = np.zeros(field.batch, np.int32)
+        for b, h in enumerate(steps_h):
+            buf[b, :len(h)] = h
+            n[b] = len(h)
+        fb = self.fiber.c()
+        check(lib().focss_ssfm_run_steps(field.ctx.h, field.h, C.byref(fb), buf.ctypes.data_as(C.c_void_p),
+                                         n.ctypes.data_as(C.c_void_p), cap, direction), field.ctx.h)
+        return n
+
 
 class Amplifier:
     """src/focss/module/amplifier.h:7-22 (ASE from a seeded counter-based stream)."""

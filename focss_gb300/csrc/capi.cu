@@ -1,4 +1,5 @@
 // capi.cu -- the extern "C" boundary (include/focss_gpu.h) over the kernels.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -425,6 +426,74 @@ FOCSS_API focss_status focss_ssfm_run(focss_ctx* c, focss_field* f, const focss_
     if (direction != 1.0 && direction != -1.0)
         return fg::set_error(c, FOCSS_ERR_INVALID_ARG, "direction must be FOCSS_FORWARD or FOCSS_BACKWARD");
     return fg::ssfm_run(c, f, *fiber, *opts, direction, steps_out);
+}
+
+// Step-grid record / replay: device copies of the step lists live in scratch
+// slot 9 (sizes) and 10 (counts).
+FOCSS_API focss_status focss_ssfm_run_record(focss_ctx* c, focss_field* f, const focss_fiber* fiber,
+                                             const focss_ssfm_opts* opts, double direction, int capacity,
+                                             double* steps_h, int* steps_out) {
+    if (!c || !f || !fiber || !opts || !steps_h || capacity <= 0) return FOCSS_ERR_INVALID_ARG;
+    if (f->ctx != c) return fg::set_error(c, FOCSS_ERR_INVALID_ARG, "field belongs to another context");
+    if (direction != 1.0 && direction != -1.0)
+        return fg::set_error(c, FOCSS_ERR_INVALID_ARG, "direction must be FOCSS_FORWARD or FOCSS_BACKWARD");
+    const size_t n = (size_t)f->batch * capacity;
+    double* d_h = (double*)fg::scratch_buffer(c, 9, sizeof(double) * n);
+    if (!d_h) return fg::set_error(c, FOCSS_ERR_OOM, "ssfm_run_record: step buffer");
+    fg::StepGrid g;
+    g.record = d_h;
+    g.cap = capacity;
+    std::vector<int> rec(f->batch);
+    focss_status st = fg::ssfm_run(c, f, *fiber, *opts, direction, steps_out, &g, rec.data());
+    if (st != FOCSS_OK) return st;
+    for (int b = 0; b < f->batch; ++b)
+        if (rec[b] > capacity)
+            return fg::set_error(c, FOCSS_ERR_INVALID_ARG,
+                                 "ssfm_run_record: realization " + std::to_string(b) + " took " +
+                                     std::to_string(rec[b]) + " steps, more than the capacity " +
+                                     std::to_string(capacity));
+    st = fg::cuda_check(c, cudaMemcpyAsync(steps_h, d_h, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream),
+                        "ssfm_run_record: readback");
+    if (st != FOCSS_OK) return st;
+    return fg::cuda_check(c, cudaStreamSynchronize(c->stream), "ssfm_run_record: sync");
+}
+
+FOCSS_API focss_status focss_ssfm_run_steps(focss_ctx* c, focss_field* f, const focss_fiber* fiber,
+                                            const double* steps_h, const int* n_steps, int capacity,
+                                            double direction) {
+    if (!c || !f || !fiber || !steps_h || !n_steps || capacity <= 0) return FOCSS_ERR_INVALID_ARG;
+    if (f->ctx != c) return fg::set_error(c, FOCSS_ERR_INVALID_ARG, "field belongs to another context");
+    if (direction != 1.0 && direction != -1.0)
+        return fg::set_error(c, FOCSS_ERR_INVALID_ARG, "direction must be FOCSS_FORWARD or FOCSS_BACKWARD");
+    int max_steps = 0;
+    for (int b = 0; b < f->batch; ++b) {
+        if (n_steps[b] < 1 || n_steps[b] > capacity)
+            return fg::set_error(c, FOCSS_ERR_INVALID_ARG, "ssfm_run_steps: step counts must be in [1, capacity]");
+        for (int i = 0; i < n_steps[b]; ++i) {
+            const double h = steps_h[(size_t)b * capacity + i];
+            if (!(h > 0) || !(h < 1e300))
+                return fg::set_error(c, FOCSS_ERR_INVALID_ARG, "ssfm_run_steps: step sizes must be finite and > 0");
+        }
+        max_steps = std::max(max_steps, n_steps[b]);
+    }
+    const size_t n = (size_t)f->batch * capacity;
+    double* d_h = (double*)fg::scratch_buffer(c, 9, sizeof(double) * n);
+    int* d_n = (int*)fg::scratch_buffer(c, 10, sizeof(int) * (size_t)f->batch);
+    if (!d_h || !d_n) return fg::set_error(c, FOCSS_ERR_OOM, "ssfm_run_steps: step buffer");
+    focss_status st = fg::cuda_check(
+        c, cudaMemcpyAsync(d_h, steps_h, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream), "steps upload");
+    if (st != FOCSS_OK) return st;
+    st = fg::cuda_check(c, cudaMemcpyAsync(d_n, n_steps, sizeof(int) * f->batch, cudaMemcpyHostToDevice, c->stream),
+                        "step counts upload");
+    if (st != FOCSS_OK) return st;
+    fg::StepGrid g;
+    g.replay = d_h;
+    g.count = d_n;
+    g.cap = capacity;
+    g.max_steps = max_steps;
+    // the grid rule is replaced; ADAPTIVE bookkeeping reports the counts
+    focss_ssfm_opts o{FOCSS_ADAPTIVE, 0, 1.0, 1.0};
+    return fg::ssfm_run(c, f, *fiber, o, direction, nullptr, &g, nullptr);
 }
 
 FOCSS_API focss_status focss_amplifier_apply(focss_ctx* c, focss_field* f, double gain, double noise_factor,

@@ -32,6 +32,7 @@ struct SsfmState {
     unsigned int peak_bits;        // atomicMax accumulator of the peak power (float bits)
     unsigned int blocks_done;      // last-block ticket
     float kerr_coef;               // (float)(kappa*gamma*h) of the next nonlinear step
+    int recorded;                  // step sizes written to SsfmParams::h_record so far
 };
 
 enum ColOp : int { COL_FWD = 0, COL_KERR = 1, COL_INV = 2, COL_IDLE = 3 };
@@ -45,6 +46,14 @@ struct SsfmParams {
     int grid, total_steps;
     int samples;
     int* n_done;
+    // Step-grid record / replay (both null on ordinary runs).  Realization b
+    // writes |h_i| of its nonlinear steps to h_record[b*h_cap + i] (i < h_cap;
+    // SsfmState::recorded counts them all), or takes the h_count[b] step sizes
+    // h_replay[b*h_cap + i] instead of its grid's rule.
+    double* h_record;
+    const double* h_replay;
+    const int* h_count;
+    int h_cap;
 };
 
 // Twiddle tables, double-float {re_hi, im_hi, re_lo, im_lo}, packed in one
@@ -136,8 +145,16 @@ void* scratch_buffer(Ctx* ctx, int slot, size_t bytes);
 bool fft_size_supported(int N);
 cudaError_t launch_col(const Plan& p, PassArgs a, int batch, cudaStream_t s);
 cudaError_t launch_row(const Plan& p, PassArgs a, int batch, cudaStream_t s);
+// Step-grid record / replay of one ssfm_run: device arrays as in SsfmParams.
+struct StepGrid {
+    double* record = nullptr;
+    const double* replay = nullptr;
+    const int* count = nullptr;
+    int cap = 0;
+    int max_steps = 0;  // replay: the largest entry of count
+};
 focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ssfm_opts& o, double dir,
-                      int* steps_out);
+                      int* steps_out, const StepGrid* grid = nullptr, int* recorded_out = nullptr);
 // Argument checks of ssfm_run and the pass arguments of one run (state and
 // finished-realization counter supplied by the caller).
 focss_status ssfm_validate(Ctx* ctx, const Field* f, const focss_fiber& fib, const focss_ssfm_opts& o);

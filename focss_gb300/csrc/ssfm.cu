@@ -22,6 +22,7 @@
 // product, so the FP32 sincospi argument is already range-reduced to [-1, 1).
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 
 #include "ssfm_kernels.cuh"
 
@@ -82,27 +83,43 @@ bool fft_size_supported(int N) {
     return lg >= 8 && lg <= 20;
 }
 
-// Opt the kernel in to `smem` bytes of dynamic shared memory (once per size).
-cudaError_t prepare(Launch& l, size_t smem) {
-    if (l.attr_set && smem <= l.smem) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute((const void*)l.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+// Launch descriptions per device and FFT length: the dynamic shared-memory
+// opt-in (cudaFuncSetAttribute) applies to the current device only, so each
+// device keeps its own record of it.
+constexpr int kMaxDevices = 64;
+std::mutex g_launch_mutex;
+
+// The cached launch of pass kind `kind` (0 column, 1 row) for log2 length lg
+// on the current device, opted in to `smem` bytes of dynamic shared memory.
+cudaError_t cached_launch(int kind, int lg, size_t smem, Launch* out) {
+    static Launch cache[kMaxDevices][2][16];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    l.attr_set = true;
-    l.smem = smem;
+    if (dev < 0 || dev >= kMaxDevices || lg < 0 || lg >= 16) return cudaErrorInvalidValue;
+    std::lock_guard<std::mutex> lock(g_launch_mutex);
+    Launch& l = cache[dev][kind][lg];
+    if (!l.fn) l = kind == 0 ? col_launch_for(lg) : row_launch_for(lg);
+    if (!l.fn) return cudaErrorInvalidValue;
+    if (!l.attr_set || smem > l.smem) {
+        e = cudaFuncSetAttribute((const void*)l.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        l.attr_set = true;
+        l.smem = smem;
+    }
+    *out = l;
     return cudaSuccess;
 }
 
 cudaError_t launch_col(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
-    static Launch cache[16];
-    Launch& l = cache[p.log2N1];
-    if (!l.fn) l = col_launch_for(p.log2N1);
+    Launch l = col_launch_for(p.log2N1);
     if (!l.fn) return cudaErrorInvalidValue;
     const int modes = a.modes > 1 ? a.modes : 1;
     // s_fc (N1) + six-step table (Q x C, Q = N1/P) + exchange (N1 x C per mode)
     const int P = l.threads / l.per_block;
     const size_t smem = sizeof(float4) * ((size_t)p.N1 + (size_t)(p.N1 / P) * l.per_block) +
                         sizeof(float2) * (size_t)p.N1 * l.per_block * modes;
-    cudaError_t e = prepare(l, smem);
+    cudaError_t e = cached_launch(0, p.log2N1, smem, &l);
     if (e != cudaSuccess) return e;
     a.N = p.N;
     a.N1 = p.N1;
@@ -117,15 +134,13 @@ cudaError_t launch_col(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
 }
 
 cudaError_t launch_row(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
-    static Launch cache[16];
-    Launch& l = cache[p.log2N2];
-    if (!l.fn) l = row_launch_for(p.log2N2);
+    Launch l = row_launch_for(p.log2N2);
     if (!l.fn) return cudaErrorInvalidValue;
     const int P = l.threads / l.per_block;
     const int Q = p.N2 / P;
     int R = l.per_block;
     const size_t smem = sizeof(float4) * ((size_t)p.N2 + 512) + sizeof(float2) * (size_t)R * Q * (P + 1);
-    cudaError_t e = prepare(l, smem);
+    cudaError_t e = cached_launch(1, p.log2N2, smem, &l);
     if (e != cudaSuccess) return e;
     a.N = p.N;
     a.N1 = p.N1;
@@ -222,10 +237,10 @@ bool ssfm_single_cta(const Ctx* ctx, const Field* f) {
     return it != ctx->ssfm_split.end() && it->second == kSingleCta && f->modes == 1 && block_split(f->samples) != 0;
 }
 
-focss_status ssfm_finish(Ctx* ctx, Field* f, const focss_ssfm_opts& o, int* steps_out);
+focss_status ssfm_finish(Ctx* ctx, Field* f, const focss_ssfm_opts& o, int* steps_out, int* recorded_out);
 
 focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ssfm_opts& o, double dir,
-                      int* steps_out) {
+                      int* steps_out, const StepGrid* grid, int* recorded_out) {
     focss_status st = ssfm_validate(ctx, f, fib, o);
     if (st != FOCSS_OK) return st;
     const Plan* p = nullptr;
@@ -238,11 +253,21 @@ focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ss
     if (st != FOCSS_OK) return st;
     st = cuda_check(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(int) * 4, s), "memset counters");
     if (st != FOCSS_OK) return st;
-    const PassArgs a = ssfm_args(f, fib, o, dir, ctx->d_state, ctx->d_counters);
+    PassArgs a = ssfm_args(f, fib, o, dir, ctx->d_state, ctx->d_counters);
+    if (grid) {
+        a.prm.h_record = grid->record;
+        a.prm.h_replay = grid->replay;
+        a.prm.h_count = grid->count;
+        a.prm.h_cap = grid->cap;
+    }
+    const bool replay = grid && grid->replay;
 
-    // Upper bound on column passes: UNIFORM is exact; the others are polled.
+    // Upper bound on column passes: UNIFORM and replayed grids are exact; the
+    // others are polled.
     long long cap;
-    if (o.grid == FOCSS_UNIFORM) {
+    if (replay) {
+        cap = (long long)grid->max_steps + 2;
+    } else if (o.grid == FOCSS_UNIFORM) {
         cap = (long long)o.total_steps + 2;
     } else {
         cap = 1ll << 17;  // ~100x the step count of a 0.005 rad/step span at +11 dBm
@@ -250,21 +275,22 @@ focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ss
     if (ssfm_single_cta(ctx, f)) {
         st = cuda_check(ctx, launch_block(*p, a, f->batch, (int)std::min<long long>(cap, 1 << 30), s), "ssfm block");
         if (st != FOCSS_OK) return st;
-        st = ssfm_finish(ctx, f, o, steps_out);
+        st = ssfm_finish(ctx, f, o, steps_out, recorded_out);
         // the kernel stops a realization at the cap, leaving it unfinished
         return st == FOCSS_ERR_TIMEOUT ? set_error(ctx, FOCSS_ERR_NOT_CONVERGED, "ssfm_run: step cap reached") : st;
     }
+    const bool fixed = replay || o.grid == FOCSS_UNIFORM;  // pass count known up front
     const int chunk = 16;
     long long launched = 0;
     bool done = false;
     cudaEvent_t ev = nullptr;
-    if (o.grid != FOCSS_UNIFORM) {
+    if (!fixed) {
         st = cuda_check(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
         if (st != FOCSS_OK) return st;
     }
     bool pending = false;
     while (!done) {
-        const long long n = (o.grid == FOCSS_UNIFORM) ? cap : chunk;
+        const long long n = fixed ? cap : chunk;
         for (long long i = 0; i < n; ++i) {
             cudaError_t e = cudaSuccess;
             if (ctx->profiling) {
@@ -285,7 +311,7 @@ focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ss
             }
         }
         launched += n;
-        if (o.grid == FOCSS_UNIFORM) break;
+        if (fixed) break;
         // Double-buffered poll: queue the next chunk before waiting on this one.
         if (pending) {
             cudaError_t e = cudaEventSynchronize(ev);
@@ -306,12 +332,12 @@ focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ss
         }
     }
     if (ev) cudaEventDestroy(ev);
-    return ssfm_finish(ctx, f, o, steps_out);
+    return ssfm_finish(ctx, f, o, steps_out, recorded_out);
 }
 
 // Reads the step states back after a run: every realization must be idle;
-// steps_out gets the step counts.
-focss_status ssfm_finish(Ctx* ctx, Field* f, const focss_ssfm_opts& o, int* steps_out) {
+// steps_out gets the step counts, recorded_out the recorded step-size counts.
+focss_status ssfm_finish(Ctx* ctx, Field* f, const focss_ssfm_opts& o, int* steps_out, int* recorded_out) {
     cudaStream_t s = ctx->stream;
     focss_status st;
     std::vector<SsfmState> hs(f->batch);
@@ -327,6 +353,7 @@ focss_status ssfm_finish(Ctx* ctx, Field* f, const focss_ssfm_opts& o, int* step
         if (hs[b].action != COL_IDLE)
             return set_error(ctx, FOCSS_ERR_TIMEOUT, "ssfm_run: a realization did not finish");
         if (steps_out) steps_out[b] = (o.grid == FOCSS_ADAPTIVE) ? hs[b].steps : hs[b].n_steps;
+        if (recorded_out) recorded_out[b] = hs[b].recorded;
     }
     return FOCSS_OK;
 }

@@ -44,7 +44,12 @@ __device__ __forceinline__ void turns_fix96(double a, unsigned long long& hi, un
     }
 }
 
-__device__ __noinline__ static void ssfm_advance(SsfmState& s, const SsfmParams& p, int op_done, float peak,
+// Step i (0-based) of realization b on a replayed grid, signed by the direction.
+__device__ __forceinline__ double replay_step(const SsfmParams& p, int b, int i) {
+    return p.direction * p.h_replay[(size_t)b * p.h_cap + i];
+}
+
+__device__ __noinline__ static void ssfm_advance(SsfmState& s, const SsfmParams& p, int b, int op_done, float peak,
                                                 double sum) {
     if (op_done == COL_INV) {
         s.action = COL_IDLE;
@@ -58,7 +63,14 @@ __device__ __noinline__ static void ssfm_advance(SsfmState& s, const SsfmParams&
         s.index = 0;
         s.steps = 1;
         s.gain_ratio = 1.0;
-        if (p.grid == FOCSS_UNIFORM) {
+        s.recorded = 0;
+        if (p.h_replay) {
+            const int n = p.h_count[b];
+            s.n_steps = n;
+            s.steps = n;
+            s.h = replay_step(p, b, 0);
+            s.final_step = n == 1;
+        } else if (p.grid == FOCSS_UNIFORM) {
             s.n_steps = p.total_steps;
             s.h = p.direction * (p.length / p.total_steps);
             s.final_step = p.total_steps == 1;
@@ -94,7 +106,11 @@ __device__ __noinline__ static void ssfm_advance(SsfmState& s, const SsfmParams&
         } else {
             double next;
             int fin;
-            if (p.grid == FOCSS_UNIFORM) {
+            if (p.h_replay) {
+                const int i = ++s.index;
+                next = replay_step(p, b, i);
+                fin = (i == s.n_steps - 1);
+            } else if (p.grid == FOCSS_UNIFORM) {
                 const int i = ++s.index;
                 next = s.h;
                 fin = (i == s.n_steps - 1);
@@ -118,6 +134,11 @@ __device__ __noinline__ static void ssfm_advance(SsfmState& s, const SsfmParams&
             s.h = next;
             s.final_step = fin;
         }
+    }
+    if (p.h_record && s.action == COL_KERR) {
+        // the nonlinear step about to be taken (s.h) is step s.recorded
+        if (s.recorded < p.h_cap) p.h_record[(size_t)b * p.h_cap + s.recorded] = fabs(s.h);
+        s.recorded++;
     }
     s.hl = hl;
     const double a = 0.5 * p.beta2 * hl * p.dw * p.dw / (2.0 * 3.14159265358979323846);
@@ -293,7 +314,7 @@ __global__ void __launch_bounds__(2 * C * ColFFT<N1>::P, 1) col_kernel(const Pas
                 __threadfence();
                 const float peak = __uint_as_float(atomicOr(&st->peak_bits, 0u));
                 const double sum = atomicAdd(&st->sum, 0.0);
-                ssfm_advance(*st, a.prm, op, peak, sum);
+                ssfm_advance(*st, a.prm, b, op, peak, sum);
                 st->peak_bits = 0u;
                 st->sum = 0.0;
                 st->blocks_done = 0u;
@@ -487,7 +508,7 @@ __global__ void __launch_bounds__(kBlockThreads, BlockShape<N1, N2>::SMEM <= 113
             __syncthreads();
         }
         block_max_sum(pk, sm, red);
-        if (threadIdx.x == 0) ssfm_advance(*st, a.prm, op, pk, (double)sm);
+        if (threadIdx.x == 0) ssfm_advance(*st, a.prm, blockIdx.x, op, pk, (double)sm);
         __syncthreads();
         if (*(volatile const int*)&st->row_active) {
             const float g = *(volatile const float*)&st->lin_gain;

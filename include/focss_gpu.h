@@ -149,6 +149,31 @@ FOCSS_API focss_status focss_field_ifft(focss_field* field);
 FOCSS_API focss_status focss_ssfm_run(focss_ctx* ctx, focss_field* field, const focss_fiber* fiber,
                                       const focss_ssfm_opts* opts, double direction, int* steps_out);
 
+/* Step-grid record and replay.  The reference has no counterpart: SSFM::run
+ * only prints the adaptive step count (src/focss/solver/ssfm.cpp:117).  An
+ * ADAPTIVE grid takes each step size from the current field's peak power
+ * (:92-118, :136-140), so two runs that differ in rounding walk slightly
+ * different grids; recording one run's grid and replaying it in another (or in
+ * an FP64 oracle) puts both on the same grid.
+ * focss_ssfm_run_record: focss_ssfm_run that also writes the nonlinear step
+ * sizes |h_i| (metres, in order) of realization b to steps_h[b*capacity + i]
+ * (host array of batch*capacity doubles; steps_out as focss_ssfm_run).
+ * Returns FOCSS_ERR_INVALID_ARG after the run when a realization took more
+ * than `capacity` steps.
+ * focss_ssfm_run_steps: SSFM::run with the given step sizes in place of a
+ * grid rule.  Realization b takes n_steps[b] (1..capacity) steps of size
+ * h_i = steps_h[b*capacity + i] (> 0; their sum is the distance covered) in
+ * the Strang pattern of the ADAPTIVE grid: L(h_0/2) N(h_0) L(h_0/2) ...
+ * N(h_last) L(h_last/2), with the fiber's loss, dispersion and Kerr
+ * coefficients.  Replaying a recorded grid on the GPU repeats the recorded
+ * run's arithmetic bit for bit. */
+FOCSS_API focss_status focss_ssfm_run_record(focss_ctx* ctx, focss_field* field, const focss_fiber* fiber,
+                                             const focss_ssfm_opts* opts, double direction, int capacity,
+                                             double* steps_h, int* steps_out);
+FOCSS_API focss_status focss_ssfm_run_steps(focss_ctx* ctx, focss_field* field, const focss_fiber* fiber,
+                                            const double* steps_h, const int* n_steps, int capacity,
+                                            double direction);
+
 /* ------------------------------------------------------------- amplifier */
 /* Amplifier::amplify / add_noise / give_power / drop_power
  * (src/focss/module/amplifier.cpp:15-42).  `gain` and `noise_factor` are the

@@ -42,6 +42,8 @@ def lib():
             "ofc_field_fft": (None, [I, I, P]),
             "ofc_field_ifft": (None, [I, I, P]),
             "ofc_ssfm_run": (I, [I, I, D, P, C.POINTER(Fiber), I, I, D, D, D]),
+            "ofc_ssfm_run_rec": (I, [I, I, D, P, C.POINTER(Fiber), I, I, D, D, D, P, I]),
+            "ofc_ssfm_run_steps": (I, [I, I, D, P, C.POINTER(Fiber), P, I, D]),
             "ofc_cd_compensation": (None, [I, I, D, P, C.POINTER(Fiber), I]),
             "ofc_amplify": (None, [I, I, D, D, P, D, D, C.c_uint64, C.c_uint64, I]),
             "ofc_add_noise": (None, [I, I, D, D, P, D, D, C.c_uint64, C.c_uint64, I]),
@@ -142,6 +144,30 @@ def ssfm_run(a, dt, fiber, grid=UNIFORM, total_steps=1, max_phase_shift=0.0,
     steps = lib().ofc_ssfm_run(m, n, dt, _ptr(a), C.byref(fiber), grid, total_steps,
                                max_phase_shift, max_step_size, direction)
     return a, steps
+
+
+def ssfm_run_recorded(a, dt, fiber, grid=UNIFORM, total_steps=1, max_phase_shift=0.0,
+                      max_step_size=0.0, direction=FORWARD, capacity=1 << 16):
+    """ssfm_run that also returns the step sizes |h_i| taken: (field, steps, h)."""
+    a = _c128(a).copy()
+    m, n = _shape(a)
+    h = np.zeros(capacity)
+    steps = lib().ofc_ssfm_run_rec(m, n, dt, _ptr(a), C.byref(fiber), grid, total_steps,
+                                   max_phase_shift, max_step_size, direction, _ptr(h), capacity)
+    if steps > capacity:
+        raise ValueError("ssfm_run_recorded: %d steps exceed the capacity %d" % (steps, capacity))
+    return a, steps, h[:steps].copy()
+
+
+def ssfm_run_steps(a, dt, fiber, h, direction=FORWARD):
+    """The ADAPTIVE loop (ssfm.cpp:92-118) on the given step sizes h."""
+    a = _c128(a).copy()
+    m, n = _shape(a)
+    h = np.ascontiguousarray(h, dtype=np.float64)
+    if h.size < 1:
+        raise ValueError("ssfm_run_steps: at least one step")
+    lib().ofc_ssfm_run_steps(m, n, dt, _ptr(a), C.byref(fiber), _ptr(h), h.size, direction)
+    return a
 
 
 def cd_compensation(a, dt, fiber, spans):

@@ -225,17 +225,59 @@ static int logarithmic_steps(const ssfm_ctx* c, const double* a) {
     return minimum > estimated ? minimum : estimated;
 }
 
-int ofc_ssfm_run(int modes, int samples, double dt, double* a,
-                 const ofc_fiber* fiber, int grid, int total_steps,
-                 double max_phase_shift, double max_step_size,
-                 double direction) {
+static double* dispersion_cache(int samples, double dt) {
     /* ssfm.cpp:39-60: dispersion cache omega_k^2 in FFT order */
     double freq_step = 2.0 * REF_PI / (dt * samples);
     double* disp = (double*)malloc(sizeof(double) * (size_t)samples);
     for (int i = 0; i <= samples / 2; ++i) disp[i] = (double)i * freq_step;
     for (int i = samples / 2 + 1; i < samples; ++i) disp[i] = (double)(i - samples) * freq_step;
     for (int i = 0; i < samples; ++i) disp[i] *= disp[i];
+    return disp;
+}
 
+static void record_step(double* h_out, int h_cap, int i, double step) {
+    if (h_out && i < h_cap) h_out[i] = step;
+}
+
+int ofc_ssfm_run(int modes, int samples, double dt, double* a,
+                 const ofc_fiber* fiber, int grid, int total_steps,
+                 double max_phase_shift, double max_step_size,
+                 double direction) {
+    return ofc_ssfm_run_rec(modes, samples, dt, a, fiber, grid, total_steps, max_phase_shift,
+                            max_step_size, direction, NULL, 0);
+}
+
+int ofc_ssfm_run_steps(int modes, int samples, double dt, double* a,
+                       const ofc_fiber* fiber, const double* h, int n_steps,
+                       double direction) {
+    /* The ADAPTIVE loop of ssfm.cpp:92-118 with its step sizes taken from h
+     * instead of next_adaptive_step: the same operations in the same order, so
+     * replaying an ADAPTIVE run's recorded steps reproduces it bit for bit. */
+    double* disp = dispersion_cache(samples, dt);
+    ssfm_ctx c = {modes, samples, fiber, disp, 0.0, 0.0};
+    ofc_field_fft(modes, samples, a);
+    for (int i = 0; i + 1 < n_steps; ++i) {
+        double step = h[i];
+        nofft_linear_step(&c, a, 0.5 * step * direction);
+        ofc_field_ifft(modes, samples, a);
+        nonlinear_step(&c, a, step * direction);
+        ofc_field_fft(modes, samples, a);
+        nofft_linear_step(&c, a, 0.5 * step * direction);
+    }
+    double step = h[n_steps - 1];
+    nofft_linear_step(&c, a, 0.5 * step * direction);
+    fft_nonlinear_step(&c, a, step * direction);
+    nofft_linear_step(&c, a, 0.5 * step * direction);
+    ofc_field_ifft(modes, samples, a);
+    free(disp);
+    return n_steps;
+}
+
+int ofc_ssfm_run_rec(int modes, int samples, double dt, double* a,
+                     const ofc_fiber* fiber, int grid, int total_steps,
+                     double max_phase_shift, double max_step_size,
+                     double direction, double* h_out, int h_cap) {
+    double* disp = dispersion_cache(samples, dt);
     ssfm_ctx c = {modes, samples, fiber, disp, max_phase_shift, max_step_size};
     int steps = 0;
     if (grid == OFC_UNIFORM) {
@@ -244,6 +286,7 @@ int ofc_ssfm_run(int modes, int samples, double dt, double* a,
         step = direction * step;
         linear_step(&c, a, 0.5 * step);
         for (int i = 0; i < total_steps; ++i) {
+            record_step(h_out, h_cap, i, fabs(step));
             nonlinear_step(&c, a, step);
             linear_step(&c, a, step);
         }
@@ -258,6 +301,7 @@ int ofc_ssfm_run(int modes, int samples, double dt, double* a,
         ofc_field_fft(modes, samples, a);
         for (int i = 0; i < n_steps; ++i) {
             double step = inv_alpha * log(1 + inv_gain / (1 + inv_gain * i));
+            record_step(h_out, h_cap, i, fabs(step));
             nofft_linear_step(&c, a, 0.5 * step);
             fft_nonlinear_step(&c, a, step);
             nofft_linear_step(&c, a, 0.5 * step);
@@ -272,6 +316,7 @@ int ofc_ssfm_run(int modes, int samples, double dt, double* a,
         int steps_done = 1;
         ofc_field_fft(modes, samples, a);
         while (distance + step < fiber->length) {
+            record_step(h_out, h_cap, steps_done - 1, step);
             nofft_linear_step(&c, a, 0.5 * step * direction);
             ofc_field_ifft(modes, samples, a);
             nonlinear_step(&c, a, step * direction);
@@ -283,6 +328,7 @@ int ofc_ssfm_run(int modes, int samples, double dt, double* a,
             steps_done++;
         }
         step = fiber->length - distance;
+        record_step(h_out, h_cap, steps_done - 1, step);
         nofft_linear_step(&c, a, 0.5 * step * direction);
         fft_nonlinear_step(&c, a, step * direction);
         nofft_linear_step(&c, a, 0.5 * step * direction);

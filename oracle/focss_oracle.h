@@ -50,6 +50,17 @@ int ofc_ssfm_run(int modes, int samples, double dt, double* a,
                  double max_phase_shift, double max_step_size,
                  double direction);
 
+/* The same, also writing the nonlinear step sizes |h_i| to h_out[i] (i < h_cap;
+ * h_out may be NULL). */
+int ofc_ssfm_run_rec(int modes, int samples, double dt, double* a,
+                     const ofc_fiber* fiber, int grid, int total_steps,
+                     double max_phase_shift, double max_step_size,
+                     double direction, double* h_out, int h_cap);
+/* The ADAPTIVE loop (ssfm.cpp:92-118) on the given step sizes h[0..n_steps). */
+int ofc_ssfm_run_steps(int modes, int samples, double dt, double* a,
+                       const ofc_fiber* fiber, const double* h, int n_steps,
+                       double direction);
+
 /* Fiber transforms (src/focss/module/fiber.cpp:4-45). */
 ofc_fiber ofc_fiber_scale(ofc_fiber f, double length_factor);
 ofc_fiber ofc_fiber_dispersive(ofc_fiber f);
