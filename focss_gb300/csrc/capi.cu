@@ -504,7 +504,7 @@ FOCSS_API focss_status focss_amplifier_apply(focss_ctx* c, focss_field* f, doubl
     if (!fg::amplifier_coeffs(op, gain, noise_factor, f->f0, f->dt, &scale, &sigma))
         return fg::set_error(c, FOCSS_ERR_INVALID_ARG, "amplifier: unknown op");
     return fg::cuda_check(c,
-                          fg::launch_amplifier(f->d, f->modes, f->samples, f->batch, (float)scale, (float)sigma,
+                          fg::launch_amplifier(f->d, f->modes, f->samples, f->batch, scale, (float)sigma,
                                                seed, counter, c->stream),
                           "amplifier");
 }

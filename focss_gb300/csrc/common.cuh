@@ -47,6 +47,28 @@ __device__ __forceinline__ float2 phase_rotation(float phi) {
     return (k & 2) ? make_float2(-c, -s) : make_float2(c, s);
 }
 
+// v * exp(i phi) applied as v + v * (cos(phi) - 1 + i sin(phi)) with cos(phi) - 1
+// formed directly.  Rounding cos(phi) itself to FP32 makes |exp(i phi)| miss 1
+// by up to 2^-25, and for |phi| < 2^-12 always upwards (cos rounds to exactly
+// 1): a gain that repeats at every split step and grows the field error
+// quadratically along a link.  The increment form leaves one unbiased rounding
+// (the final additions).
+__device__ __forceinline__ float2 kerr_rotate(float2 v, float phi) {
+    float cm1, s;
+    if (fabsf(phi) <= 0.25f) {
+        const float p2 = phi * phi;
+        s = phi * fmaf(p2, fmaf(p2, fmaf(p2, -1.0f / 5040.0f, 1.0f / 120.0f), -1.0f / 6.0f), 1.0f);
+        cm1 = p2 * fmaf(p2, fmaf(p2, fmaf(p2, 1.0f / 40320.0f, -1.0f / 720.0f), 1.0f / 24.0f), -0.5f);
+    } else {
+        const float2 r = phase_rotation(phi);  // cos(phi) <= 0.97: cos - 1 is exact
+        cm1 = r.x - 1.0f;
+        s = r.y;
+    }
+    const float dx = fmaf(v.x, cm1, -v.y * s);
+    const float dy = fmaf(v.y, cm1, v.x * s);
+    return make_float2(v.x + dx, v.y + dy);
+}
+
 // Block-wide reductions (blockDim.x multiple of 32, <= 1024).
 __device__ __forceinline__ float warp_max(float v) {
 #pragma unroll
@@ -97,6 +119,12 @@ __device__ __forceinline__ double block_sum_d(double v, double* scratch) {
     return v;
 }
 
+// A double as the unevaluated sum of two floats.
+__host__ __device__ __forceinline__ float2 split_df(double v) {
+    const float hi = (float)v;
+    return make_float2(hi, (float)(v - (double)hi));
+}
+
 // Counter-based generator: Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).
 __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
 #pragma unroll
@@ -123,11 +151,13 @@ __device__ __forceinline__ float2 gaussian_pair(uint32_t x0, uint32_t x1) {
 // One sample of Amplifier::amplify / add_noise (src/focss/module/amplifier.cpp:15-28):
 // scale*a + sigma*(z0 + i z1), (z0, z1) Box-Muller on Philox4x32-10 with
 // counter {sample, mode + modes*realization, c_lo, c_hi} (element i of a
-// realization-major, mode-major buffer of `samples` per mode).
-__device__ __forceinline__ float2 amplifier_sample(float2 a, size_t i, int samples, float scale, float sigma,
+// realization-major, mode-major buffer of `samples` per mode).  The scale is a
+// two-float sum hi + lo applied with a compensated product, so the span gain
+// carries no FP32 rounding of its own that would repeat at every span.
+__device__ __forceinline__ float2 amplifier_sample(float2 a, size_t i, int samples, float2 scale, float sigma,
                                                    uint2 key, uint32_t c_lo, uint32_t c_hi) {
-    a.x *= scale;
-    a.y *= scale;
+    a.x = fmaf(a.x, scale.x, a.x * scale.y);
+    a.y = fmaf(a.y, scale.x, a.y * scale.y);
     if (sigma != 0.0f) {
         const uint32_t sample = (uint32_t)(i % (size_t)samples);
         const uint32_t stream = (uint32_t)(i / (size_t)samples);

@@ -27,17 +27,17 @@ cudaError_t launch_scale(float2* d, size_t n, float2 s, cudaStream_t st) {
 // Amplifier::amplify / add_noise (src/focss/module/amplifier.cpp:15-28):
 // A <- scale*A + sigma*(z0 + i z1), (z0, z1) Box-Muller on Philox4x32-10 with
 // counter {sample, mode + modes*realization, counter_lo, counter_hi}.
-__global__ void amplifier_kernel(float2* __restrict__ d, int modes, int samples, size_t n, float scale,
+__global__ void amplifier_kernel(float2* __restrict__ d, int modes, int samples, size_t n, float2 scale,
                                  float sigma, uint2 key, uint32_t c_lo, uint32_t c_hi) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
         d[i] = amplifier_sample(d[i], i, samples, scale, sigma, key, c_lo, c_hi);
     (void)modes;
 }
 
-cudaError_t launch_amplifier(float2* d, int modes, int samples, int batch, float scale, float sigma,
+cudaError_t launch_amplifier(float2* d, int modes, int samples, int batch, double scale, float sigma,
                              uint64_t seed, uint64_t counter, cudaStream_t st) {
     const size_t n = (size_t)batch * modes * samples;
-    amplifier_kernel<<<grid_for(n, 256), 256, 0, st>>>(d, modes, samples, n, scale, sigma,
+    amplifier_kernel<<<grid_for(n, 256), 256, 0, st>>>(d, modes, samples, n, split_df(scale), sigma,
                                                         make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)),
                                                         (uint32_t)counter, (uint32_t)(counter >> 32));
     count_launch();

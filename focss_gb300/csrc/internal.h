@@ -199,7 +199,7 @@ focss_status fft_inverse_transposed(Ctx* ctx, float2* data, int N, int batch);
 
 // ---- dsp.cu
 cudaError_t launch_scale(float2* d, size_t n, float2 s, cudaStream_t st);
-cudaError_t launch_amplifier(float2* d, int modes, int samples, int batch, float scale, float sigma,
+cudaError_t launch_amplifier(float2* d, int modes, int samples, int batch, double scale, float sigma,
                              uint64_t seed, uint64_t counter, cudaStream_t st);
 cudaError_t launch_power(const float2* d, int modes, int samples, int batch, double* avg,
                          unsigned int* peak_bits, cudaStream_t st);

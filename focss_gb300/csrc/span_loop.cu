@@ -70,7 +70,7 @@ __global__ void span_end_kernel(const SsfmState* __restrict__ st, int batch, int
     }
 }
 
-__global__ void amp_graph_kernel(float2* __restrict__ d, int samples, size_t n, float scale, float sigma,
+__global__ void amp_graph_kernel(float2* __restrict__ d, int samples, size_t n, float2 scale, float sigma,
                                  const unsigned long long* __restrict__ sc, int span) {
     const unsigned long long seed = sc[0], counter = sc[1] + (unsigned long long)span;
     const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
@@ -147,7 +147,7 @@ cudaError_t record_branch(Ctx* ctx, LoopGraph* g, int i, Field* f, const Plan& p
     if (e == cudaSuccess) e = cudaMemsetAsync(ctr, 0, sizeof(int) * kCtr, s);
     for (int span = 0; span < spans && e == cudaSuccess; ++span) {
         if (amp.before != FOCSS_AMP_NONE) {
-            amp_graph_kernel<<<amp_grid(n), 256, 0, s>>>(f->d, f->samples, n, (float)sc_b, (float)sg_b,
+            amp_graph_kernel<<<amp_grid(n), 256, 0, s>>>(f->d, f->samples, n, split_df(sc_b), (float)sg_b,
                                                          g->d_amp + 2 * i, span);
             e = cudaGetLastError();
             g->static_kernels += 1;
@@ -212,7 +212,7 @@ cudaError_t record_branch(Ctx* ctx, LoopGraph* g, int i, Field* f, const Plan& p
         e = cudaGetLastError();
         g->static_kernels += 1;
         if (e == cudaSuccess && amp.after != FOCSS_AMP_NONE) {
-            amp_graph_kernel<<<amp_grid(n), 256, 0, s>>>(f->d, f->samples, n, (float)sc_a, (float)sg_a,
+            amp_graph_kernel<<<amp_grid(n), 256, 0, s>>>(f->d, f->samples, n, split_df(sc_a), (float)sg_a,
                                                          g->d_amp + 2 * i, span);
             e = cudaGetLastError();
             g->static_kernels += 1;
@@ -397,7 +397,7 @@ FOCSS_API focss_status focss_autotune(focss_ctx* c, int samples, int batch, int*
     if (e != cudaSuccess) return fg::cuda_check(c, e, "autotune scratch");
     // Gaussian field of ~1 mW per sample: a representative nonlinear phase.
     e = cudaMemsetAsync(f.d, 0, sizeof(float2) * f.n(), s);
-    if (e == cudaSuccess) e = fg::launch_amplifier(f.d, 1, samples, batch, 0.0f, std::sqrt(0.5e-3f), 17, 0, s);
+    if (e == cudaSuccess) e = fg::launch_amplifier(f.d, 1, samples, batch, 0.0, std::sqrt(0.5e-3f), 17, 0, s);
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     if (e == cudaSuccess) e = cudaEventCreate(&t0);
     if (e == cudaSuccess) e = cudaEventCreate(&t1);

@@ -209,7 +209,7 @@ __device__ __forceinline__ void col_work(const PassArgs& a, int op, const SsfmSt
 #pragma unroll
             for (int j = 0; j < Q; ++j) {
                 const float p = cnorm(v[j]);
-                v[j] = cmul(v[j], phase_rotation(coef * p));
+                v[j] = kerr_rotate(v[j], coef * p);
                 pk = fmaxf(pk, p);
             }
         } else {
@@ -223,7 +223,7 @@ __device__ __forceinline__ void col_work(const PassArgs& a, int op, const SsfmSt
             for (int j = 0; j < Q; ++j) {
                 const int i = (t + P * j) * C + c;
                 const float p = pw[i] + pw[stride + i];
-                v[j] = cmul(v[j], phase_rotation(coef * p));
+                v[j] = kerr_rotate(v[j], coef * p);
                 pk = fmaxf(pk, p);
             }
             __syncthreads();  // the forward transform reuses the buffers

@@ -466,22 +466,26 @@ FOCSS_API focss_status focss_cnn_loss_grad(focss_cnn* model, const focss_field* 
 FOCSS_API focss_status focss_cnn_adam_step(focss_cnn* model, double lr, double beta1, double beta2, double eps);
 
 /* ------------------------------------------------- allocation-free SSFM */
-/* No counterpart in the reference.  The same computation as focss_ssfm_run
- * (SSFM::run on every realization) for callers that cannot let a library
- * allocate device memory: frameworks that own the device heap through their
- * own pool, latency-critical loops where an allocation and the
- * synchronization it implies are not allowed, or processes with a fixed
- * device-memory budget.  `data` is the caller's device buffer of
- * batch*samples complex64 (interleaved float pairs), propagated in place on
- * `stream` (a cudaStream_t; NULL = legacy default stream).  The library
- * allocates nothing: step state and twiddle tables live in one fixed
- * 59 KB __device__ array per device, held until the process exits.
+/* No counterpart in the reference.  SSFM::run on every realization, like
+ * focss_ssfm_run, for callers that cannot let a library allocate device
+ * memory: frameworks that own the device heap through their own pool,
+ * latency-critical loops where an allocation and the synchronization it
+ * implies are not allowed, or processes with a fixed device-memory budget.
+ * It always uses the balanced two-pass FFT split; where focss_set_fft_split
+ * or focss_autotune chose another split (or the single-CTA kernel) for
+ * focss_ssfm_run, the two fields agree to FP32 rounding, not bit for bit.
+ * `data` is the caller's device buffer of batch*samples complex64
+ * (interleaved float pairs), propagated in place on `stream` (a
+ * cudaStream_t; NULL = legacy default stream).  The library allocates
+ * nothing: step state and twiddle tables live in one fixed 59 KB
+ * __device__ array per device, held until the process exits.
  * Limits: samples a power of two in [2^8, 2^17], batch <= 256; larger shapes
  * return FOCSS_ERR_UNSUPPORTED before any GPU work.  Single-mode fields only.
  * The first call on a device looks up that array's device address (a
  * one-time set-up); make that first call before any stream capture.  Every
- * call shares the array, so calls that overlap on the GPU race.  Returns
- * after the stream has finished the propagation. */
+ * call shares the array, so calls that overlap on the GPU race.  Each call
+ * synchronizes `stream` before it returns (ADAPTIVE and LOGARITHMIC grids
+ * also poll a step counter from the host while they run). */
 FOCSS_API focss_status focss_ssfm_run_noalloc(void* stream, void* data, int samples, int batch, double time_step,
                                               const focss_fiber* fiber, const focss_ssfm_opts* opts,
                                               double direction, int* steps_out);

@@ -77,6 +77,7 @@ def lib():
             "ref_find_certainty": (D, [I, I, P, P]),
             "ref_certainty_sd": (None, [I, I, P, D, P]),
             "ref_hd_rms": (None, [I, I, P, P]),
+            "ref_field_power": (None, [I, I, P, P, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -335,3 +336,12 @@ def hd_rms(field):
     o = np.zeros_like(f)
     lib().ref_hd_rms(f.shape[0], f.shape[1], _p(f), _p(o))
     return o
+
+
+def field_power(a):
+    """Field::average_power / peak_power (field.cpp:164-187): (average, peak)."""
+    a = _c(np.atleast_2d(a))
+    m, n = _shape(a)
+    avg, pk = np.zeros(1), np.zeros(1)
+    lib().ref_field_power(m, n, _p(a), _p(avg), _p(pk))
+    return float(avg[0]), float(pk[0])

@@ -89,6 +89,13 @@ void ref_amplify(int modes, int samples, double dt, double f0, double* data, dou
     store(f, data);
 }
 
+/* Field::average_power / peak_power (field.cpp:164-187). */
+void ref_field_power(int modes, int samples, const double* data, double* average, double* peak) {
+    Field f = make_field(modes, samples, 1.0, 0, data);
+    *average = f.average_power();
+    *peak = f.peak_power();
+}
+
 void ref_drop_power(int modes, int samples, double* data, double gain) {
     Field f = make_field(modes, samples, 1.0, 0, data);
     Amplifier(gain).drop_power(f);

@@ -228,7 +228,22 @@ def main_ppe():
     print("wrote", len(g), "PPE arrays; certainty", cert)
 
 
+def main_power():
+    """Field::average_power / peak_power (field.cpp:164-187), 1 and 2 modes."""
+    assert ref.available(), "reference build unavailable"
+    rng = np.random.default_rng(20261205)
+    g = {}
+    for modes in (1, 2):
+        a = (rng.standard_normal((modes, 4096)) + 1j * rng.standard_normal((modes, 4096))) * 0.03
+        a = a.astype(np.complex64).astype(np.complex128)  # exactly representable on the GPU
+        g["power_in%d" % modes] = a
+        g["power_out%d" % modes] = np.array(ref.field_power(a))
+    np.savez_compressed(os.path.join(OUT, "field_power_golden.npz"), **g)
+    print("wrote", len(g), "power arrays")
+
+
 if __name__ == "__main__":
     if "--ppe-only" not in sys.argv:
         main()
     main_ppe()
+    main_power()

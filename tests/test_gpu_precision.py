@@ -6,11 +6,13 @@ matched filter, phase-shift equalizer.  The field must stay within 1e-5
 relative L2 of the FP64 run with the same step counts, and Q within 0.05 dB.
 
 5-channel WDM (the precision-study link with 2^9 symbols per channel,
-N = 2^13): on a UNIFORM grid (100 steps per span) the field stays within
-3e-5; on the ADAPTIVE grid every step size comes from the FP32 field's peak
-power, so the two runs take slightly different (equally valid) grids and the
-fields part by the grid's own sensitivity, while step counts and the centre
-channel's Q agree (within 0.05 dB).
+N = 2^13), UNIFORM (100 steps per span) and ADAPTIVE.  On the ADAPTIVE grid
+every step size comes from the field's peak power, so the GPU records its
+grid (focss_ssfm_run_record) and the oracle replays it (ofc_ssfm_run_steps):
+both then walk one grid.  The field must stay within the FP32 rounding walk
+3e-7 sqrt(K) after K split steps (see test_gpu_step_grid.py), step counts
+must agree with a free-running FP64 run, and the centre channel's Q within
+0.05 dB.
 """
 import numpy as np
 import pytest
@@ -83,20 +85,25 @@ def test_wdm_link(ctx, oracle_cpu, grid):
     dt = field.domain.time_step
     x0 = field.numpy()[0, 0]
     fib = link.fiber()
+    ofib = cpu.Fiber(ALPHA, BETA2, GAMMA, 80e3, 1.55e-6, 1.0)
     if grid == "uniform":
         steps = _gpu_link(field, fg.SSFM(fib, 100), spans)
         want, wsteps = _oracle_link(cpu, x0, dt, cpu.UNIFORM, 100, spans)
+        assert steps == wsteps
     else:
-        steps = _gpu_link(field, _adaptive(fib), spans)
-        want, wsteps = _oracle_link(cpu, x0, dt, cpu.ADAPTIVE, 1, spans)
-    assert steps == wsteps
-    if grid == "uniform":
-        assert rel_l2(field.numpy()[0, 0], want) < 3e-5
+        ssfm, want, steps = _adaptive(fib), x0.copy(), 0
+        for _ in range(spans):
+            st, h = ssfm.run_recorded(field)
+            fg.Amplifier(G).amplify(field)
+            want = cpu.amplify(cpu.ssfm_run_steps(want, dt, ofib, h[0]), dt, F0, G)
+            steps += int(st[0])
+        _, free_steps = _oracle_link(cpu, x0, dt, cpu.ADAPTIVE, 1, spans)
+        assert abs(steps - free_steps) <= spans
+    assert rel_l2(field.numpy()[0, 0], want) < 3e-7 * np.sqrt(steps)
     fg.cd_compensation(field, fib, spans)
     r = dsp.rrc_sampling(dsp.wdm_select(field, 0, link.spacing), link.osf, link.roll_off)
     r = dsp.PhaseShiftEqualizer(720).train_equalize(tx, r)
     q_gpu = dsp.q2_factor(tx, r, 100)[0]
-    ofib = cpu.Fiber(ALPHA, BETA2, GAMMA, 80e3, 1.55e-6, 1.0)
     t = tx.numpy()[0, 0]
     ao = cpu.wdm_select(cpu.cd_compensation(want, dt, ofib, spans), dt, 0, link.spacing)
     ro = cpu.rrc_sampling(ao, link.osf, link.roll_off)

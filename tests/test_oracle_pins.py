@@ -168,3 +168,15 @@ def test_live_reference_noise_statistics(oracle_cpu, ref_live):
     for z in (a, b):
         assert abs(np.var(z.real) / var - 1) < 0.03
         assert abs(np.var(z.imag) / var - 1) < 0.03
+
+
+def test_field_power(oracle_cpu):
+    """Field::average_power / peak_power (field.cpp:164-187), golden from the reference build."""
+    import os
+    from conftest import ROOT
+    g = dict(np.load(os.path.join(ROOT, "tests", "golden", "field_power_golden.npz")))
+    for modes in (1, 2):
+        a = g["power_in%d" % modes]
+        avg, peak = g["power_out%d" % modes]
+        assert abs(oracle_cpu.average_power(a) - avg) < 1e-15 * avg
+        assert abs(oracle_cpu.peak_power(a) - peak) < 1e-15 * peak
