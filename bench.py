@@ -14,8 +14,10 @@ Workload (one bench step = one forward propagation of the whole batch):
 Arms:
   default            hand-written sm_103a kernels through libfocss_gpu (C ABI)
   --impl reference   the reference algorithm on the host cores: the FP64 C
-                     restatement of src/focss/solver/ssfm.cpp (oracle port), a
-                     bounded sample of the same workload per step.
+                     restatement of src/focss/solver/ssfm.cpp and amplifier.cpp
+                     (oracle port), a bounded sample of the same workload per
+                     step (ADAPTIVE steps with ASE over the first 2 km of a
+                     span, one realization per host thread).
 
 Prints one JSON line on rank 0.
 """
@@ -159,26 +161,50 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- CPU reference / baseline
-def cpu_sample(threads, n_steps):
-    """FP64 reference split steps (oracle port of ssfm.cpp) on the host cores:
-    `threads` realizations of the workload's field, n_steps uniform 1 km steps each."""
+def bench_config(world):
+    """The workload's `config`, identical in both arms."""
+    B = len(W["powers_dbm"]) * W["ase_seeds"]
+    return dict(W, batch=B, samples=N,
+                l2="batch of %d MB complex64, %.1fx the 129 MB L2 (inputs larger than L2 between steps)"
+                   % (B * N * 8 >> 20, B * N * 8 / 129e6),
+                parallelism="replicas" if world > 1 else "single GPU")
+
+
+def cpu_sample(threads, segment_m):
+    """The workload's algorithm on the host cores, with the FP64 oracle port of
+    src/focss/solver/ssfm.cpp and src/focss/module/amplifier.cpp: 4 x
+    `threads` realizations of the N = 2^19 WDM field (launch powers cycling
+    over the workload's -2..+4 dBm/ch, highest first so the threads finish
+    together), each an ADAPTIVE split-step run (0.005 rad, 1 km) over the
+    first `segment_m` metres of a span, then the EDFA with ASE (NF 5 dB, the
+    GPU's Philox stream).  Returns (sample-steps/s / 1e9, seconds, split steps
+    taken)."""
     from oracle import build as obuild
     from oracle import cpu
     obuild.build_oracle()
     alpha, beta2, gamma = fiber_params()
-    x = synth_wdm()[None, None, :] * np.sqrt(1e-3)
-    a = np.ascontiguousarray(np.repeat(x, threads, axis=0))
-    fib = cpu.Fiber(alpha, beta2, gamma, W["span_m"], 1.55e-6, 1.0)
+    base = synth_wdm()
+    powers = sorted(W["powers_dbm"], reverse=True)
+    R = 4 * threads
+    a = np.empty((R, 1, N), np.complex128)
+    for i in range(R):
+        a[i, 0] = base * np.sqrt(1e-3 * 10 ** (powers[(i * len(powers)) // R] / 10.0))
+    fib = cpu.Fiber(alpha, beta2, gamma, segment_m, 1.55e-6, 1.0)
+    G = 10 ** (W["alpha_db_per_km"] * W["span_m"] / 1e3 / 10)
+    NF = 10 ** (W["noise_figure_db"] / 10)
     t0 = time.perf_counter()
-    cpu.uniform_steps_batch(a, DT, fib, 1000.0, n_steps, threads)
+    out, steps = cpu.ssfm_batch(a, DT, fib, cpu.ADAPTIVE, 1, W["max_phase_shift"], W["max_step_m"], threads=threads)
+    for i in range(R):
+        out[i] = cpu.amplify(out[i], DT, F0, G, NF, seed=7, counter=0, realization=i)
     dt = time.perf_counter() - t0
-    return threads * n_steps * N / dt / 1e9, dt
+    k = int(np.sum(steps))
+    return k * N / dt / 1e9, dt, k
 
 
-# Split steps per realization of the CPU samples: ~10-20 s of FP64 work on
-# 16 host cores for the baseline, a few seconds per reference-arm step.
-CPU_BASELINE_STEPS = 200
-CPU_REFERENCE_STEPS = 40
+# Metres of the first span per realization in a CPU sample: ~2 s of FP64
+# work on 16 host cores per reference-arm step, ~10 s for the baseline.
+CPU_REFERENCE_SEGMENT_M = 500.0
+CPU_BASELINE_SEGMENT_M = 2500.0
 
 
 def run_reference(args):
@@ -186,22 +212,25 @@ def run_reference(args):
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    n_steps = CPU_REFERENCE_STEPS
     for _ in range(args.warmup):
-        cpu_sample(threads, n_steps)
-    vals, times = [], []
+        cpu_sample(threads, CPU_REFERENCE_SEGMENT_M)
+    vals, times, ks = [], [], []
     for _ in range(args.steps):
-        v, t = cpu_sample(threads, n_steps)
+        v, t, k = cpu_sample(threads, CPU_REFERENCE_SEGMENT_M)
         vals.append(v)
         times.append(t)
+        ks.append(k)
     value = float(np.median(vals))
-    sample = "%d realizations x %d uniform 1 km split steps of the N=2^19 WDM field, FP64, %d threads" % (
-        threads, n_steps, threads)
+    sample = ("%d realizations (launch powers -2..+4 dBm/ch) x the first %.0f m of a span: ADAPTIVE split "
+              "steps (%d in total per sample) and the EDFA with ASE, FP64 oracle port of ssfm.cpp/amplifier.cpp, "
+              "%d threads" % (4 * threads, CPU_REFERENCE_SEGMENT_M, int(np.median(ks)), threads))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.median(times)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": dict(W, note="reference arm: oracle port (reference sources need FFTW, absent on the GPU host)"),
+        "config": bench_config(args.gpus),
+        "reference_code": "oracle port: the reference's own sources build only where the reference tree exists "
+                          "(FFTW/Armadillo stand-ins in oracle/), not on the GPU host",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -380,19 +409,17 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / max(1, args.steps), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": dict(W, batch=B, samples=N,
-                       l2="batch of %d MB complex64, %.1fx the 129 MB L2" % (B * N * 8 >> 20, B * N * 8 / 129e6),
-                       fft_split="%d x %d (autotuned)" % (1 << split, N >> split),
-                       parallelism="replicas" if world > 1 else "single GPU",
-                       sample_steps_per_step=sample_steps / max(1, args.steps)),
+        "config": bench_config(world),
+        "fft_split": "%d x %d (autotuned)" % (1 << split, N >> split),
+        "sample_steps_per_step": sample_steps / max(1, args.steps),
         "roofline": roofline,
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(hin.nbytes),
                 "d2h_bytes_per_step": int(hout.nbytes)},
         "gpu_launches": int(launches),
         "clocks": clk,
     }
-    if not args.no_dbp:
-        line["dbp"] = dbp_section(fg, ctx)
+    if not args.no_precision:
+        line["precision"] = precision_section(fg, ctx)
     if not args.no_sweep:
         line["sweep"] = sweep_section(fg, ctx, stream)
     if not args.no_ppe:
@@ -405,12 +432,15 @@ def run_ours(args):
         line["single_channel"] = single_channel_section(fg, ctx, stream)
     if world == 1 and rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        n_steps = CPU_BASELINE_STEPS
-        v, t = cpu_sample(threads, n_steps)
+        v, t, k = cpu_sample(threads, CPU_BASELINE_SEGMENT_M)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": "%d realizations x %d uniform 1 km split steps of the N=2^19 WDM "
-                                          "field, FP64 oracle port of ssfm.cpp, one realization per thread, "
-                                          "%.1f s" % (threads, n_steps, t)}
+                                "sample": "%d realizations (launch powers -2..+4 dBm/ch) x the first %.0f m of a "
+                                          "span: %d ADAPTIVE split steps in total and the EDFA with ASE, FP64 oracle "
+                                          "port of ssfm.cpp/amplifier.cpp, %d threads, %.1f s"
+                                          % (4 * threads, CPU_BASELINE_SEGMENT_M, k, threads, t)}
+    if not args.no_dbp:
+        # last, so the compact learned-vs-plain table ends the line
+        line["learned_vs_plain"] = learned_vs_plain_section(fg, ctx)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -418,34 +448,77 @@ def run_ours(args):
     return 0
 
 
-def dbp_section(fg, ctx, power_dbm=2.0, batch=8):
-    """Q (dB) per DBP GPU time, learned vs plain, on the same link: the centre
-    channel at `power_dbm` per channel, 2 samples/symbol, independent train
-    and test sets of `batch` realizations each (fresh symbols and ASE)."""
+def precision_section(fg, ctx, spans=None):
+    """FP32 against FP64 on the workload's link at its own size, noise off:
+    one realization at -2 and one at +4 dBm/ch propagated by the GPU with its
+    ADAPTIVE grid recorded (focss_ssfm_run_record), the same grid replayed by
+    a complex128 restatement of ssfm.cpp on the GPU (tests/fp64_ssfm.py, test
+    infrastructure pinned to the FP64 oracle), field relative L2 after the
+    20 spans, and the GPU's step counts against a free-running FP64 run."""
+    import math
+
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import fp64_ssfm
     from focss_gb300 import links
-    link = links.Link(spans=W["spans"], span_m=W["span_m"], noise_figure_db=W["noise_figure_db"],
-                      max_phase=W["max_phase_shift"], max_step=W["max_step_m"], channels=W["channels"],
-                      spacing=W["spacing_hz"], osf=W["samples_per_symbol"], roll_off=W["roll_off"])
-    ns = W["symbols_per_channel"]
-    a, ta = links.wdm_transmitter(link, ns, batch, power_dbm, seed=101, ctx=ctx)
-    b, tb = links.wdm_transmitter(link, ns, batch, power_dbm, seed=202, ctx=ctx)
-    links.propagate(link, a, seed=11)
-    links.propagate(link, b, seed=22)
-    ra, rb = links.centre_channel(link, a), links.centre_channel(link, b)
-    out = {"power_dbm_per_channel": power_dbm, "test_realizations": batch, "symbols_per_realization": ns,
-           "samples_per_symbol": 2, "plain": {}}
-    for k in (1, 2, 4, 100):
-        q, ms = links.plain_dbp_q(link, rb, tb, k)
-        out["plain"]["%d_steps_per_span" % k] = {"q_db": float(np.mean(q)), "ms": ms}
-    for k in (2, 4):
-        r = links.learned_dbp(link, ra, ta, rb, tb, steps_per_span=k, taps=63, mf_taps=255, iters=500, lr=3e-4,
-                              cnn_iters=300, cnn_lr=1e-3)
-        out["learned_%d_steps_per_span" % k] = {
-            "q_db": float(np.mean(r["q_learned"])), "ms": r["ms_learned"],
-            "q_db_at_init": float(np.mean(r["q_init"])), "train_s": r["train_s"],
-            "loss_first": r["loss_first"], "loss_last": r["loss_last"]}
-        out["learned_%d_steps_per_span_cnn" % k] = {
-            "q_db": float(np.mean(r["q_learned_cnn"])), "ms": r["ms_learned_cnn"], "train_s": r["cnn_train_s"]}
+    spans = spans or W["spans"]
+    link = links.Link(spans=spans)
+    fib = link.fiber()
+    amp = math.sqrt(link.gain())
+    out = {"link": "N=2^19 WDM precision study, 20 x 80 km, ADAPTIVE, noise off, replayed grid"}
+    for p in (-2.0, 4.0):
+        field, _ = links.wdm_transmitter(link, W["symbols_per_channel"], 1, p, seed=7, ctx=ctx)
+        rep = torch.from_numpy(field.numpy()[0]).cuda(ctx.device)
+        free = rep.clone()
+        s = fg.SSFM(fib)
+        s.set_grid(fg.SSFM.ADAPTIVE)
+        s.set_maximum_phase_shift(W["max_phase_shift"])
+        s.set_maximum_step_size(W["max_step_m"])
+        steps, d_steps = 0, 0
+        for _ in range(spans):
+            st, h = s.run_recorded(field, capacity=1 << 17)
+            fg.Amplifier(link.gain()).amplify(field)
+            rep = fp64_ssfm.run_steps(rep, field.domain.time_step, fib, h[0]) * amp
+            free, taken = fp64_ssfm.run_adaptive(free, field.domain.time_step, fib, W["max_phase_shift"],
+                                                 W["max_step_m"])
+            free = free * amp
+            steps += int(st[0])
+            d_steps = max(d_steps, abs(int(st[0]) - len(taken)))
+        got, want = field.numpy()[0, 0], rep.cpu().numpy()[0]
+        err = float(np.linalg.norm(got - want) / np.linalg.norm(want))
+        out["%+d_dbm" % p] = {"steps": steps, "field_rel_l2": err, "per_sqrt_step": err / math.sqrt(steps),
+                              "max_step_count_delta_per_span": d_steps}
+    return out
+
+
+LVP = dict(
+    wdm_link="5-ch WDM 20 x 80 km ADAPTIVE + ASE, centre channel at 2 sps",
+    wdm_powers_dbm=[-2.0, 4.0], single_channel="1 channel 4 sps, 20 x 80 km ADAPTIVE + ASE, 3 dBm",
+    realizations=8, symbols_per_realization=2 ** 15, steps_per_span=4, iters=300, cnn_iters=200,
+)
+
+
+def learned_vs_plain_section(fg, ctx):
+    """Learned DBP at 4 steps/span against plain DBP at 1 / 4 / 100
+    steps/span: Q (dB, mean over 8 test realizations x 2^15 symbols) and DBP
+    time (ms) per launch power, on the WDM link's centre channel and on a
+    single-channel link (training and test sets generated by the GPU split
+    step).  Compact: [q_db, ms] per entry."""
+    from focss_gb300 import links
+    c = LVP
+    out = {"config": c}
+
+    def compact(r):
+        return {k: [round(v["q_db"], 3), round(v["ms"], 3)] for k, v in r.items()}
+
+    for p in c["wdm_powers_dbm"]:
+        r = links.learned_vs_plain(links.Link(), p, c["symbols_per_realization"], c["realizations"],
+                                   seed=int(500 + 10 * p), ctx=ctx, iters=c["iters"], cnn_iters=c["cnn_iters"])
+        out["wdm_%+d_dbm" % p] = compact(r)
+    single = links.Link(channels=1, osf=4)
+    r = links.learned_vs_plain(single, 3.0, c["symbols_per_realization"], c["realizations"], seed=900, ctx=ctx,
+                               iters=c["iters"], cnn_iters=c["cnn_iters"])
+    out["single_channel_+3_dbm"] = compact(r)
     return out
 
 
@@ -998,6 +1071,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-dbp", action="store_true", help="skip the learned-vs-plain DBP section")
+    ap.add_argument("--no-precision", action="store_true",
+                    help="skip the FP32-vs-FP64 field error on the replayed grid (about 20 s)")
     ap.add_argument("--no-sweep", action="store_true", help="skip the uneven-length batched sweep section")
     ap.add_argument("--no-ppe", action="store_true", help="skip the perturbation-equalizer section")
     ap.add_argument("--no-wdm-ppe", action="store_true",

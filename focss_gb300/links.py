@@ -225,14 +225,45 @@ def learned_dbp(link: Link, rx_train: Field, tx_train: Field, rx_test: Field, tx
 
 def plain_dbp_q(link: Link, rx2: Field, tx: Field, steps_per_span, cut=100, angle_steps=720):
     """backward_propagation with UNIFORM steps (systems.cpp:86-103), matched
-    filter, phase-shift equalizer, Q per realization and the DBP GPU time."""
-    f = rx2.copy()
+    filter, phase-shift equalizer, Q per realization and the DBP time (timed
+    like the learned DBP: one warm-up, then the mean of 3 runs)."""
     s = SSFM(link.fiber(), steps_per_span)
-    f.ctx.sync()
-    t0 = time.perf_counter()
-    backward_propagation(f, link.fiber(), s, link.gain(), link.spans)
-    f.ctx.sync()
-    ms = (time.perf_counter() - t0) * 1e3
+    f = rx2.copy()
+
+    def run():
+        f.assign(rx2)
+        backward_propagation(f, link.fiber(), s, link.gain(), link.spans)
+        return f
+
+    f, ms = _timed(run, rx2.ctx)
     sym = dsp.rrc_sampling(f, rx2.domain.samples // tx.domain.samples, link.roll_off)
     eq = dsp.PhaseShiftEqualizer(angle_steps).train_equalize(tx, sym)
     return dsp.q2_factor(tx, eq, cut), ms
+
+
+def learned_vs_plain(link: Link, power_dbm, n_symbols=1 << 15, batch=8, seed=0, ctx=None, steps_per_span=4,
+                     plain_steps=(1, 4, 100), iters=300, lr=3e-4, cnn_iters=200, cnn_lr=1e-3, taps=63,
+                     mf_taps=255):
+    """Learned DBP at `steps_per_span` (and with the correction CNN) against
+    plain DBP on one link and launch power: independent training and test sets
+    of `batch` realizations x `n_symbols` (fresh symbols and ASE), propagated
+    on the GPU (ADAPTIVE steps, EDFA with ASE), the centre channel at 2
+    samples/symbol.  Returns {name: {"q_db": mean Q over the test set, "ms":
+    DBP time over the test set}}."""
+    a, ta = wdm_transmitter(link, n_symbols, batch, power_dbm, seed=seed + 1, ctx=ctx)
+    b, tb = wdm_transmitter(link, n_symbols, batch, power_dbm, seed=seed + 2, ctx=ctx)
+    propagate(link, a, seed=seed + 3)
+    propagate(link, b, seed=seed + 4)
+    ra, rb = centre_channel(link, a), centre_channel(link, b)
+    del a, b
+    out = {}
+    for k in plain_steps:
+        q, ms = plain_dbp_q(link, rb, tb, k)
+        out["plain_%d" % k] = {"q_db": float(np.mean(q)), "ms": ms}
+    r = learned_dbp(link, ra, ta, rb, tb, steps_per_span=steps_per_span, taps=taps, mf_taps=mf_taps, iters=iters,
+                    lr=lr, cnn_iters=cnn_iters, cnn_lr=cnn_lr)
+    out["learned_%d" % steps_per_span] = {"q_db": float(np.mean(r["q_learned"])), "ms": r["ms_learned"],
+                                          "train_s": r["train_s"]}
+    out["learned_%d_cnn" % steps_per_span] = {"q_db": float(np.mean(r["q_learned_cnn"])),
+                                              "ms": r["ms_learned_cnn"], "train_s": r["cnn_train_s"]}
+    return out
