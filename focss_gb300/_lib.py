@@ -123,6 +123,7 @@ SIGNATURES = {
     "focss_cnn_create": (I, [P, I, I, I, I, D, C.POINTER(P)]),
     "focss_cnn_destroy": (I, [P]),
     "focss_cnn_num_params": (I, [P]),
+    "focss_cnn_set_triplets": (I, [P, I, P, P]),
     "focss_cnn_set_params": (I, [P, P, I]),
     "focss_cnn_get_params": (I, [P, P, P, I]),
     "focss_cnn_forward": (I, [P, P, P]),

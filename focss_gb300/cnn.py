@@ -1,6 +1,8 @@
 """Convolutional correction of the learned-DBP output (focss_cnn_*): a 4-layer
-1D CNN (64 channels, kernel 9) on [Re y, Im y] whose output is added back to
-the symbols.  Training (forward, backward, Adam) runs on the GPU."""
+1D CNN (64 channels, kernel 9) on [Re y, Im y] and first-order perturbation
+triplets of y (T(m, n) + T(-m, -n), SINO::term, src/focss/equalizer/
+sino.cpp:161-171), whose output is added back to the symbols.  Training
+(forward, backward, Adam) runs on the GPU."""
 from __future__ import annotations
 
 import ctypes as C
@@ -24,14 +26,21 @@ def layout():
     return out, o
 
 
-def he_init(rng, zero_last=True):
+# Triplet offsets (m, n) of the input features: the SPM term and the
+# neighbours along n = 0 and m = n, m = -n that dominate first-order
+# perturbation coefficients.
+TRIPLETS = ((0, 0), (0, 1), (0, 2), (0, 3), (1, 1), (1, -1), (1, 2))
+
+
+def he_init(rng, zero_last=True, n_triplets=0):
     lay, total = layout()
     p = np.zeros(total, np.float32)
-    fan = [2 * KW, 64 * KW, 64 * KW, 64 * KW]  # real fan-in (2 used input channels in layer 1)
+    used = 2 + 2 * n_triplets  # input channels in use in layer 1
+    fan = [used * KW, 64 * KW, 64 * KW, 64 * KW]
     for l, (wo, shape, bo, cout) in enumerate(lay):
         w = rng.standard_normal(shape) * np.sqrt(2.0 / fan[l])
         if l == 0:
-            w[:, :, 2:] = 0
+            w[:, :, used:] = 0
         if l == 3:
             w[2:] = 0
             if zero_last:
@@ -41,13 +50,19 @@ def he_init(rng, zero_last=True):
 
 
 class CorrectionCNN:
-    def __init__(self, length, batch, input_scale, ctx=None):
+    def __init__(self, length, batch, input_scale, ctx=None, triplets=()):
         self.ctx = ctx or Context.default()
         self.length, self.batch = length, batch
         h = C.c_void_p()
         check(lib().focss_cnn_create(self.ctx.h, 64, KW, length, batch, input_scale, C.byref(h)), self.ctx.h)
         self.h = h
         self.n_params = lib().focss_cnn_num_params(h)
+        self.triplets = tuple(triplets)
+        if self.triplets:
+            m = np.array([t[0] for t in self.triplets], np.int32)
+            n = np.array([t[1] for t in self.triplets], np.int32)
+            check(lib().focss_cnn_set_triplets(h, len(self.triplets), m.ctypes.data_as(P), n.ctypes.data_as(P)),
+                  self.ctx.h)
 
     def set_params(self, flat):
         f = np.ascontiguousarray(flat, np.float32)

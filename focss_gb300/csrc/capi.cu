@@ -122,6 +122,18 @@ focss_status ensure_red(Ctx* ctx, size_t doubles) {
     return FOCSS_OK;
 }
 
+int sm_count() {
+    static int cached[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (!cached[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) return 152;
+        cached[dev] = n;
+    }
+    return cached[dev];
+}
+
 void* scratch_buffer(Ctx* ctx, int slot, size_t bytes) {
     if ((int)ctx->scratch.size() <= slot) {
         ctx->scratch.resize(slot + 1, nullptr);

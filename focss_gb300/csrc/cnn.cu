@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <new>
 #include <vector>
 
@@ -425,15 +426,45 @@ __global__ void __launch_bounds__(256) bias_grad_kernel(const bf16* __restrict__
     }
 }
 
-// x0 = [Re y / s, Im y / s, 0 ...] (16 channels)
-__global__ void cnn_input_kernel(const float2* __restrict__ y, size_t n, float inv_s, bf16* __restrict__ x0) {
+// First-order perturbation triplets fed to the network's idle input channels:
+// feature j of symbol k is T(m_j, n_j) + T(-m_j, -n_j) (T(0, 0) alone) with
+// T(m, n)[k] = y[k+m] y[k+n] conj(y[k+m+n]) (src/focss/equalizer/sino.cpp:161-171,
+// one mode), symbols outside the realization counting as zero, scaled by 1/s^3.
+constexpr int kMaxTriplets = (CIN0 - 2) / 2;
+struct Triplets {
+    int count;
+    int m[kMaxTriplets], n[kMaxTriplets];
+};
+
+__device__ __forceinline__ float2 sym_at(const float2* __restrict__ row, int L, int k) {
+    return (k >= 0 && k < L) ? row[k] : make_float2(0.f, 0.f);
+}
+__device__ __forceinline__ float2 triplet_at(const float2* __restrict__ row, int L, int k, int m, int n) {
+    const float2 c = sym_at(row, L, k + m + n);
+    return cmul(cmul(sym_at(row, L, k + m), sym_at(row, L, k + n)), make_float2(c.x, -c.y));
+}
+
+// x0 = [Re y / s, Im y / s, Re f_0 / s^3, Im f_0 / s^3, ..., 0 ...] (16 channels)
+__global__ void cnn_input_kernel(const float2* __restrict__ y, size_t n, int L, float inv_s, Triplets tr,
+                                 bf16* __restrict__ x0) {
+    const float inv_s3 = inv_s * inv_s * inv_s;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const float2 v = y[i];
         bf16* o = x0 + i * CIN0;
         o[0] = __float2bfloat16(v.x * inv_s);
         o[1] = __float2bfloat16(v.y * inv_s);
+        const float2* row = y + (i / L) * L;
+        const int k = (int)(i % L);
 #pragma unroll
-        for (int c = 2; c < CIN0; ++c) o[c] = __float2bfloat16(0.f);
+        for (int j = 0; j < kMaxTriplets; ++j) {
+            float2 f = make_float2(0.f, 0.f);
+            if (j < tr.count) {
+                f = triplet_at(row, L, k, tr.m[j], tr.n[j]);
+                if (tr.m[j] != 0 || tr.n[j] != 0) f = cadd(f, triplet_at(row, L, k, -tr.m[j], -tr.n[j]));
+            }
+            o[2 + 2 * j] = __float2bfloat16(f.x * inv_s3);
+            o[3 + 2 * j] = __float2bfloat16(f.y * inv_s3);
+        }
     }
 }
 
@@ -485,7 +516,9 @@ __global__ void cnn_adam_kernel(float* __restrict__ p, const float* __restrict__
     }
 }
 
-inline int gridn(size_t n) { return (int)std::max<size_t>(1, std::min<size_t>((n + 255) / 256, 152 * 16)); }
+inline int gridn(size_t n) {
+    return (int)std::max<size_t>(1, std::min<size_t>((n + 255) / 256, (size_t)sm_count() * 16));
+}
 
 template <int CIN, int COUT, bool F32>
 cudaError_t conv_fwd(const bf16* in, const bf16* W, const float* bias, void* out, int L, int B, int relu,
@@ -498,7 +531,7 @@ cudaError_t conv_fwd(const bf16* in, const bf16* W, const float* bias, void* out
     // about two waves of CTAs, each running several position tiles on one
     // staged copy of the weights
     const int ntiles = (L + tc::M - 1) / tc::M;
-    const int per_item = std::max(1, (152 * 4 + B - 1) / B);
+    const int per_item = std::max(1, (sm_count() * 4 + B - 1) / B);
     const int tiles = std::max(1, (ntiles + per_item - 1) / per_item);
     conv_fwd_tc_kernel<CIN, COUT, F32><<<dim3((ntiles + tiles - 1) / tiles, B), 128, smem, s>>>(in, W, bias, out, L,
                                                                                                  relu, mask, tiles);
@@ -548,6 +581,7 @@ struct focss_cnn {
     focss_ctx* ctx = nullptr;
     int length = 0, batch = 0;
     float scale = 1.f;
+    fg::Triplets triplets{};   // input features beside [Re y, Im y] (none by default)
     CnnLayout lay;
     float* params = nullptr;   // masters, grads, m1, m2
     float* grads = nullptr;
@@ -570,7 +604,7 @@ static cudaError_t cnn_forward(focss_cnn* m, const focss_field* y) {
     cudaStream_t s = m->ctx->stream;
     const int L = m->length, B = m->batch;
     const size_t n = m->positions();
-    fg::cnn_input_kernel<<<fg::gridn(n), 256, 0, s>>>(y->d, n, 1.f / m->scale, m->act[0]);
+    fg::cnn_input_kernel<<<fg::gridn(n), 256, 0, s>>>(y->d, n, L, 1.f / m->scale, m->triplets, m->act[0]);
     fg::count_launch();
     cudaError_t e = cudaGetLastError();
     const float* P = m->params;
@@ -660,6 +694,20 @@ FOCSS_API focss_status focss_cnn_destroy(focss_cnn* m) {
 
 FOCSS_API int focss_cnn_num_params(const focss_cnn* m) { return m ? (int)m->lay.total : 0; }
 
+FOCSS_API focss_status focss_cnn_set_triplets(focss_cnn* m, int count, const int32_t* tm, const int32_t* tn) {
+    if (!m || count < 0 || count > fg::kMaxTriplets || (count > 0 && (!tm || !tn))) return FOCSS_ERR_INVALID_ARG;
+    for (int j = 0; j < count; ++j)
+        if (std::abs(tm[j]) > m->length || std::abs(tn[j]) > m->length) return FOCSS_ERR_INVALID_ARG;
+    fg::Triplets t{};
+    t.count = count;
+    for (int j = 0; j < count; ++j) {
+        t.m[j] = tm[j];
+        t.n[j] = tn[j];
+    }
+    m->triplets = t;
+    return FOCSS_OK;
+}
+
 FOCSS_API focss_status focss_cnn_set_params(focss_cnn* m, const float* host, int n) {
     if (!m || !host || n != (int)m->lay.total) return FOCSS_ERR_INVALID_ARG;
     cudaStream_t s = m->ctx->stream;
@@ -717,7 +765,7 @@ FOCSS_API focss_status focss_cnn_loss_grad(focss_cnn* m, const focss_field* y, c
     // layer 4 (no activation): weights, bias, input gradient masked by out3 > 0
     if (e == cudaSuccess) e = fg::conv_wgrad<fg::CW, fg::COUT4>(m->g16, m->act[3], G + Y.w[3], L, B, s);
     if (e == cudaSuccess) {
-        fg::bias_grad_kernel<fg::COUT4><<<152 * 4, 256, 0, s>>>(m->g16, n, G + Y.b[3]);
+        fg::bias_grad_kernel<fg::COUT4><<<fg::sm_count() * 4, 256, 0, s>>>(m->g16, n, G + Y.b[3]);
         fg::count_launch();
         e = cudaGetLastError();
     }
@@ -729,7 +777,7 @@ FOCSS_API focss_status focss_cnn_loss_grad(focss_cnn* m, const focss_field* y, c
     for (int l = 2; l >= 1 && e == cudaSuccess; --l) {
         e = fg::conv_wgrad<fg::CW, fg::CW>(g, m->act[l], G + Y.w[l], L, B, s);
         if (e == cudaSuccess) {
-            fg::bias_grad_kernel<fg::CW><<<152 * 4, 256, 0, s>>>(g, n, G + Y.b[l]);
+            fg::bias_grad_kernel<fg::CW><<<fg::sm_count() * 4, 256, 0, s>>>(g, n, G + Y.b[l]);
             fg::count_launch();
             e = cudaGetLastError();
         }
@@ -739,7 +787,7 @@ FOCSS_API focss_status focss_cnn_loss_grad(focss_cnn* m, const focss_field* y, c
     // layer 1: weights and bias only
     if (e == cudaSuccess) e = fg::conv_wgrad<fg::CIN0, fg::CW>(g, m->act[0], G + Y.w[0], L, B, s);
     if (e == cudaSuccess) {
-        fg::bias_grad_kernel<fg::CW><<<152 * 4, 256, 0, s>>>(g, n, G + Y.b[0]);
+        fg::bias_grad_kernel<fg::CW><<<fg::sm_count() * 4, 256, 0, s>>>(g, n, G + Y.b[0]);
         fg::count_launch();
         e = cudaGetLastError();
     }

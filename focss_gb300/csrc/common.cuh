@@ -56,9 +56,12 @@ __device__ __forceinline__ float2 phase_rotation(float phi) {
 __device__ __forceinline__ float2 kerr_rotate(float2 v, float phi) {
     float cm1, s;
     if (fabsf(phi) <= 0.25f) {
+        // The increment multiplies v, so sin and cos - 1 need FP32 accuracy
+        // relative to themselves: Taylor to phi^5 and phi^6 (truncation below
+        // 5e-8 and 1.3e-8 relative at |phi| = 1/4).
         const float p2 = phi * phi;
-        s = phi * fmaf(p2, fmaf(p2, fmaf(p2, -1.0f / 5040.0f, 1.0f / 120.0f), -1.0f / 6.0f), 1.0f);
-        cm1 = p2 * fmaf(p2, fmaf(p2, fmaf(p2, 1.0f / 40320.0f, -1.0f / 720.0f), 1.0f / 24.0f), -0.5f);
+        s = phi * fmaf(p2, fmaf(p2, 1.0f / 120.0f, -1.0f / 6.0f), 1.0f);
+        cm1 = p2 * fmaf(p2, fmaf(p2, -1.0f / 720.0f, 1.0f / 24.0f), -0.5f);
     } else {
         const float2 r = phase_rotation(phi);  // cos(phi) <= 0.97: cos - 1 is exact
         cm1 = r.x - 1.0f;

@@ -8,7 +8,7 @@ namespace fg {
 namespace {
 inline int grid_for(size_t n, int threads) {
     size_t g = (n + threads - 1) / threads;
-    if (g > (size_t)152 * 32) g = (size_t)152 * 32;
+    if (g > (size_t)sm_count() * 32) g = (size_t)sm_count() * 32;
     return (int)(g ? g : 1);
 }
 }  // namespace

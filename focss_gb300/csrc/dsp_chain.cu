@@ -25,7 +25,7 @@ namespace {
 
 inline int grid_for(size_t n, int threads) {
     size_t g = (n + threads - 1) / threads;
-    if (g > (size_t)152 * 32) g = (size_t)152 * 32;
+    if (g > (size_t)sm_count() * 32) g = (size_t)sm_count() * 32;
     return (int)(g ? g : 1);
 }
 
@@ -33,7 +33,7 @@ inline int grid_for(size_t n, int threads) {
 // about 8 CTAs of 256 threads per SM over the whole launch (each CTA forms
 // its realization's FP64 scale once, so fewer, longer CTAs amortize it).
 inline dim3 grid_per_realization(size_t per, int batch) {
-    const size_t by_work = (per + 255) / 256, by_fill = ((size_t)152 * 8 + batch - 1) / (size_t)batch;
+    const size_t by_work = (per + 255) / 256, by_fill = ((size_t)sm_count() * 8 + batch - 1) / (size_t)batch;
     size_t gx = by_work < by_fill ? by_work : by_fill;
     return dim3((unsigned)(gx ? gx : 1), (unsigned)batch);
 }

@@ -131,6 +131,9 @@ struct Field {
 };
 
 // ---- helpers implemented in capi.cu
+// Streaming multiprocessors of the current device (queried once per device;
+// grid sizes are multiples of it).
+int sm_count();
 focss_status set_error(Ctx* ctx, focss_status st, const std::string& msg);
 focss_status cuda_check(Ctx* ctx, cudaError_t e, const char* what);
 focss_status get_plan(Ctx* ctx, int N, const Plan** out);  // balanced split

@@ -292,7 +292,7 @@ struct LdbpModel {
 
 inline int gridn(size_t n) {
     size_t g = (n + 255) / 256;
-    return (int)std::max<size_t>(1, std::min<size_t>(g, 152 * 16));
+    return (int)std::max<size_t>(1, std::min<size_t>(g, (size_t)fg::sm_count() * 16));
 }
 }  // namespace
 

@@ -36,7 +36,7 @@ namespace {
 constexpr int GT = 64;  // Gram tile (features)
 inline int grid_for_(size_t n) {
     const size_t g = (n + 255) / 256;
-    return (int)std::min<size_t>(g ? g : 1, (size_t)152 * 32);
+    return (int)std::min<size_t>(g ? g : 1, (size_t)sm_count() * 32);
 }
 constexpr int GK = 16;  // samples per shared-memory chunk
 constexpr int kFlush = 1;  // chunks summed in FP32 before an FP64 accumulation (16 samples; 64 measurably loses accuracy)
@@ -431,7 +431,7 @@ cudaError_t fit_alloc(FitBuffers& b, const std::vector<Feature>& fs, size_t kp, 
 // Splits each of `cols` columns of ns samples over enough CTAs to give the
 // GPU about 8 CTAs of 256 threads per SM, at least 4096 samples per CTA.
 inline unsigned column_split(int cols, size_t ns) {
-    const size_t by_work = (ns + 4095) / 4096, by_fill = ((size_t)152 * 8 + cols - 1) / (size_t)cols;
+    const size_t by_work = (ns + 4095) / 4096, by_fill = ((size_t)sm_count() * 8 + cols - 1) / (size_t)cols;
     const size_t y = std::min(by_work, by_fill);
     return (unsigned)std::max<size_t>(1, std::min<size_t>(y, 65535));
 }
@@ -478,7 +478,7 @@ cudaError_t fit_finish(FitBuffers& b, size_t kp, size_t ns, int nf, int nfp, dou
     // that merge the splits few.
     const int tiles = (nfp / GT) * (nfp / GT + 1) / 2;
     const int kmax = std::max(1, std::min(256, (int)(kp / GK)));
-    constexpr int kWave = 152 * 2;
+    const int kWave = sm_count() * 2;
     auto per_wave = [&](int k) { return (double)k / (double)((tiles * k + kWave - 1) / kWave); };
     double best = 0.0;
     for (int k = 1; k <= kmax; ++k) best = std::max(best, per_wave(k));

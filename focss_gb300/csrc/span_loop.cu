@@ -80,7 +80,7 @@ __global__ void amp_graph_kernel(float2* __restrict__ d, int samples, size_t n, 
 
 int amp_grid(size_t n) {
     size_t g = (n + 255) / 256;
-    if (g > (size_t)152 * 32) g = (size_t)152 * 32;
+    if (g > (size_t)sm_count() * 32) g = (size_t)sm_count() * 32;
     return (int)(g ? g : 1);
 }
 

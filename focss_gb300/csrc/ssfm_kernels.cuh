@@ -272,7 +272,12 @@ __device__ __forceinline__ void col_work(const PassArgs& a, int op, const SsfmSt
 // A CTA holds the same C columns of every mode of one realization (a.modes
 // groups of C*P threads; 1 or 2 modes), so the Kerr phase can use the power
 // summed over modes (Field::power, src/focss/field.cpp:164-171).  The launch
-// bound (2 groups, 1 CTA) keeps the same 128-register budget as 1 group x 2 CTAs.
+// bound of 2 groups x 1 CTA fixes the register budget at 65536 / (2 C P)
+// per thread (64 for N1 = 512: 2 x 512 threads), exactly what two
+// single-mode CTAs (1 group each) need to share an SM, so the two-CTA
+// residency of the single-mode launches cannot be lost to a register
+// heuristic; a bound of (C P, 2) would express the same budget but reject
+// the two-mode launches of 2 C P threads.
 template <int N1, int C>
 __global__ void __launch_bounds__(2 * C * ColFFT<N1>::P, 1) col_kernel(const PassArgs a) {
     constexpr int P = ColFFT<N1>::P, Q = ColFFT<N1>::Q;
@@ -362,7 +367,11 @@ __device__ __forceinline__ void row_work(const PassArgs& a, int op, float2* data
     for (int j = 0; j < Q; ++j) v[j] = base[P * j];
     __syncthreads();
     const RowLayout<P> lay{rl * Q * (P + 1)};
-    if (op != ROW_INV) fft_pq<P, Q, false, false>(v, sx, lay, t, s_tw);
+    // Lifting sub-FFTs with a mirrored inverse, as in the column pass: the
+    // forward transform's constant roundings are undone exactly by the
+    // inverse, so between the two they act only through their commutator
+    // with the (near-identity) Kerr step of the next column pass.
+    if (op != ROW_INV) fft_pq_lift<P, Q, false>(v, sx, lay, t, s_tw);
     const int N = a.N, N1 = a.N1;
     if (op == ROW_SSFM) {
         // exp(-alpha hl/2)/N * exp(i beta2/2 hl w_k^2) (ssfm.cpp:142-158), w_k = k' dw,
@@ -409,7 +418,7 @@ __device__ __forceinline__ void row_work(const PassArgs& a, int op, float2* data
 #pragma unroll
         for (int j = 0; j < Q; ++j) v[j] = cscale(v[j], g);
     }
-    if (op != ROW_FWD) fft_pq<P, Q, true, false>(v, sx, lay, t, s_tw);
+    if (op != ROW_FWD) fft_pq_lift_inv<P, Q, false>(v, sx, lay, t, s_tw);
 #pragma unroll
     for (int j = 0; j < Q; ++j) base[P * j] = v[j];
 }

@@ -180,11 +180,14 @@ def _timed(fn, ctx, repeat=3):
 
 def learned_dbp(link: Link, rx_train: Field, tx_train: Field, rx_test: Field, tx_test: Field, steps_per_span=2,
                 taps=63, mf_taps=63, iters=300, lr=2e-3, cnn_iters=300, cnn_lr=2e-3, cut=100, angle_steps=720,
-                seed=0):
+                seed=0, cnn_triplets=None):
     """Train the learned DBP (initialised from split-step DBP) and then the
-    correction CNN on (rx_train, tx_train); score both on the independent
-    (rx_test, tx_test).  Returns a dict of Q per realization and GPU times."""
-    from .cnn import CorrectionCNN, he_init
+    correction CNN (on the symbols and their perturbation triplets,
+    cnn.TRIPLETS unless given) on (rx_train, tx_train); score both on the
+    independent (rx_test, tx_test).  Returns a dict of Q per realization and
+    GPU times."""
+    from .cnn import TRIPLETS, CorrectionCNN, he_init
+    cnn_triplets = TRIPLETS if cnn_triplets is None else tuple(cnn_triplets)
     from .ldbp import LearnedDBP, rrc_response
     ctx = rx_train.ctx
     B = rx_train.batch
@@ -210,8 +213,8 @@ def learned_dbp(link: Link, rx_train: Field, tx_train: Field, rx_test: Field, tx
     q_ldbp = dsp.q2_factor(tx_test, pse.train_equalize(tx_test, y_test), cut)
     y_train = model.forward(rx_train)
     p_rms = float(np.sqrt(np.mean(np.abs(tx_train.numpy(np.complex64)) ** 2)))
-    net = CorrectionCNN(ns, B, p_rms, ctx=ctx)
-    net.set_params(he_init(np.random.default_rng(seed)))
+    net = CorrectionCNN(ns, B, p_rms, ctx=ctx, triplets=cnn_triplets)
+    net.set_params(he_init(np.random.default_rng(seed), n_triplets=len(cnn_triplets)))
     t0 = time.perf_counter()
     chist = net.fit(y_train, tx_train, iters=cnn_iters, lr=cnn_lr)
     ctx.sync()
@@ -243,7 +246,7 @@ def plain_dbp_q(link: Link, rx2: Field, tx: Field, steps_per_span, cut=100, angl
 
 def learned_vs_plain(link: Link, power_dbm, n_symbols=1 << 15, batch=8, seed=0, ctx=None, steps_per_span=4,
                      plain_steps=(1, 4, 100), iters=300, lr=3e-4, cnn_iters=200, cnn_lr=1e-3, taps=63,
-                     mf_taps=255):
+                     mf_taps=255, cnn_triplets=None):
     """Learned DBP at `steps_per_span` (and with the correction CNN) against
     plain DBP on one link and launch power: independent training and test sets
     of `batch` realizations x `n_symbols` (fresh symbols and ASE), propagated
@@ -261,7 +264,7 @@ def learned_vs_plain(link: Link, power_dbm, n_symbols=1 << 15, batch=8, seed=0, 
         q, ms = plain_dbp_q(link, rb, tb, k)
         out["plain_%d" % k] = {"q_db": float(np.mean(q)), "ms": ms}
     r = learned_dbp(link, ra, ta, rb, tb, steps_per_span=steps_per_span, taps=taps, mf_taps=mf_taps, iters=iters,
-                    lr=lr, cnn_iters=cnn_iters, cnn_lr=cnn_lr)
+                    lr=lr, cnn_iters=cnn_iters, cnn_lr=cnn_lr, cnn_triplets=cnn_triplets)
     out["learned_%d" % steps_per_span] = {"q_db": float(np.mean(r["q_learned"])), "ms": r["ms_learned"],
                                           "train_s": r["train_s"]}
     out["learned_%d_cnn" % steps_per_span] = {"q_db": float(np.mean(r["q_learned_cnn"])),

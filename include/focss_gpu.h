@@ -447,17 +447,26 @@ FOCSS_API focss_status focss_ldbp_adam_step(focss_ldbp* model, double lr, double
 
 /* No reference counterpart: the convolutional correction stage after the
  * learned DBP.  z = y + s (d_re + i d_im) with d = a 4-layer 1D CNN
- * (64 channels, kernel 9, ReLU, zero padding) of x = [Re y/s, Im y/s];
+ * (64 channels, kernel 9, ReLU, zero padding) of x = [Re y/s, Im y/s] and
+ * optional perturbation triplets of y (focss_cnn_set_triplets);
  * BF16 weights (FP32 masters), FP32 accumulation on the tensor cores.
  * y, z, tx: fields of `length` symbols x `batch`, one mode.
  * Parameters (float): per layer l = 1..4 W_l[cout][9][cin] then b_l[cout],
  * with (cin, cout) = (16, 64), (64, 64), (64, 64), (64, 16); input channels
- * 2..15 and output channels 2..15 are padding. */
+ * beyond the triplets and output channels 2..15 are padding. */
 typedef struct focss_cnn focss_cnn;
 FOCSS_API focss_status focss_cnn_create(focss_ctx* ctx, int channels, int kernel, int length, int batch,
                                         double input_scale, focss_cnn** out);
 FOCSS_API focss_status focss_cnn_destroy(focss_cnn* model);
 FOCSS_API int focss_cnn_num_params(const focss_cnn* model);
+/* First-order perturbation triplets as further input channels (no reference
+ * counterpart; the terms are those of SINO::term, src/focss/equalizer/
+ * sino.cpp:161-171): input channels 2+2j and 3+2j (j < count <= 7) carry
+ * Re and Im of (T(m_j, n_j) + T(-m_j, -n_j)) / input_scale^3, T(0, 0) alone
+ * for m_j = n_j = 0, with T(m, n)[k] = y[k+m] y[k+n] conj(y[k+m+n]) and
+ * symbols outside the realization counting as zero.  count = 0 (the default)
+ * leaves those channels zero.  |m_j|, |n_j| <= length. */
+FOCSS_API focss_status focss_cnn_set_triplets(focss_cnn* model, int count, const int32_t* m, const int32_t* n);
 FOCSS_API focss_status focss_cnn_set_params(focss_cnn* model, const float* params, int n);
 FOCSS_API focss_status focss_cnn_get_params(focss_cnn* model, float* params, float* grads, int n);
 FOCSS_API focss_status focss_cnn_forward(focss_cnn* model, const focss_field* y, focss_field* z);

@@ -53,12 +53,45 @@ def wgrad(g, x):
     return np.stack([np.einsum("blo,bli->oi", g, shift(x, kk - HALF)) for kk in range(KW)], axis=1)
 
 
-def forward(flat, y, s):
+def _at(y, d):
+    """y[:, k + d] with zero outside the realization (y: B, L)."""
+    out = np.zeros_like(y)
+    L = y.shape[1]
+    if d >= 0:
+        out[:, : max(0, L - d)] = y[:, d:]
+    else:
+        out[:, -d:] = y[:, : L + d]
+    return out
+
+
+def triplet(y, m, n):
+    """T(m, n)[k] = y[k+m] y[k+n] conj(y[k+m+n]) (src/focss/equalizer/sino.cpp:161-171, one mode)."""
+    return _at(y, m) * _at(y, n) * np.conj(_at(y, m + n))
+
+
+def triplet_features(y, pairs):
+    """Feature j = T(m_j, n_j) + T(-m_j, -n_j) (T(0, 0) alone), as focss_cnn_set_triplets."""
+    out = []
+    for m, n in pairs:
+        f = triplet(y, m, n)
+        if m != 0 or n != 0:
+            f = f + triplet(y, -m, -n)
+        out.append(f)
+    return out
+
+
+def forward(flat, y, s, triplets=()):
     P = unpack(flat)
     B, L = y.shape
     x0 = np.zeros((B, L, 16))
     x0[..., 0] = y.real / s
     x0[..., 1] = y.imag / s
+    # FP32 products as on the GPU, then the 1/s^3 scale
+    y32 = y.astype(np.complex64)
+    for j, f in enumerate(triplet_features(y32, triplets)):
+        f = f.astype(np.complex64).astype(np.complex128)
+        x0[..., 2 + 2 * j] = f.real / s ** 3
+        x0[..., 3 + 2 * j] = f.imag / s ** 3
     acts = [bf16(x0)]
     for l in range(3):
         w, b = P[l]
@@ -69,9 +102,9 @@ def forward(flat, y, s):
     return z, acts
 
 
-def loss_grad(flat, y, tx, s):
+def loss_grad(flat, y, tx, s, triplets=()):
     P = unpack(flat)
-    z, acts = forward(flat, y, s)
+    z, acts = forward(flat, y, s, triplets)
     M = y.size
     d = z - tx
     loss = float(np.sum(np.abs(d) ** 2) / M)
