@@ -494,7 +494,7 @@ def precision_section(fg, ctx, spans=None):
 LVP = dict(
     wdm_link="5-ch WDM 20 x 80 km ADAPTIVE + ASE, centre channel at 2 sps",
     wdm_powers_dbm=[-2.0, 4.0], single_channel="1 channel 4 sps, 20 x 80 km ADAPTIVE + ASE, 3 dBm",
-    realizations=8, symbols_per_realization=2 ** 15, steps_per_span=4, iters=300, cnn_iters=200,
+    realizations=8, symbols_per_realization=2 ** 15, steps_per_span=4, iters=300, cnn_iters=1000,
 )
 
 
@@ -803,7 +803,7 @@ def ppe_section(fg, ctx, stream):
 DBP_SWEEP = dict(
     workload="learned_dbp_sweep_wdm5_centre_2^20sym_-2..+4dBm",
     powers_dbm=[-2, -1, 0, 1, 2, 3, 4], realizations=32, symbols_per_realization=2 ** 15, steps_per_span=4,
-    taps=63, mf_taps=255, iters=300, lr=3e-4, cnn_iters=200, cnn_lr=1e-3,
+    taps=63, mf_taps=255, iters=300, lr=3e-4, cnn_iters=1000, cnn_lr=3e-4,
 )
 
 

@@ -32,7 +32,10 @@ def layout():
 TRIPLETS = ((0, 0), (0, 1), (0, 2), (0, 3), (1, 1), (1, -1), (1, 2))
 
 
-def he_init(rng, zero_last=True, n_triplets=0):
+def he_init(rng, zero_last=True, n_triplets=0, last_scale=1.0):
+    """He-normal weights, zero biases; the unused input channels of layer 1 and
+    output channels of layer 4 zero; layer 4 zero (zero_last: the network
+    starts as the identity z = y) or scaled by last_scale."""
     lay, total = layout()
     p = np.zeros(total, np.float32)
     used = 2 + 2 * n_triplets  # input channels in use in layer 1
@@ -43,8 +46,7 @@ def he_init(rng, zero_last=True, n_triplets=0):
             w[:, :, used:] = 0
         if l == 3:
             w[2:] = 0
-            if zero_last:
-                w[:] = 0
+            w *= 0.0 if zero_last else last_scale
         p[wo:wo + w.size] = w.ravel()
     return p
 
@@ -86,6 +88,14 @@ class CorrectionCNN:
 
     def adam_step(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
         check(lib().focss_cnn_adam_step(self.h, lr, beta1, beta2, eps), self.ctx.h)
+
+    def identity_params(self, flat):
+        """flat with layer 4 zeroed: the network then passes y through."""
+        p = np.array(flat, np.float32)
+        lay, _ = layout()
+        wo, shape, bo, cout = lay[3]
+        p[wo:bo + cout] = 0
+        return p
 
     def fit(self, y: Field, tx: Field, iters=100, lr=1e-3):
         hist = []
