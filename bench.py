@@ -201,9 +201,9 @@ def cpu_sample(threads, segment_m):
     return k * N / dt / 1e9, dt, k
 
 
-# Metres of the first span per realization in a CPU sample: ~2 s of FP64
+# Metres of the first span per realization in a CPU sample: ~5 s of FP64
 # work on 16 host cores per reference-arm step, ~10 s for the baseline.
-CPU_REFERENCE_SEGMENT_M = 500.0
+CPU_REFERENCE_SEGMENT_M = 1000.0
 CPU_BASELINE_SEGMENT_M = 2500.0
 
 
@@ -493,14 +493,14 @@ def precision_section(fg, ctx, spans=None):
 
 LVP = dict(
     wdm_link="5-ch WDM 20 x 80 km ADAPTIVE + ASE, centre channel at 2 sps",
-    wdm_powers_dbm=[-2.0, 4.0], single_channel="1 channel 4 sps, 20 x 80 km ADAPTIVE + ASE, 3 dBm",
-    realizations=8, symbols_per_realization=2 ** 15, steps_per_span=4, iters=300, cnn_iters=1000,
+    wdm_powers_dbm=[-2.0, 2.0, 4.0], single_channel="1 channel 4 sps, 20 x 80 km ADAPTIVE + ASE, 3 dBm",
+    realizations=16, symbols_per_realization=2 ** 15, steps_per_span=4, iters=300, cnn_iters=1000,
 )
 
 
 def learned_vs_plain_section(fg, ctx):
     """Learned DBP at 4 steps/span against plain DBP at 1 / 4 / 100
-    steps/span: Q (dB, mean over 8 test realizations x 2^15 symbols) and DBP
+    steps/span: Q (dB, mean over 16 test realizations x 2^15 symbols) and DBP
     time (ms) per launch power, on the WDM link's centre channel and on a
     single-channel link (training and test sets generated by the GPU split
     step).  Compact: [q_db, ms] per entry."""
