@@ -396,6 +396,15 @@ def autotune(samples: int, batch: int, ctx: Context | None = None):
 
 
 SPLIT_SINGLE_CTA = -1  # FOCSS_SPLIT_SINGLE_CTA: one CTA per realization, field in shared memory
+STAGING_LOADS, STAGING_BULK = 0, 1  # FOCSS_STAGING_*: how the row pass moves its rows
+
+
+def set_row_staging(mode: int, ctx: Context | None = None):
+    """Row-pass staging of this context's split steps: STAGING_LOADS
+    (per-thread coalesced loads, the default) or STAGING_BULK (TMA bulk
+    copies); the results are the same bit for bit."""
+    ctx = ctx or Context.default()
+    check(lib().focss_set_row_staging(ctx.h, int(mode)), ctx.h)
 
 
 def set_fft_split(samples: int, log2_n1: int, ctx: Context | None = None):

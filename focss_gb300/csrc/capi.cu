@@ -95,6 +95,7 @@ focss_status get_plan_split(Ctx* ctx, int N, int log2N1, const Plan** out) {
         cudaFree(p.tw);
         return cuda_check(ctx, e, "twiddle upload");
     }
+    p.row_staging = ctx->row_staging;
     auto res = ctx->plans.emplace(key, p);
     *out = &res.first->second;
     return FOCSS_OK;
@@ -438,6 +439,13 @@ FOCSS_API focss_status focss_ssfm_run(focss_ctx* c, focss_field* f, const focss_
     if (direction != 1.0 && direction != -1.0)
         return fg::set_error(c, FOCSS_ERR_INVALID_ARG, "direction must be FOCSS_FORWARD or FOCSS_BACKWARD");
     return fg::ssfm_run(c, f, *fiber, *opts, direction, steps_out);
+}
+
+FOCSS_API focss_status focss_set_row_staging(focss_ctx* c, int mode) {
+    if (!c || (mode != FOCSS_STAGING_LOADS && mode != FOCSS_STAGING_BULK)) return FOCSS_ERR_INVALID_ARG;
+    c->row_staging = mode;
+    for (auto& kv : c->plans) kv.second.row_staging = mode;
+    return FOCSS_OK;
 }
 
 // Step-grid record / replay: device copies of the step lists live in scratch

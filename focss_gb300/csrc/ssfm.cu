@@ -89,17 +89,21 @@ bool fft_size_supported(int N) {
 constexpr int kMaxDevices = 64;
 std::mutex g_launch_mutex;
 
-// The cached launch of pass kind `kind` (0 column, 1 row) for log2 length lg
+// The cached launch of pass kind `kind` (0 column, 1 row, 2 row with
+// bulk-copy staging) for log2 length lg
 // on the current device, opted in to `smem` bytes of dynamic shared memory.
 cudaError_t cached_launch(int kind, int lg, size_t smem, Launch* out) {
-    static Launch cache[kMaxDevices][2][16];
+    static Launch cache[kMaxDevices][3][16];
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices || lg < 0 || lg >= 16) return cudaErrorInvalidValue;
     std::lock_guard<std::mutex> lock(g_launch_mutex);
     Launch& l = cache[dev][kind][lg];
-    if (!l.fn) l = kind == 0 ? col_launch_for(lg) : row_launch_for(lg);
+    if (!l.fn) {
+        l = kind == 0 ? col_launch_for(lg) : row_launch_for(lg);
+        if (kind == 2) l.fn = l.fn_bulk;
+    }
     if (!l.fn) return cudaErrorInvalidValue;
     if (!l.attr_set || smem > l.smem) {
         e = cudaFuncSetAttribute((const void*)l.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -140,7 +144,7 @@ cudaError_t launch_row(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
     const int Q = p.N2 / P;
     int R = l.per_block;
     const size_t smem = sizeof(float4) * ((size_t)p.N2 + 512) + sizeof(float2) * (size_t)R * Q * (P + 1);
-    cudaError_t e = cached_launch(1, p.log2N2, smem, &l);
+    cudaError_t e = cached_launch(p.row_staging == FOCSS_STAGING_BULK ? 2 : 1, p.log2N2, smem, &l);
     if (e != cudaSuccess) return e;
     a.N = p.N;
     a.N1 = p.N1;
@@ -254,6 +258,7 @@ focss_status ssfm_run(Ctx* ctx, Field* f, const focss_fiber& fib, const focss_ss
     st = cuda_check(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(int) * 4, s), "memset counters");
     if (st != FOCSS_OK) return st;
     PassArgs a = ssfm_args(f, fib, o, dir, ctx->d_state, ctx->d_counters);
+    a.fault = ctx->d_counters + 2;
     if (grid) {
         a.prm.h_record = grid->record;
         a.prm.h_replay = grid->replay;
@@ -341,13 +346,18 @@ focss_status ssfm_finish(Ctx* ctx, Field* f, const focss_ssfm_opts& o, int* step
     cudaStream_t s = ctx->stream;
     focss_status st;
     std::vector<SsfmState> hs(f->batch);
+    int fault = 0;
     st = cuda_check(ctx,
                     cudaMemcpyAsync(hs.data(), ctx->d_state, sizeof(SsfmState) * f->batch,
                                     cudaMemcpyDeviceToHost, s),
                     "state readback");
     if (st != FOCSS_OK) return st;
+    st = cuda_check(ctx, cudaMemcpyAsync(&fault, ctx->d_counters + 2, sizeof(int), cudaMemcpyDeviceToHost, s),
+                    "fault readback");
+    if (st != FOCSS_OK) return st;
     st = cuda_check(ctx, cudaStreamSynchronize(s), "ssfm sync");
     if (st != FOCSS_OK) return st;
+    if (fault) return set_error(ctx, FOCSS_ERR_TIMEOUT, "ssfm_run: a bulk-copy wait ran out");
     if (ctx->profiling) prof_collect(ctx);
     for (int b = 0; b < f->batch; ++b) {
         if (hs[b].action != COL_IDLE)

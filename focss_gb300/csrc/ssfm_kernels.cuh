@@ -356,16 +356,13 @@ struct PhaseRun {
     }
 };
 
+// The row work on the thread's elements v[j] = x[t + P j] of row k1, in
+// registers from load to store.
 template <int N2>
-__device__ __forceinline__ void row_work(const PassArgs& a, int op, float2* data, int k1, int rl, int t,
+__device__ __forceinline__ void row_core(const PassArgs& a, int op, float2 (&v)[PQ<N2>::Q], int k1, int rl, int t,
                                          const float4* s_tw, const float4* s_T, float2* sx, float g,
-                                         unsigned long long dhi, unsigned long long dlo, int ld) {
+                                         unsigned long long dhi, unsigned long long dlo) {
     constexpr int P = PQ<N2>::P, Q = PQ<N2>::Q;
-    float2* base = data + (size_t)k1 * ld + t;
-    float2 v[Q];
-#pragma unroll
-    for (int j = 0; j < Q; ++j) v[j] = base[P * j];
-    __syncthreads();
     const RowLayout<P> lay{rl * Q * (P + 1)};
     // Lifting sub-FFTs with a mirrored inverse, as in the column pass: the
     // forward transform's constant roundings are undone exactly by the
@@ -419,6 +416,19 @@ __device__ __forceinline__ void row_work(const PassArgs& a, int op, float2* data
         for (int j = 0; j < Q; ++j) v[j] = cscale(v[j], g);
     }
     if (op != ROW_FWD) fft_pq_lift_inv<P, Q, false>(v, sx, lay, t, s_tw);
+}
+
+template <int N2>
+__device__ __forceinline__ void row_work(const PassArgs& a, int op, float2* data, int k1, int rl, int t,
+                                         const float4* s_tw, const float4* s_T, float2* sx, float g,
+                                         unsigned long long dhi, unsigned long long dlo, int ld) {
+    constexpr int P = PQ<N2>::P, Q = PQ<N2>::Q;
+    float2* base = data + (size_t)k1 * ld + t;
+    float2 v[Q];
+#pragma unroll
+    for (int j = 0; j < Q; ++j) v[j] = base[P * j];
+    __syncthreads();
+    row_core<N2>(a, op, v, k1, rl, t, s_tw, s_T, sx, g, dhi, dlo);
 #pragma unroll
     for (int j = 0; j < Q; ++j) base[P * j] = v[j];
 }
@@ -447,6 +457,96 @@ __global__ void __launch_bounds__(R* PQ<N2>::P, 2) row_kernel(const PassArgs a) 
     const int rl = threadIdx.x / P, t = threadIdx.x % P;
     row_work<N2>(a, st ? (int)ROW_SSFM : a.op, a.data + (size_t)b * a.N, blockIdx.x * R + rl, rl, t, s_tw, s_T, sx,
                  g, dhi, dlo, N2);
+}
+
+// ---------------------------------------------------------------- row pass, bulk-copy staging
+// The same row pass with its rows moved by the TMA bulk-copy engine
+// (cp.async.bulk): one thread queues the CTA's R rows (N2 x 8 B each,
+// contiguous in HBM) into the rows' exchange-buffer slots behind one
+// mbarrier while the CTA loads its tables, the threads read their elements
+// from shared memory, and each row goes back to HBM as one bulk store.  The
+// wait is bounded: past kBulkWaitCap polls the CTA records a fault (a.fault)
+// and skips its rows.
+constexpr int kBulkWaitCap = 1 << 22;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+    for (int i = 0; i < kBulkWaitCap; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+template <int N2, int R>
+__global__ void __launch_bounds__(R* PQ<N2>::P, 2) row_kernel_bulk(const PassArgs a) {
+    constexpr int P = PQ<N2>::P, Q = PQ<N2>::Q;
+    constexpr uint32_t kRowBytes = N2 * sizeof(float2);
+    static_assert(kRowBytes % 16 == 0 && (Q * (P + 1) * sizeof(float2)) % 16 == 0, "bulk copies move 16-byte units");
+    extern __shared__ float4 smem4[];
+    float4* s_tw = smem4;                                    // W_N2^e (double-float)
+    float4* s_T = s_tw + N2;                                 // exp(2 pi i j/512)
+    float2* sx = reinterpret_cast<float2*>(s_T + 512);       // R * Q * (P+1): landing zone and exchange
+    __shared__ __align__(8) unsigned long long bar;
+
+    const int b = blockIdx.y;  // realization * modes + mode
+    const SsfmState* st = a.state ? a.state + b / (a.modes > 1 ? a.modes : 1) : nullptr;
+    unsigned long long dhi = 0ull, dlo = 0ull;
+    float g = a.scale;
+    if (st) {
+        if (!*(volatile const int*)&st->row_active) return;  // before any copy is queued
+        dhi = st->disp_hi;
+        dlo = st->disp_lo << 32;
+        g = st->lin_gain;
+    }
+    const int k1_0 = blockIdx.x * R;
+    float2* rows = a.data + (size_t)b * a.N + (size_t)k1_0 * N2;
+    const uint32_t ub = smem_addr(&bar);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(ub) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ub), "r"(R * kRowBytes)
+                     : "memory");
+        for (int r = 0; r < R; ++r)
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                             smem_addr(sx + (size_t)r * Q * (P + 1))),
+                         "l"(rows + (size_t)r * N2), "r"(kRowBytes), "r"(ub)
+                         : "memory");
+    }
+    for (int i = threadIdx.x; i < N2; i += blockDim.x) s_tw[i] = a.tw[a.N1 + i];
+    if (st)
+        for (int i = threadIdx.x; i < 512; i += blockDim.x) s_T[i] = a.tw[2 * a.N1 + 2 * N2 + i];
+    __syncthreads();  // barrier initialised, tables in place
+    if (!mbar_wait_bounded(ub, 0)) {
+        if (a.fault) atomicExch(a.fault, 1);
+        if (threadIdx.x == 0) mbar_wait_bounded(ub, 0);  // the copies must land before the CTA exits
+        return;
+    }
+    const int rl = threadIdx.x / P, t = threadIdx.x % P;
+    float2* row_s = sx + (size_t)rl * Q * (P + 1);
+    float2 v[Q];
+#pragma unroll
+    for (int j = 0; j < Q; ++j) v[j] = row_s[t + P * j];
+    __syncwarp();  // the row's lanes (one warp holds whole rows) have read before the exchange writes
+    row_core<N2>(a, st ? (int)ROW_SSFM : a.op, v, k1_0 + rl, rl, t, s_tw, s_T, sx, g, dhi, dlo);
+#pragma unroll
+    for (int j = 0; j < Q; ++j) row_s[t + P * j] = v[j];
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the writes, visible to the copy engine
+    __syncwarp();
+    if (t == 0) {
+        asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(rows + (size_t)rl * N2),
+                     "r"(smem_addr(row_s)), "r"(kRowBytes)
+                     : "memory");
+        asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+        asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // shared memory read before exit
+    }
 }
 
 // ---------------------------------------------------------------- single CTA
@@ -535,6 +635,7 @@ __global__ void __launch_bounds__(kBlockThreads, BlockShape<N1, N2>::SMEM <= 113
 typedef void (*PassFn)(PassArgs);
 struct Launch {
     PassFn fn = nullptr;
+    PassFn fn_bulk = nullptr;  // row pass with bulk-copy staging
     int threads = 0, per_block = 0;
     size_t smem = 0;
     bool attr_set = false;
@@ -575,6 +676,7 @@ Launch row_launch_for(int log2N2);
     Launch row_launch_##LG() {                                                 \
         Launch l;                                                              \
         l.fn = row_kernel<L, RowShape<L>::R>;                                  \
+        l.fn_bulk = row_kernel_bulk<L, RowShape<L>::R>;                        \
         l.threads = RowShape<L>::R * PQ<L>::P;                                 \
         l.per_block = RowShape<L>::R;                                          \
         return l;                                                              \

@@ -149,6 +149,17 @@ FOCSS_API focss_status focss_field_ifft(focss_field* field);
 FOCSS_API focss_status focss_ssfm_run(focss_ctx* ctx, focss_field* field, const focss_fiber* fiber,
                                       const focss_ssfm_opts* opts, double direction, int* steps_out);
 
+/* How the split-step row pass moves its rows between HBM and shared memory
+ * (no reference counterpart): FOCSS_STAGING_LOADS (default) with coalesced
+ * 8-byte loads and stores by every thread, FOCSS_STAGING_BULK with the TMA
+ * bulk-copy engine (cp.async.bulk, one copy per row behind an mbarrier).
+ * The arithmetic is the same, so the results are the same bit for bit.
+ * Applies to this context's split-step and transform passes from the next
+ * launch on. */
+#define FOCSS_STAGING_LOADS 0
+#define FOCSS_STAGING_BULK 1
+FOCSS_API focss_status focss_set_row_staging(focss_ctx* ctx, int mode);
+
 /* Step-grid record and replay.  The reference has no counterpart: SSFM::run
  * only prints the adaptive step count (src/focss/solver/ssfm.cpp:117).  An
  * ADAPTIVE grid takes each step size from the current field's peak power
