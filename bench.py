@@ -787,9 +787,14 @@ def ppe_section(fg, ctx, stream):
     model.equalize(y, tx, c["prune"])  # warm-up
     eq, ppe_ms = _stream_ms(torch, stream, lambda: model.equalize(y, tx, c["prune"]))
     q_ppe = float(np.mean(dsp.q2_factor(tx, pse.train_equalize(tx, eq), c["cut"])))
+    import ctypes as C
+    peak = C.c_double()
+    fg.lib().focss_measure_fp32_fma(ctx.h, C.byref(peak))
+    tflops = 8.0 * m.size * c["symbols"] / ppe_ms / 1e9
     out = {"config": c, "terms": int(m.size), "fit_s": fit_s, "q_db_cdc": q_cdc,
            "ppe": {"q_db": q_ppe, "ms": ppe_ms, "msymbols_per_s": c["symbols"] / ppe_ms / 1e3,
-                   "gflops": 8.0 * m.size * c["symbols"] / ppe_ms / 1e6}}
+                   "gflops": tflops * 1e3, "fp32_fma_peak_tflops_measured": peak.value,
+                   "frac_of_fp32_peak": tflops / peak.value if peak.value > 0 else None}}
     rx2 = dsp.decimate(sig, osf // 2)
     for k in (1, 100):
         f = rx2.copy()

@@ -133,6 +133,7 @@ SIGNATURES = {
     "focss_ssfm_run_noalloc": (I, [P, P, I, I, D, C.POINTER(CFiber), C.POINTER(CSsfmOpts), D, P]),
     "focss_profile_enable": (I, [P, I]),
     "focss_profile_read": (I, [P, P, P, P, P, I]),
+    "focss_measure_fp32_fma": (I, [P, P]),
     "focss_launch_count": (C.c_longlong, []),
 }
 

@@ -519,6 +519,11 @@ FOCSS_API focss_status focss_ssfm_run_noalloc(void* stream, void* data, int samp
 FOCSS_API focss_status focss_profile_enable(focss_ctx* ctx, int enable);
 FOCSS_API focss_status focss_profile_read(focss_ctx* ctx, double* col_ms, long long* col_launches,
                                           double* row_ms, long long* row_launches, int reset);
+/* FP32 FMA throughput of this GPU (TFLOP/s, 2 flops per FMA), measured by a
+ * micro-kernel of independent FMA chains over whole waves of CTAs, best of 3
+ * timed launches; the denominator for FP32-bound kernels such as the triplet
+ * sum.  Changes no device setting. */
+FOCSS_API focss_status focss_measure_fp32_fma(focss_ctx* ctx, double* tflops);
 /* Total kernel launches issued by this library in this process. */
 FOCSS_API long long focss_launch_count(void);
 
