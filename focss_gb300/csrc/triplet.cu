@@ -18,7 +18,10 @@
 // reads are conflict-free.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <map>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "common.cuh"
@@ -172,6 +175,97 @@ bool build_terms(int n_terms, const int32_t* m, const int32_t* n, const double* 
     return true;
 }
 
+// Device term tables of recent term lists, per context: an equalizer applied
+// again with the same coefficients skips the host grouping and the upload.
+// The device buffer lives in ctx->tables (freed with the context); its
+// layout is {gm[ng], gnlo[ng], goff[ng+1], pad to 16 B, coef runs}.
+struct TermPlan {
+    int ng = 0, halo_q = 0, halo_a = 0;
+    size_t coef_offset = 0;
+};
+std::mutex g_term_mutex;
+std::map<std::pair<const Ctx*, std::string>, TermPlan> g_term_plans;
+constexpr int kMaxTermPlans = 16;
+
+uint64_t fnv1a(const void* p, size_t n, uint64_t h) {
+    const unsigned char* b = (const unsigned char*)p;
+    for (size_t i = 0; i < n; ++i) {
+        h ^= b[i];
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+
+std::string term_key(int n_terms, const int32_t* m, const int32_t* n, const double* c) {
+    uint64_t h1 = 1469598103934665603ull, h2 = 0x9E3779B97F4A7C15ull;
+    h1 = fnv1a(&n_terms, sizeof n_terms, h1);
+    h1 = fnv1a(m, sizeof(int32_t) * n_terms, h1);
+    h1 = fnv1a(n, sizeof(int32_t) * n_terms, h1);
+    h1 = fnv1a(c, sizeof(double) * 2 * n_terms, h1);
+    h2 = fnv1a(c, sizeof(double) * 2 * n_terms, h2);
+    h2 = fnv1a(n, sizeof(int32_t) * n_terms, h2);
+    h2 = fnv1a(m, sizeof(int32_t) * n_terms, h2);
+    char buf[64];
+    std::snprintf(buf, sizeof buf, "triplet:%016llx%016llx:%d", (unsigned long long)h1, (unsigned long long)h2,
+                  n_terms);
+    return buf;
+}
+
+// The cached device tables of a term list (built and uploaded on a miss).
+focss_status term_plan(Ctx* c, int n_terms, const int32_t* m, const int32_t* n, const double* coef,
+                       const char** dev, TermPlan* plan) {
+    const std::string key = term_key(n_terms, m, n, coef);
+    std::lock_guard<std::mutex> lock(g_term_mutex);
+    auto it = g_term_plans.find({c, key});
+    auto tt = c->tables.find(key);
+    if (it != g_term_plans.end() && tt != c->tables.end()) {
+        *dev = (const char*)tt->second;
+        *plan = it->second;
+        return FOCSS_OK;
+    }
+    int cached = 0;
+    for (auto& kv : c->tables) cached += kv.first.compare(0, 8, "triplet:") == 0;
+    if (cached >= kMaxTermPlans) {  // drop them all (in-flight kernels finish first)
+        cudaStreamSynchronize(c->stream);
+        for (auto kv = c->tables.begin(); kv != c->tables.end();) {
+            if (kv->first.compare(0, 8, "triplet:") == 0) {
+                cudaFree(kv->second);
+                g_term_plans.erase({c, kv->first});
+                kv = c->tables.erase(kv);
+            } else {
+                ++kv;
+            }
+        }
+    }
+    Terms t;
+    build_terms(n_terms, m, n, coef, t);
+    TermPlan p;
+    p.ng = (int)t.gm.size();
+    p.halo_q = t.halo_q;
+    p.halo_a = t.halo_a;
+    const size_t bytes_i = sizeof(int) * (3 * (size_t)p.ng + 1);
+    p.coef_offset = (bytes_i + 15) / 16 * 16;
+    std::vector<char> host(p.coef_offset + sizeof(float2) * t.coef.size(), 0);
+    int* hi = (int*)host.data();
+    std::copy(t.gm.begin(), t.gm.end(), hi);
+    std::copy(t.gnlo.begin(), t.gnlo.end(), hi + p.ng);
+    std::copy(t.goff.begin(), t.goff.end(), hi + 2 * p.ng);
+    std::copy(t.coef.begin(), t.coef.end(), (float2*)(host.data() + p.coef_offset));
+    void* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, host.size());
+    if (e != cudaSuccess) return cuda_check(c, e, "triplet tables");
+    e = cudaMemcpy(d, host.data(), host.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return cuda_check(c, e, "triplet upload");
+    }
+    c->tables[key] = d;
+    g_term_plans[{c, key}] = p;
+    *dev = (const char*)d;
+    *plan = p;
+    return FOCSS_OK;
+}
+
 }  // namespace
 
 // The triplet sum over `modes` consecutive rows of each realization of `in`
@@ -186,23 +280,14 @@ focss_status run_triplet_rows(Ctx* c, const float2* in, size_t in_bstride, int m
     for (int i = 0; i < n_terms; ++i)
         if (std::abs(m[i]) > 4096 || std::abs(n[i]) > 4096)
             return set_error(c, FOCSS_ERR_INVALID_ARG, "triplet: |m|, |n| must be <= 4096");
-    Terms t;
-    build_terms(n_terms, m, n, coef, t);
-    const size_t ng = t.gm.size();
-    const size_t bytes_i = sizeof(int) * (3 * ng + 1);
-    const size_t bytes = bytes_i + 16 + sizeof(float2) * t.coef.size();
-    char* d = (char*)scratch_buffer(c, 7, bytes);
-    if (!d) return set_error(c, FOCSS_ERR_OOM, "triplet scratch");
-    std::vector<int> hi(3 * ng + 1);
-    std::copy(t.gm.begin(), t.gm.end(), hi.begin());
-    std::copy(t.gnlo.begin(), t.gnlo.end(), hi.begin() + ng);
-    std::copy(t.goff.begin(), t.goff.end(), hi.begin() + 2 * ng);
-    float2* dcoef = (float2*)(d + ((bytes_i + 15) / 16) * 16);
+    const char* d = nullptr;
+    TermPlan t;
+    focss_status st = term_plan(c, n_terms, m, n, coef, &d, &t);
+    if (st != FOCSS_OK) return st;
+    const size_t ng = (size_t)t.ng;
+    const float2* dcoef = (const float2*)(d + t.coef_offset);
     cudaStream_t s = c->stream;
-    cudaError_t e = cudaMemcpyAsync(d, hi.data(), bytes_i, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(dcoef, t.coef.data(), sizeof(float2) * t.coef.size(), cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return cuda_check(c, e, "triplet upload");
+    cudaError_t e = cudaSuccess;
     TripletArgs a{};
     a.in = in;
     a.in_bstride = in_bstride;
@@ -232,7 +317,6 @@ focss_status run_triplet_rows(Ctx* c, const float2* in, size_t in_bstride, int m
     }
     count_launch();
     e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // host term vectors go out of scope
     return cuda_check(c, e, "triplet");
 }
 
