@@ -90,10 +90,10 @@ constexpr int kMaxDevices = 64;
 std::mutex g_launch_mutex;
 
 // The cached launch of pass kind `kind` (0 column, 1 row, 2 row with
-// bulk-copy staging) for log2 length lg
+// bulk-copy staging, 3 row in 64-thread CTAs) for log2 length lg
 // on the current device, opted in to `smem` bytes of dynamic shared memory.
 cudaError_t cached_launch(int kind, int lg, size_t smem, Launch* out) {
-    static Launch cache[kMaxDevices][3][16];
+    static Launch cache[kMaxDevices][4][16];
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
@@ -103,6 +103,11 @@ cudaError_t cached_launch(int kind, int lg, size_t smem, Launch* out) {
     if (!l.fn) {
         l = kind == 0 ? col_launch_for(lg) : row_launch_for(lg);
         if (kind == 2) l.fn = l.fn_bulk;
+        if (kind == 3) {
+            l.fn = l.fn_narrow;
+            l.threads = l.per_block_narrow * (l.threads / l.per_block);
+            l.per_block = l.per_block_narrow;
+        }
     }
     if (!l.fn) return cudaErrorInvalidValue;
     if (!l.attr_set || smem > l.smem) {
@@ -142,9 +147,14 @@ cudaError_t launch_row(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
     if (!l.fn) return cudaErrorInvalidValue;
     const int P = l.threads / l.per_block;
     const int Q = p.N2 / P;
-    int R = l.per_block;
+    const int rows = batch * (a.modes > 1 ? a.modes : 1);
+    // few row blocks in the whole launch: 64-thread CTAs spread them over more SMs
+    const bool narrow = p.row_staging != FOCSS_STAGING_BULK && (long long)(p.N1 / l.per_block) * rows < sm_count() &&
+                        p.N1 % l.per_block_narrow == 0;
+    const int kind = p.row_staging == FOCSS_STAGING_BULK ? 2 : narrow ? 3 : 1;
+    int R = narrow ? l.per_block_narrow : l.per_block;
     const size_t smem = sizeof(float4) * ((size_t)p.N2 + 512) + sizeof(float2) * (size_t)R * Q * (P + 1);
-    cudaError_t e = cached_launch(p.row_staging == FOCSS_STAGING_BULK ? 2 : 1, p.log2N2, smem, &l);
+    cudaError_t e = cached_launch(kind, p.log2N2, smem, &l);
     if (e != cudaSuccess) return e;
     a.N = p.N;
     a.N1 = p.N1;

@@ -636,6 +636,8 @@ typedef void (*PassFn)(PassArgs);
 struct Launch {
     PassFn fn = nullptr;
     PassFn fn_bulk = nullptr;  // row pass with bulk-copy staging
+    PassFn fn_narrow = nullptr;  // row pass in 64-thread CTAs (few rows in the whole launch)
+    int per_block_narrow = 0;
     int threads = 0, per_block = 0;
     size_t smem = 0;
     bool attr_set = false;
@@ -654,6 +656,10 @@ struct RowShape {
     static constexpr int R0 = 256 / P;
     static constexpr int RH = (N2 / 2 > 16 ? N2 / 2 : 16);
     static constexpr int R = R0 < RH ? R0 : RH;
+    // 64-thread CTAs: when a launch has fewer row blocks than the GPU has SMs
+    // (a single field of 2^17 samples at a 128 x 1024 split has 16), four
+    // times as many SMs take part.
+    static constexpr int RN = 64 / P;
 };
 
 Launch col_launch_for(int log2N1);
@@ -677,6 +683,8 @@ Launch row_launch_for(int log2N2);
         Launch l;                                                              \
         l.fn = row_kernel<L, RowShape<L>::R>;                                  \
         l.fn_bulk = row_kernel_bulk<L, RowShape<L>::R>;                        \
+        l.fn_narrow = row_kernel<L, RowShape<L>::RN>;                          \
+        l.per_block_narrow = RowShape<L>::RN;                                  \
         l.threads = RowShape<L>::R * PQ<L>::P;                                 \
         l.per_block = RowShape<L>::R;                                          \
         return l;                                                              \
