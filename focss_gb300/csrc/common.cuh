@@ -73,6 +73,15 @@ __device__ __forceinline__ float2 kerr_rotate(float2 v, float phi) {
 }
 
 // Block-wide reductions (blockDim.x multiple of 32, <= 1024).
+// Programmatic dependent launch (kernels launched with the programmatic
+// stream-serialization attribute): pdl_trigger lets the next such kernel in
+// the stream be scheduled now; pdl_wait blocks until the grids this one
+// depends on have completed and their memory is visible (a no-op in a kernel
+// launched without the attribute).  A kernel reads or writes no global memory
+// that its predecessors touch before pdl_wait.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 __device__ __forceinline__ float warp_max(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));

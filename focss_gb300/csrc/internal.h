@@ -46,6 +46,10 @@ struct SsfmParams {
     int grid, total_steps;
     int samples;
     int* n_done;
+    // Derived per-run constants (ssfm_derive): kappa gamma, |kappa gamma|,
+    // beta2/2 dw^2 / (2 pi) (the dispersion phase per metre of hl, in turns),
+    // -alpha/2 and 1/samples.
+    double kg, kg_abs, disp_c, loss_c, inv_samples;
     // Step-grid record / replay (both null on ordinary runs).  Realization b
     // writes |h_i| of its nonlinear steps to h_record[b*h_cap + i] (i < h_cap;
     // SsfmState::recorded counts them all), or takes the h_count[b] step sizes
@@ -55,6 +59,15 @@ struct SsfmParams {
     const int* h_count;
     int h_cap;
 };
+
+// Fills the derived constants of p from its fiber and grid fields.
+inline void ssfm_derive(SsfmParams& p) {
+    p.kg = p.kappa * p.gamma;
+    p.kg_abs = p.kg < 0 ? -p.kg : p.kg;
+    p.disp_c = 0.5 * p.beta2 * p.dw * p.dw / (2.0 * 3.14159265358979323846);
+    p.loss_c = -0.5 * p.alpha;
+    p.inv_samples = 1.0 / (double)p.samples;  // exact: samples is a power of 2
+}
 
 // Twiddle tables, double-float {re_hi, im_hi, re_lo, im_lo}, packed in one
 // device buffer (offsets in entries):

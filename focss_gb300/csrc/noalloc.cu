@@ -145,6 +145,7 @@ extern "C" FOCSS_API focss_status focss_ssfm_run_noalloc(void* stream, void* dat
     a.prm.total_steps = o.total_steps;
     a.prm.samples = samples;
     a.prm.n_done = sc->counters;
+    ssfm_derive(a.prm);
 
     if (o.grid == FOCSS_UNIFORM) {
         for (long long i = 0; i < (long long)o.total_steps + 2 && e == cudaSuccess; ++i) {

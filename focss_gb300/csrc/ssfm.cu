@@ -90,10 +90,11 @@ constexpr int kMaxDevices = 64;
 std::mutex g_launch_mutex;
 
 // The cached launch of pass kind `kind` (0 column, 1 row, 2 row with
-// bulk-copy staging, 3 row in 64-thread CTAs) for log2 length lg
-// on the current device, opted in to `smem` bytes of dynamic shared memory.
+// bulk-copy staging, 3 row in 64-thread CTAs, 4 column in 64-thread CTAs) for
+// log2 length lg on the current device, opted in to `smem` bytes of dynamic
+// shared memory.
 cudaError_t cached_launch(int kind, int lg, size_t smem, Launch* out) {
-    static Launch cache[kMaxDevices][4][16];
+    static Launch cache[kMaxDevices][5][16];
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
@@ -101,9 +102,9 @@ cudaError_t cached_launch(int kind, int lg, size_t smem, Launch* out) {
     std::lock_guard<std::mutex> lock(g_launch_mutex);
     Launch& l = cache[dev][kind][lg];
     if (!l.fn) {
-        l = kind == 0 ? col_launch_for(lg) : row_launch_for(lg);
+        l = kind == 0 || kind == 4 ? col_launch_for(lg) : row_launch_for(lg);
         if (kind == 2) l.fn = l.fn_bulk;
-        if (kind == 3) {
+        if (kind == 3 || kind == 4) {
             l.fn = l.fn_narrow;
             l.threads = l.per_block_narrow * (l.threads / l.per_block);
             l.per_block = l.per_block_narrow;
@@ -120,15 +121,48 @@ cudaError_t cached_launch(int kind, int lg, size_t smem, Launch* out) {
     return cudaSuccess;
 }
 
+// Launches a pass kernel.  Launched directly into a stream, it carries
+// programmatic stream serialization: when the previous operation in the
+// stream is a kernel, this one may be scheduled as soon as that kernel's CTAs
+// have all started, and runs up to its pdl_wait (the column pass computes its
+// six-step factors there) while the other finishes, instead of paying the
+// launch latency after it (one 2^17 field, 100 steps through focss_ssfm_run:
+// 2.31 -> 2.13 ms).  Captured into a graph it is a plain kernel node: graph
+// launches already hide that latency, and programmatic edges there measured
+// slower (800 steps of one 2^17 field: 17.8 -> 19.9 us per step).
+cudaError_t launch_pass(const Launch& l, dim3 grid, int threads, size_t smem, cudaStream_t s, const PassArgs& a) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    const cudaError_t ce = cudaStreamIsCapturing(s, &cs);
+    if (ce != cudaSuccess) return ce;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = cs == cudaStreamCaptureStatusNone ? 1 : 0;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, l.fn, a);
+    count_launch();
+    const cudaError_t last = cudaGetLastError();  // consumed, as after a <<<>>> launch
+    return e != cudaSuccess ? e : last;
+}
+
 cudaError_t launch_col(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
     Launch l = col_launch_for(p.log2N1);
     if (!l.fn) return cudaErrorInvalidValue;
     const int modes = a.modes > 1 ? a.modes : 1;
+    // few column blocks in the whole launch: 64-thread CTAs spread them over more SMs
+    const bool narrow = l.per_block_narrow < l.per_block &&
+                        (long long)(p.N2 / l.per_block) * batch < sm_count() && p.N2 % l.per_block_narrow == 0;
+    const int C = narrow ? l.per_block_narrow : l.per_block;
     // s_fc (N1) + six-step table (Q x C, Q = N1/P) + exchange (N1 x C per mode)
     const int P = l.threads / l.per_block;
-    const size_t smem = sizeof(float4) * ((size_t)p.N1 + (size_t)(p.N1 / P) * l.per_block) +
-                        sizeof(float2) * (size_t)p.N1 * l.per_block * modes;
-    cudaError_t e = cached_launch(0, p.log2N1, smem, &l);
+    const size_t smem = sizeof(float4) * ((size_t)p.N1 + (size_t)(p.N1 / P) * C) +
+                        sizeof(float2) * (size_t)p.N1 * C * modes;
+    cudaError_t e = cached_launch(narrow ? 4 : 0, p.log2N1, smem, &l);
     if (e != cudaSuccess) return e;
     a.N = p.N;
     a.N1 = p.N1;
@@ -136,10 +170,7 @@ cudaError_t launch_col(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
     a.log2N2 = p.log2N2;
     a.tw = p.tw;
     a.batch = batch;
-    dim3 grid(p.N2 / l.per_block, batch);
-    l.fn<<<grid, l.threads * modes, smem, s>>>(a);
-    count_launch();
-    return cudaGetLastError();
+    return launch_pass(l, dim3(p.N2 / l.per_block, batch), l.threads * modes, smem, s, a);
 }
 
 cudaError_t launch_row(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
@@ -163,10 +194,7 @@ cudaError_t launch_row(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
     a.tw = p.tw;
     a.batch = batch;
     if (p.N1 % R != 0) return cudaErrorInvalidValue;
-    dim3 grid(p.N1 / R, batch * (a.modes > 1 ? a.modes : 1));
-    l.fn<<<grid, l.threads, smem, s>>>(a);
-    count_launch();
-    return cudaGetLastError();
+    return launch_pass(l, dim3(p.N1 / R, batch * (a.modes > 1 ? a.modes : 1)), l.threads, smem, s, a);
 }
 
 // ---------------------------------------------------------------- SSFM driver
@@ -235,6 +263,7 @@ PassArgs ssfm_args(const Field* f, const focss_fiber& fib, const focss_ssfm_opts
     a.prm.total_steps = o.total_steps;
     a.prm.samples = N;
     a.prm.n_done = n_done;
+    ssfm_derive(a.prm);
     a.modes = f->modes;
     return a;
 }

@@ -10,9 +10,37 @@
 namespace fg {
 
 // ---------------------------------------------------------------- state update
+// The state update runs on one thread between the passes of every split step,
+// so its FP64 dependency chain is on the critical path of small launches
+// (FP64 instructions have long latency on this GPU: the library exp() alone
+// takes ~1600 cycles).  The per-run constants come precomputed in SsfmParams
+// (ssfm_derive) and the per-step exponential is the short-chain one below.
+
+// exp(x), |x| < 700, to ~2 ulp: Cody & Waite's reduction x = k ln2 + r with a
+// two-part ln 2 (the 42-bit head makes k ln2_hi exact for |k| < 2^11),
+// |r| <= ln2/2, then the Taylor series of exp(r) to degree 13 (remainder below
+// 2^-55 relative) evaluated by Estrin's scheme (depth 4 instead of Horner's
+// 13), and 2^k put into the exponent field.
+__device__ __forceinline__ double exp_short(double x) {
+    constexpr double kLog2e = 1.4426950408889634;
+    constexpr double kLn2Hi = 0x1.62e42fefa38p-1, kLn2Lo = 0x1.ef35793c7673p-45;
+    constexpr double c2 = 1.0 / 2, c3 = 1.0 / 6, c4 = 1.0 / 24, c5 = 1.0 / 120, c6 = 1.0 / 720,
+                     c7 = 1.0 / 5040, c8 = 1.0 / 40320, c9 = 1.0 / 362880, c10 = 1.0 / 3628800,
+                     c11 = 1.0 / 39916800, c12 = 1.0 / 479001600, c13 = 1.0 / 6227020800.0;
+    const double k = rint(x * kLog2e);
+    const double r = fma(-k, kLn2Lo, fma(-k, kLn2Hi, x));
+    const double r2 = r * r, r4 = r2 * r2, r8 = r4 * r4;
+    const double q0 = fma(r2, fma(r, c3, c2), 1.0 + r);
+    const double q1 = fma(r2, fma(r, c7, c6), fma(r, c5, c4));
+    const double q2 = fma(r2, fma(r, c11, c10), fma(r, c9, c8));
+    const double q3 = fma(r, c13, c12);
+    const double e = fma(r8, fma(r4, q3, q2), fma(r4, q1, q0));
+    return e * __longlong_as_double((long long)(1023 + (int)k) << 52);
+}
+
 __device__ __forceinline__ double adaptive_estimate(const SsfmParams& p, float peak) {
-    // src/focss/solver/ssfm.cpp:136-140
-    const double argument = fabs(p.kappa * p.gamma);
+    // src/focss/solver/ssfm.cpp:136-140 (argument = |kappa gamma|, kg_abs)
+    const double argument = p.kg_abs;
     const double phase_shift = argument * (double)peak;
     const double h = p.max_phase / phase_shift;
     return p.max_step < h ? p.max_step : h;
@@ -30,10 +58,10 @@ __device__ __forceinline__ double log_step(const SsfmParams& p, int K, int i) {
 __device__ __forceinline__ void turns_fix96(double a, unsigned long long& hi, unsigned long long& lo) {
     const double ab = fabs(a);
     const double fr = ab - floor(ab);             // exact
-    const double s64 = ldexp(fr, 64);             // exact, < 2^64
+    const double s64 = fr * 0x1p64;               // exact, < 2^64
     const double h = floor(s64);
     hi = __double2ull_rz(h);
-    lo = __double2ull_rz(ldexp(s64 - h, 32));     // < 2^32
+    lo = __double2ull_rz((s64 - h) * 0x1p32);     // < 2^32
     if (a < 0) {
         if (lo == 0) {
             hi = 0ull - hi;
@@ -141,16 +169,18 @@ __device__ __noinline__ static void ssfm_advance(SsfmState& s, const SsfmParams&
         s.recorded++;
     }
     s.hl = hl;
-    const double a = 0.5 * p.beta2 * hl * p.dw * p.dw / (2.0 * 3.14159265358979323846);
-    turns_fix96(a, s.disp_hi, s.disp_lo);
+    turns_fix96(p.disp_c * hl, s.disp_hi, s.disp_lo);  // beta2/2 hl dw^2 in turns
     // FP32 gain with error feedback: the running product of applied gains
     // tracks the exact FP64 product to one rounding instead of drifting.
-    const double g = exp(-0.5 * p.alpha * hl) / (double)p.samples;
-    const float g32 = (float)(g * s.gain_ratio);
-    s.gain_ratio = s.gain_ratio * g / (double)g32;
+    // ratio' = t / g32 = 1 + (t - g32) / g32 with t - g32 exact (Sterbenz) and
+    // ~2^-24 relative, so the FP32 reciprocal of g32 carries it to ~2^-48.
+    const double g = exp_short(p.loss_c * hl) * p.inv_samples;
+    const double t = g * s.gain_ratio;
+    const float g32 = (float)t;
+    s.gain_ratio = fma(t - (double)g32, (double)__frcp_rn(g32), 1.0);
     s.lin_gain = g32;
     s.row_active = 1;
-    s.kerr_coef = (float)(p.kappa * p.gamma * s.h);
+    s.kerr_coef = (float)(p.kg * s.h);
 }
 
 // ---------------------------------------------------------------- column pass
@@ -290,6 +320,13 @@ __global__ void __launch_bounds__(2 * C * ColFFT<N1>::P, 1) col_kernel(const Pas
     float2* sx = s_x0 + (size_t)mo * N1 * C;
     __shared__ float red[64];
 
+    // The six-step factors depend on nothing in memory: computed while the
+    // previous pass finishes (programmatic dependent launch).
+    pdl_trigger();
+    const int log2N = a.log2N2 + ilog2c(N1);
+    for (int i = threadIdx.x; i < Q * C; i += blockDim.x)
+        s_B[i] = sixstep_factor((blockIdx.x * C + i % C) * a1 * (i / C), log2N);
+    pdl_wait();
     const int b = blockIdx.y;
     SsfmState* st = a.state ? a.state + b : nullptr;
     int op = a.op;
@@ -297,10 +334,7 @@ __global__ void __launch_bounds__(2 * C * ColFFT<N1>::P, 1) col_kernel(const Pas
         op = *(volatile int*)&st->action;
         if (op == COL_IDLE) return;
     }
-    const int log2N = a.log2N2 + ilog2c(N1);
     for (int i = threadIdx.x; i < N1; i += blockDim.x) s_fc[i] = a.tw[i];
-    for (int i = threadIdx.x; i < Q * C; i += blockDim.x)
-        s_B[i] = sixstep_factor((blockIdx.x * C + i % C) * a1 * (i / C), log2N);
     const int modes = a.modes > 1 ? a.modes : 1;
     float pk = 0.0f, sm = 0.0f;
     col_work<N1, C>(a, op, st, a.data + ((size_t)b * modes + mo) * a.N, blockIdx.x * C, s_fc, s_B, C, sx, s_x0, mo,
@@ -441,6 +475,8 @@ __global__ void __launch_bounds__(R* PQ<N2>::P, 2) row_kernel(const PassArgs a) 
     float4* s_T = s_tw + N2;                                 // exp(2 pi i j/512)
     float2* sx = reinterpret_cast<float2*>(s_T + 512);       // R * Q * (P+1)
 
+    pdl_trigger();
+    pdl_wait();
     const int b = blockIdx.y;  // realization * modes + mode
     const SsfmState* st = a.state ? a.state + b / (a.modes > 1 ? a.modes : 1) : nullptr;
     unsigned long long dhi = 0ull, dlo = 0ull;
@@ -496,6 +532,8 @@ __global__ void __launch_bounds__(R* PQ<N2>::P, 2) row_kernel_bulk(const PassArg
     float2* sx = reinterpret_cast<float2*>(s_T + 512);       // R * Q * (P+1): landing zone and exchange
     __shared__ __align__(8) unsigned long long bar;
 
+    pdl_trigger();
+    pdl_wait();
     const int b = blockIdx.y;  // realization * modes + mode
     const SsfmState* st = a.state ? a.state + b / (a.modes > 1 ? a.modes : 1) : nullptr;
     unsigned long long dhi = 0ull, dlo = 0ull;
@@ -636,7 +674,7 @@ typedef void (*PassFn)(PassArgs);
 struct Launch {
     PassFn fn = nullptr;
     PassFn fn_bulk = nullptr;  // row pass with bulk-copy staging
-    PassFn fn_narrow = nullptr;  // row pass in 64-thread CTAs (few rows in the whole launch)
+    PassFn fn_narrow = nullptr;  // the pass in 64-thread CTAs (few blocks in the whole launch)
     int per_block_narrow = 0;
     int threads = 0, per_block = 0;
     size_t smem = 0;
@@ -648,6 +686,11 @@ struct Launch {
 template <int N1>
 struct ColShape {
     static constexpr int C = N1 >= 1024 ? 8 : 16;
+    // 64-thread CTAs (2 columns at N1 = 512, 4 at 256) when a launch has fewer
+    // column blocks than the GPU has SMs: a single 2^17 field at a 512 x 256
+    // split has 16 blocks of 16 columns, which leaves 136 SMs idle while each
+    // of the 16 runs 16 warps through the whole transform pair.
+    static constexpr int CN = 64 / ColFFT<N1>::P < C ? 64 / ColFFT<N1>::P : C;
 };
 // Row-pass rows per block: must divide N1 (N1 >= max(16, N2/2) for every plan).
 template <int N2>
@@ -672,6 +715,8 @@ Launch row_launch_for(int log2N2);
     Launch col_launch_##LG() {                                                 \
         Launch l;                                                              \
         l.fn = col_kernel<L, ColShape<L>::C>;                                  \
+        l.fn_narrow = col_kernel<L, ColShape<L>::CN>;                          \
+        l.per_block_narrow = ColShape<L>::CN;                                  \
         l.threads = ColShape<L>::C * ColFFT<L>::P;                             \
         l.per_block = ColShape<L>::C;                                          \
         return l;                                                              \
