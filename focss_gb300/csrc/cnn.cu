@@ -13,11 +13,14 @@
 // Input gradient: the same conv with W'[ci][kk][co] = W[co][8-kk][ci].
 // Weight gradient: gW[co][kk][ci] = sum_p g[p][co] in[p+kk-4][ci]
 //   GEMM per tap, K = positions (chunked, atomics).
+#include <cuda.h>  // CUtensorMap (the encoder is reached through the runtime's driver entry point)
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -42,30 +45,40 @@ __device__ __forceinline__ uint32_t pack2(bf16 lo, bf16 hi) {
 // Every forward-type convolution (the four layers, and the input gradients)
 // as a tcgen05 implicit GEMM: D[p][co] with M = 128 positions per tile,
 // N = COUT output channels, K = 9 taps x CIN input channels, accumulated in
-// tensor memory (FP32 columns); one thread issues the MMAs of K = 16 and
-// commits them to an mbarrier, then each warp reads its 32 rows back with
-// tcgen05.ld for the epilogue (bias, ReLU, mask, BF16 or FP32).  A CTA stages
-// the weights once and then runs `tiles` consecutive position tiles, the
-// activations of the next tile copied asynchronously (cp.async) into the
-// second of two buffers while the current tile's MMAs and epilogue run.
-// Shared-memory operands use the no-swizzle K-major canonical layout: rows of
-// 8 consecutive K elements (16 bytes), 8-row core matrices SBO = 128 B apart
-// along M/N, core matrices LBO apart along K.  Activations are stored
-// [k group][row][8] with 136 rows (the tile plus the 4-sample halo on each
-// side), so the operand of tap kk is the same layout starting kk rows
-// (kk x 16 B) further: the im2col is an address offset.  Weights are stored
-// [tap][k group][co][8].
+// tensor memory (FP32 columns), read back with tcgen05.ld for the epilogue
+// (bias, ReLU, mask, BF16 or FP32).  The activation tile holds 136 rows (the
+// tile plus the 4-sample halo on each side), so the operand of tap kk is the
+// same layout starting kk rows further: the im2col is an address offset.
+// 64 input channels: rows of 128 bytes in the 128-byte-swizzled K-major
+// layout, written by one TMA box per tile (CU_TENSOR_MAP_SWIZZLE_128B); the
+// swizzle follows the absolute shared-memory address bits, so a start kk rows
+// into a 1024-byte-aligned tile needs no base offset, and a 16-channel step
+// is 32 bytes along the row.  16 input channels: the no-swizzle K-major
+// canonical layout [k group][row][8] (8-row core matrices SBO = 128 B apart
+// along M, LBO apart along K), one TMA box per 8-channel group.  Weights are
+// stored [tap][k group][co][8] (no swizzle).  The kernel's pipeline is
+// described at conv_fwd_tc_kernel.
 namespace tc {
 constexpr int M = 128, ROWS = M + 2 * HALF;
 constexpr uint32_t SBO = 128;
 constexpr long long kWaitCap = 1ll << 22;  // mbarrier polls before giving up
 
+constexpr int STAGES = 4;                  // activation tiles in flight per CTA
+constexpr int FWD_THREADS = 320;           // producer, MMA, two groups of four epilogue warps
+
 template <int CIN, int COUT>
 struct Shape {
-    static constexpr uint32_t LBO_A = ROWS * 16, LBO_B = COUT * 16;
+    // 64 input channels: an activation tile is 136 rows of 128 bytes in the
+    // 128-byte-swizzled K-major layout (one TMA box per tile); fewer: the
+    // unswizzled layout [k group][row][8] (one box per 8-channel group)
+    static constexpr bool SW128 = CIN == 64;
+    [[maybe_unused]] static constexpr uint32_t LBO_A = ROWS * 16;
+    static constexpr uint32_t LBO_B = COUT * 16;
     static constexpr size_t SMEM_B = (size_t)KW * (CIN / 8) * COUT * 16;
-    static constexpr size_t SMEM_A = (size_t)(CIN / 8) * ROWS * 16;  // one activation buffer (two are used)
-    static constexpr uint32_t TMEM_COLS = COUT < 32 ? 32 : COUT;  // allocation: a power of two >= 32
+    static constexpr uint32_t STAGE_BYTES = (CIN / 8) * ROWS * 16;  // one activation tile
+    static constexpr size_t SMEM = SMEM_B + STAGES * (size_t)STAGE_BYTES + 1024;  // + alignment slack
+    static constexpr uint32_t ACC_COLS = COUT < 32 ? 32 : COUT;   // one FP32 accumulator
+    static constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;           // two: a power of two >= 32
 };
 
 // Shared-memory matrix descriptor: start address, LBO and SBO in 16-byte
@@ -73,6 +86,14 @@ struct Shape {
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
     return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
            (1ull << 46);
+}
+// The same for a K-major operand in the 128-byte swizzled layout (TMA
+// CU_TENSOR_MAP_SWIZZLE_128B): rows of 128 bytes, 8-row groups SBO = 1024 B
+// apart, swizzling mode 2 at bit 61; LBO is not used (encoded 1).  `addr`
+// must be 1024-byte aligned (base offset 0).
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | (1ull << 16) | ((uint64_t)(1024 >> 4) << 32) | (1ull << 46) |
+           (2ull << 61);
 }
 // kind::f16 instruction descriptor: FP32 accumulator (bits 4-5 = 1), BF16 A
 // and B (bits 7-9 and 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at
@@ -83,11 +104,80 @@ __host__ __device__ constexpr uint32_t idesc(int n) {
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+// Waits for the phase of parity `parity` of `bar`, at most kWaitCap polls.
+// Gives up early when *abort is set, and sets it when the polls run out.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity, volatile int* abort) {
+    const uint32_t a = smem_addr(bar);
+    for (long long it = 0; it < kWaitCap; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.b32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (abort && *abort) return false;
+    }
+    if (abort) *abort = 1;
+    return false;
+}
+// D (tensor memory) = A B (+ D when `accumulate`), kind::f16, one CTA.
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, bool accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"((uint32_t)accumulate));
+}
+// Arrives on `bar` once every tcgen05 operation this thread issued so far completes.
+__device__ __forceinline__ void mma_commit(unsigned long long* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smem_addr(bar))
+                 : "memory");
+}
+constexpr int FWD_EPI = FWD_THREADS - 64;  // epilogue threads
+
+// TMA tensor copy of one box at (x, y, z) of a 3-D tensor map into shared
+// memory, completing on `bar` (x * element size must be a multiple of 16 bytes).
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z,
+                                            unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+        : "memory");
+}
+
 // 16-byte asynchronous copy global -> shared; `bytes` = 0 writes zeros.
 __device__ __forceinline__ void cp16(uint32_t dst, const void* src, uint32_t bytes) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
 }
 
+// tcgen05.ld of 16 columns without the wait; wait_ld then waits for every
+// load in flight and ties these registers to the wait, so that no use of
+// them can be scheduled before it.
+__device__ __forceinline__ void ld_x16_async(uint32_t taddr, uint32_t (&u)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]),
+          "=r"(u[8]), "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15])
+        : "r"(taddr));
+}
+__device__ __forceinline__ void wait_ld(uint32_t (&u)[16]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n"
+                 : "+r"(u[0]), "+r"(u[1]), "+r"(u[2]), "+r"(u[3]), "+r"(u[4]), "+r"(u[5]), "+r"(u[6]), "+r"(u[7]),
+                   "+r"(u[8]), "+r"(u[9]), "+r"(u[10]), "+r"(u[11]), "+r"(u[12]), "+r"(u[13]), "+r"(u[14]), "+r"(u[15])
+                 :
+                 : "memory");
+}
 __device__ __forceinline__ void ld_x16(uint32_t taddr, float (&r)[16]) {
     uint32_t u[16];
     asm volatile(
@@ -100,143 +190,227 @@ __device__ __forceinline__ void ld_x16(uint32_t taddr, float (&r)[16]) {
 }
 }  // namespace tc
 
-// in: [B][L][CIN] bf16, W: [COUT][KW][CIN] bf16, bias: [COUT] f32 or null,
+// in: [B][L][CIN] bf16 (read through `amap`, a 3-D tensor map {CIN, L, B}
+// with box {8, ROWS, 1}), W: [COUT][KW][CIN] bf16, bias: [COUT] f32 or null,
 // out [B][L][COUT] (bf16, or f32 when OUT_F32); mask (optional, [B][L][COUT]
-// bf16): multiply the result by (mask > 0).  If the MMAs do not complete
-// within the poll cap the tile is written as NaN.
+// bf16): multiply the result by (mask > 0).
+//
+// Persistent and warp-specialized: the grid covers the SMs, each CTA stages
+// the weights once and takes position tiles i = blockIdx.x + k gridDim.x of
+// all B x ceil(L/128) tiles.  Warp 0 (one thread) loads each tile's
+// activations with TMA tensor copies (cp.async.bulk.tensor: one box of 8
+// channels x 136 rows per 8-channel group, zero-filled outside [0, L)) into a
+// ring of STAGES buffers (mbarriers full / empty); warp 1 (one thread) issues
+// the tile's 9 CIN/16 MMAs into one of two tensor-memory accumulators and
+// commits them to the stage's `empty` barrier and the accumulator's `full`
+// barrier; warps 2-5 (the four lane quarters of tensor memory) run the
+// epilogue of tile k while the MMAs of tile k + 1 and the loads of the tiles
+// after it are in flight, and release the accumulator through `acc_empty`.
+// Every wait is bounded: past kWaitCap polls a role sets `abort`, the others
+// leave their loops, the CTA waits (bounded) for its copies and MMAs in
+// flight, frees its tensor memory and writes its tiles as NaN.
 template <int CIN, int COUT, bool OUT_F32>
-__global__ void __launch_bounds__(128) conv_fwd_tc_kernel(const bf16* __restrict__ in, const bf16* __restrict__ W,
-                                                          const float* __restrict__ bias, void* __restrict__ out,
-                                                          int L, int relu, const bf16* __restrict__ mask, int tiles) {
+__global__ void __launch_bounds__(tc::FWD_THREADS, 1)
+    conv_fwd_tc_kernel(const __grid_constant__ CUtensorMap amap, const bf16* __restrict__ W,
+                       const float* __restrict__ bias, void* __restrict__ out, int L, int B, int relu,
+                       const bf16* __restrict__ mask) {
     using S = tc::Shape<CIN, COUT>;
-    constexpr int KG = CIN / 8;
+    constexpr int KG = CIN / 8, ST = tc::STAGES;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    bf16* Bs = reinterpret_cast<bf16*>(smem_raw);              // [tap][kgroup][co][8]
-    bf16* As = reinterpret_cast<bf16*>(smem_raw + S::SMEM_B);  // 2 x [kgroup][row][8]
-    __shared__ __align__(8) unsigned long long bar;
+    // operands from a 1024-byte boundary (TMA destinations want 128)
+    const uint32_t raw = tc::smem_addr(smem_raw), sbase = (raw + 1023u) & ~1023u;
+    bf16* Bs = reinterpret_cast<bf16*>(smem_raw + (sbase - raw));  // [tap][kgroup][co][8]
+    unsigned char* As = smem_raw + (sbase - raw) + S::SMEM_B;      // ST x [kgroup][row][8]
+    __shared__ __align__(8) unsigned long long full[ST], empty[ST], acc_full[2], acc_empty[2], drain, wready;
     __shared__ uint32_t tmem_base;
+    __shared__ volatile int abort_flag;
     __shared__ float s_bias[COUT];
-    const int b = blockIdx.y;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const bf16* inb = in + (size_t)b * L * CIN;
-    for (int i = threadIdx.x; i < COUT; i += 128) s_bias[i] = bias ? bias[i] : 0.f;
-
-    if (warp == 0) {
+    const int ntiles = (L + tc::M - 1) / tc::M, T = ntiles * B;
+    for (int i = threadIdx.x; i < COUT; i += blockDim.x) s_bias[i] = bias ? bias[i] : 0.f;
+    if (threadIdx.x == 0) {
+        abort_flag = 0;
+        for (int i = 0; i < ST; ++i) {
+            tc::mbar_init(&full[i], 1);
+            tc::mbar_init(&empty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            tc::mbar_init(&acc_full[i], 1);
+            tc::mbar_init(&acc_empty[i], 4);
+        }
+        tc::mbar_init(&drain, 1);
+        tc::mbar_init(&wready, tc::FWD_EPI);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(tc::smem_addr(&tmem_base)),
                      "r"(S::TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
     }
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(tc::smem_addr(&bar)), "r"(1));
-        asm volatile("fence.mbarrier_init.release.cluster;\n");
-    }
-    // weights: 16-byte rows W[co][kk][8g .. 8g+7] -> Bs[(kk*KG + g)*COUT + co],
-    // asynchronous copies committed with the first activation tile
-    const uint4* W4 = reinterpret_cast<const uint4*>(W);
-    const uint32_t bs0 = tc::smem_addr(Bs);
-    for (int i = threadIdx.x; i < KW * KG * COUT; i += 128) {
-        const int co = i % COUT, kg = i / COUT;  // kg = kk*KG + g
-        tc::cp16(bs0 + 16u * i, W4 + ((size_t)co * KW + kg / KG) * KG + kg % KG, 16u);
-    }
-    // activation tile t -> buffer t & 1: As[g][r] = in[p0 - 4 + r][8g .. 8g+7]
-    // (zero outside [0, L)), as asynchronous copies that overlap the previous
-    // tile's MMAs and epilogue
-    const uint4* in4 = reinterpret_cast<const uint4*>(inb);
-    auto stage = [&](int t) {
-        const int p0 = (blockIdx.x * tiles + t) * tc::M;
-        const uint32_t base = tc::smem_addr(As) + (uint32_t)((t & 1) * S::SMEM_A);
-        for (int i = threadIdx.x; i < KG * tc::ROWS; i += 128) {
-            const int g = i / tc::ROWS, r = i % tc::ROWS;
-            const int p = p0 - HALF + r;
-            const bool in_range = p >= 0 && p < L;
-            tc::cp16(base + 16u * i, in_range ? (const void*)(in4 + (size_t)p * KG + g) : (const void*)in4,
-                     in_range ? 16u : 0u);
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = tmem_base;
+    const uint32_t a_base = tc::smem_addr(As), bs0 = tc::smem_addr(Bs);
+    if (warp >= 2) {
+        // the epilogue warps stage the weights while the first tiles load:
+        // 16-byte rows W[co][kk][8g .. 8g+7] -> Bs[(kk*KG + g)*COUT + co],
+        // made visible to the tensor core's proxy before `wready` completes
+        const uint4* W4 = reinterpret_cast<const uint4*>(W);
+        for (int i = threadIdx.x - 64; i < KW * KG * COUT; i += tc::FWD_EPI) {
+            const int co = i % COUT, kg = i / COUT;  // kg = kk*KG + g
+            tc::cp16(bs0 + 16u * i, W4 + ((size_t)co * KW + kg / KG) * KG + kg % KG, 16u);
         }
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-    };
-    const int rem = (L - (int)blockIdx.x * tiles * tc::M + tc::M - 1) / tc::M;  // tiles left from this CTA's first
-    const int n_here = rem < tiles ? rem : tiles;
-    if (n_here > 0) stage(0);
-    uint32_t tmem = 0;
-    bool ok = true;
-    for (int t = 0; t < n_here; ++t) {
-        const int p0 = (blockIdx.x * tiles + t) * tc::M;
-        // this tile's rows (and, for the first, the weights) have landed: the
-        // only group in flight; make them visible to the tensor core's proxy
-        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        tmem = tmem_base;
-        if (threadIdx.x == 0) {
-            const uint32_t a0 = tc::smem_addr(As) + (uint32_t)((t & 1) * S::SMEM_A), b0 = tc::smem_addr(Bs);
-            for (int kk = 0; kk < KW; ++kk)
-#pragma unroll
-                for (int kc = 0; kc < CIN / 16; ++kc) {  // 16 input channels = 2 K core matrices per MMA
-                    const uint64_t ad = tc::smem_desc(a0 + kk * 16 + kc * 2 * S::LBO_A, S::LBO_A, tc::SBO);
-                    const uint64_t bd = tc::smem_desc(b0 + (kk * KG + kc * 2) * S::LBO_B, S::LBO_B, tc::SBO);
-                    const uint32_t acc = (kk | kc) ? 1u : 0u;
-                    asm volatile(
-                        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-                        "l"(ad), "l"(bd), "r"(tc::idesc(COUT)), "r"(acc));
-                }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                tc::smem_addr(&bar)));
-        }
-        // the other buffer was read by the MMAs of tile t - 1, complete before
-        // that tile's epilogue: refill it with tile t + 1
-        if (t + 1 < n_here) stage(t + 1);
-        // bounded wait for this tile's MMAs (barrier phase t)
-        uint32_t done = 0;
-        for (long long it = 0; it < tc::kWaitCap && !done; ++it)
-            asm volatile(
-                "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.b32 %0, 1, 0, p;\n}\n"
-                : "=r"(done)
-                : "r"(tc::smem_addr(&bar)), "r"((uint32_t)(t & 1)));
-        ok = ok && done;
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        tc::mbar_arrive(&wready);
+    }
 
-        const int p = p0 + 32 * warp + lane;
-        const size_t ob = (size_t)b * L * COUT;
-#pragma unroll
-        for (int c0 = 0; c0 < COUT; c0 += 16) {
-            float v[16];
-            tc::ld_x16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
-            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-            if (p < L) {
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    float x = v[j] + s_bias[c0 + j];
-                    if (relu) x = fmaxf(x, 0.f);
-                    if (mask && !(__bfloat162float(mask[ob + (size_t)p * COUT + c0 + j]) > 0.f)) x = 0.f;
-                    v[j] = ok ? x : __int_as_float(0x7fc00000);
-                }
-                if (OUT_F32) {
-                    float4* o = reinterpret_cast<float4*>(reinterpret_cast<float*>(out) + ob + (size_t)p * COUT + c0);
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    int issued = 0;  // producer: tiles whose loads were queued
+    if (warp == 0) {
+        if (lane == 0) {
+            for (int i = blockIdx.x, k = 0; i < T; i += gridDim.x, ++k) {
+                const int s = k % ST;
+                if (k >= ST && !tc::mbar_wait(&empty[s], ((k / ST) & 1) ^ 1, &abort_flag)) break;
+                const int b = i / ntiles, p0 = (i % ntiles) * tc::M;
+                tc::mbar_expect_tx(&full[s], S::STAGE_BYTES);
+                const uint32_t dst = a_base + (uint32_t)s * S::STAGE_BYTES;
+                if constexpr (S::SW128) {
+                    tc::tma_load_3d(dst, &amap, 0, p0 - HALF, b, &full[s]);
                 } else {
-                    uint32_t packed[8];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) packed[j] = pack2(__float2bfloat16(v[2 * j]), __float2bfloat16(v[2 * j + 1]));
-                    uint4* o = reinterpret_cast<uint4*>(reinterpret_cast<bf16*>(out) + ob + (size_t)p * COUT + c0);
-                    o[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-                    o[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+                    for (int g = 0; g < KG; ++g)
+                        tc::tma_load_3d(dst + (uint32_t)g * (tc::ROWS * 16), &amap, 8 * g, p0 - HALF, b, &full[s]);
                 }
+                issued = k + 1;
             }
         }
-        // every warp's reads of the accumulator and of the activation tile
-        // are done before the next tile's MMAs and staging
-        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    } else if (warp == 1) {
+        if (lane == 0 && tc::mbar_wait(&wready, 0, &abort_flag)) {
+            const uint64_t bdesc = tc::smem_desc(bs0, S::LBO_B, tc::SBO);
+            for (int i = blockIdx.x, k = 0; i < T; i += gridDim.x, ++k) {
+                const int s = k % ST, ac = k & 1;
+                if (!tc::mbar_wait(&full[s], (k / ST) & 1, &abort_flag)) break;
+                if (k >= 2 && !tc::mbar_wait(&acc_empty[ac], ((k >> 1) & 1) ^ 1, &abort_flag)) break;
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t d = tmem + (uint32_t)ac * S::ACC_COLS;
+                // descriptors of the stage and of the weights; each MMA adds a
+                // constant offset to the start-address field (addresses stay
+                // below 2^18, so the 14-bit field cannot carry)
+                const uint32_t a0 = a_base + (uint32_t)s * S::STAGE_BYTES;
+                if constexpr (S::SW128) {
+                    // tap kk starts kk rows (kk x 128 B) into the tile and the
+                    // 16-channel step kc 32 B into each row; the stage is
+                    // 1024-byte aligned, so the start's row phase inside the
+                    // 8-row swizzle pattern (the descriptor's base offset) is kk & 7
+                    const uint64_t adesc = tc::smem_desc_sw128(a0);
+#pragma unroll
+                    for (int kk = 0; kk < KW; ++kk)
+#pragma unroll
+                        for (int kc = 0; kc < CIN / 16; ++kc)
+                            tc::mma_bf16(d, adesc + (uint64_t)((kk * 128 + kc * 32) >> 4),
+                                         bdesc + (uint64_t)(((kk * KG + kc * 2) * S::LBO_B) >> 4), tc::idesc(COUT),
+                                         (kk | kc) != 0);
+                } else {
+                    const uint64_t adesc = tc::smem_desc(a0, S::LBO_A, tc::SBO);
+#pragma unroll
+                    for (int kk = 0; kk < KW; ++kk)
+#pragma unroll
+                        for (int kc = 0; kc < CIN / 16; ++kc)  // 16 input channels = 2 K core matrices per MMA
+                            tc::mma_bf16(d, adesc + (uint64_t)((kk * 16 + kc * 2 * S::LBO_A) >> 4),
+                                         bdesc + (uint64_t)(((kk * KG + kc * 2) * S::LBO_B) >> 4), tc::idesc(COUT),
+                                         (kk | kc) != 0);
+                }
+                tc::mma_commit(&empty[s]);    // the stage is free once these MMAs have read it
+                tc::mma_commit(&acc_full[ac]);
+            }
+        }
+    } else {
+        // epilogue group ac = (warp - 2) / 4 takes the tiles of accumulator ac
+        // (every other tile); warp & 3 selects its tensor-memory lanes
+        // 32q .. 32q+31 = tile rows
+        const int q = warp & 3, ac = (warp - 2) >> 2;
+        for (int i = blockIdx.x + ac * gridDim.x, k = ac; i < T; i += 2 * gridDim.x, k += 2) {
+            if (!tc::mbar_wait(&acc_full[ac], (k >> 1) & 1, &abort_flag)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const int b = i / ntiles, p = (i % ntiles) * tc::M + 32 * q + lane;
+            const size_t ob = (size_t)b * L * COUT + (size_t)p * COUT;
+            // the whole row of the accumulator in flight at once, one wait
+            uint32_t raw[COUT / 16][16];
+#pragma unroll
+            for (int c = 0; c < COUT / 16; ++c)
+                tc::ld_x16_async(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(ac * S::ACC_COLS + 16 * c), raw[c]);
+#pragma unroll
+            for (int c = 0; c < COUT / 16; ++c) tc::wait_ld(raw[c]);
+#pragma unroll
+            for (int c0 = 0; c0 < COUT; c0 += 16) {
+                float v[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(raw[c0 / 16][j]);
+                if (p < L) {
+                    uint4 mk[2] = {};
+                    if (mask) {
+                        const uint4* m4 = reinterpret_cast<const uint4*>(mask + ob + c0);
+                        mk[0] = m4[0];
+                        mk[1] = m4[1];
+                    }
+                    const bf16* mb = reinterpret_cast<const bf16*>(mk);
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        float x = v[j] + s_bias[c0 + j];
+                        if (relu) x = fmaxf(x, 0.f);
+                        if (mask && !(__bfloat162float(mb[j]) > 0.f)) x = 0.f;
+                        v[j] = x;
+                    }
+                    if (OUT_F32) {
+                        float4* o = reinterpret_cast<float4*>(reinterpret_cast<float*>(out) + ob + c0);
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) o[u] = make_float4(v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]);
+                    } else {
+                        uint32_t packed[8];
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) packed[j] = pack2(__float2bfloat16(v[2 * j]), __float2bfloat16(v[2 * j + 1]));
+                        uint4* o = reinterpret_cast<uint4*>(reinterpret_cast<bf16*>(out) + ob + c0);
+                        o[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                        o[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+                    }
+                }
+            }
+            // this warp's reads of the accumulator are complete: release it
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&acc_empty[ac]);
+        }
+    }
+    __syncthreads();
+    if (abort_flag) {
+        // drain: the producer's queued copies and the issued MMAs land before
+        // the CTA leaves (bounded again), then its tiles are marked invalid
+        if (warp == 0 && lane == 0)
+            for (int k = issued > ST ? issued - ST : 0; k < issued; ++k) tc::mbar_wait(&full[k % ST], (k / ST) & 1, nullptr);
+        if (warp == 1 && lane == 0) {
+            tc::mma_commit(&drain);  // completes once every MMA this thread issued has
+            tc::mbar_wait(&drain, 0, nullptr);
+        }
         __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        for (int i = blockIdx.x; i < T; i += gridDim.x) {
+            const int b = i / ntiles, p0 = (i % ntiles) * tc::M;
+            for (int e = threadIdx.x; e < tc::M * COUT; e += blockDim.x) {
+                const int p = p0 + e / COUT;
+                if (p >= L) continue;
+                const size_t o = (size_t)b * L * COUT + (size_t)p * COUT + e % COUT;
+                if (OUT_F32)
+                    reinterpret_cast<float*>(out)[o] = __int_as_float(0x7fc00000);
+                else
+                    reinterpret_cast<bf16*>(out)[o] = __float2bfloat16(__int_as_float(0x7fc00000));
+            }
+        }
     }
-    if (warp == 0) {
-        tmem = tmem_base;
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (warp == 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(S::TMEM_COLS));
-    }
 }
 
 // ------------------------------------------------------------ tcgen05 weight gradient
@@ -520,21 +694,53 @@ inline int gridn(size_t n) {
     return (int)std::max<size_t>(1, std::min<size_t>((n + 255) / 256, (size_t)sm_count() * 16));
 }
 
+// cuTensorMapEncodeTiled, found once through the runtime's driver entry point.
+cudaError_t tensor_map_encoder(PFN_cuTensorMapEncodeTiled_v12000* out) {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess) return e;
+        if (q != cudaDriverEntryPointSuccess || !p) return cudaErrorNotSupported;
+        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    *out = fn;
+    return cudaSuccess;
+}
+
 template <int CIN, int COUT, bool F32>
 cudaError_t conv_fwd(const bf16* in, const bf16* W, const float* bias, void* out, int L, int B, int relu,
                      const bf16* mask, cudaStream_t s) {
     using S = tc::Shape<CIN, COUT>;
-    const size_t smem = S::SMEM_B + 2 * S::SMEM_A;
-    cudaError_t e = cudaFuncSetAttribute(conv_fwd_tc_kernel<CIN, COUT, F32>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    auto kern = conv_fwd_tc_kernel<CIN, COUT, F32>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
     if (e != cudaSuccess) return e;
-    // about two waves of CTAs, each running several position tiles on one
-    // staged copy of the weights
-    const int ntiles = (L + tc::M - 1) / tc::M;
-    const int per_item = std::max(1, (sm_count() * 4 + B - 1) / B);
-    const int tiles = std::max(1, (ntiles + per_item - 1) / per_item);
-    conv_fwd_tc_kernel<CIN, COUT, F32><<<dim3((ntiles + tiles - 1) / tiles, B), 128, smem, s>>>(in, W, bias, out, L,
-                                                                                                 relu, mask, tiles);
+    PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    e = tensor_map_encoder(&encode);
+    if (e != cudaSuccess) return e;
+    // activations [B][L][CIN] as a 3-D tensor {CIN, L, B}; one box = all 64
+    // channels (128 bytes, swizzled) or 8 channels (16 bytes) x ROWS positions
+    // of one realization
+    CUtensorMap amap;
+    const cuuint64_t dims[3] = {(cuuint64_t)CIN, (cuuint64_t)L, (cuuint64_t)B};
+    const cuuint64_t strides[2] = {(cuuint64_t)CIN * sizeof(bf16), (cuuint64_t)L * CIN * sizeof(bf16)};
+    const cuuint32_t box[3] = {S::SW128 ? (cuuint32_t)CIN : 8u, (cuuint32_t)tc::ROWS, 1}, estr[3] = {1, 1, 1};
+    if (encode(&amap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<bf16*>(in), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, S::SW128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    // persistent: at most the CTAs that are resident at once (tensor memory
+    // for two accumulators each, 512 columns per SM)
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tc::FWD_THREADS, S::SMEM);
+    if (e != cudaSuccess) return e;
+    per_sm = std::max(1, std::min(per_sm, std::min(2, (int)(512 / S::TMEM_COLS))));
+    const long long tiles = (long long)((L + tc::M - 1) / tc::M) * B;
+    const int grid = (int)std::max(1ll, std::min(tiles, (long long)sm_count() * per_sm));
+    kern<<<grid, tc::FWD_THREADS, S::SMEM, s>>>(amap, W, bias, out, L, B, relu, mask);
     count_launch();
     return cudaGetLastError();
 }
