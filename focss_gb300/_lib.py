@@ -69,6 +69,7 @@ SIGNATURES = {
     "focss_field_ifft": (I, [P]),
     "focss_ssfm_run": (I, [P, P, C.POINTER(CFiber), C.POINTER(CSsfmOpts), D, P]),
     "focss_set_row_staging": (I, [P, I]),
+    "focss_set_pass_staging": (I, [P, I]),
     "focss_ssfm_run_record": (I, [P, P, C.POINTER(CFiber), C.POINTER(CSsfmOpts), D, I, P, P]),
     "focss_ssfm_run_steps": (I, [P, P, C.POINTER(CFiber), P, P, I, D]),
     "focss_amplifier_apply": (I, [P, P, D, D, U64, U64, I]),

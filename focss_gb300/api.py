@@ -396,13 +396,20 @@ def autotune(samples: int, batch: int, ctx: Context | None = None):
 
 
 SPLIT_SINGLE_CTA = -1  # FOCSS_SPLIT_SINGLE_CTA: one CTA per realization, field in shared memory
-STAGING_LOADS, STAGING_BULK = 0, 1  # FOCSS_STAGING_*: how the row pass moves its rows
+STAGING_LOADS, STAGING_BULK, STAGING_TMA = 0, 1, 2  # FOCSS_STAGING_*: how the passes move their data
+
+
+def set_pass_staging(mode: int, ctx: Context | None = None):
+    """Staging of this context's split-step passes: STAGING_LOADS
+    (per-thread coalesced loads, the default), STAGING_BULK (the row pass
+    by TMA bulk copies) or STAGING_TMA (as BULK, and the column pass's tiles
+    by 2-D TMA tensor copies); the results are the same bit for bit."""
+    ctx = ctx or Context.default()
+    check(lib().focss_set_pass_staging(ctx.h, int(mode)), ctx.h)
 
 
 def set_row_staging(mode: int, ctx: Context | None = None):
-    """Row-pass staging of this context's split steps: STAGING_LOADS
-    (per-thread coalesced loads, the default) or STAGING_BULK (TMA bulk
-    copies); the results are the same bit for bit."""
+    """set_pass_staging restricted to STAGING_LOADS and STAGING_BULK."""
     ctx = ctx or Context.default()
     check(lib().focss_set_row_staging(ctx.h, int(mode)), ctx.h)
 

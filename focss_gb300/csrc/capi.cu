@@ -95,7 +95,7 @@ focss_status get_plan_split(Ctx* ctx, int N, int log2N1, const Plan** out) {
         cudaFree(p.tw);
         return cuda_check(ctx, e, "twiddle upload");
     }
-    p.row_staging = ctx->row_staging;
+    p.staging = ctx->staging;
     auto res = ctx->plans.emplace(key, p);
     *out = &res.first->second;
     return FOCSS_OK;
@@ -441,11 +441,17 @@ FOCSS_API focss_status focss_ssfm_run(focss_ctx* c, focss_field* f, const focss_
     return fg::ssfm_run(c, f, *fiber, *opts, direction, steps_out);
 }
 
-FOCSS_API focss_status focss_set_row_staging(focss_ctx* c, int mode) {
-    if (!c || (mode != FOCSS_STAGING_LOADS && mode != FOCSS_STAGING_BULK)) return FOCSS_ERR_INVALID_ARG;
-    c->row_staging = mode;
-    for (auto& kv : c->plans) kv.second.row_staging = mode;
+FOCSS_API focss_status focss_set_pass_staging(focss_ctx* c, int mode) {
+    if (!c || (mode != FOCSS_STAGING_LOADS && mode != FOCSS_STAGING_BULK && mode != FOCSS_STAGING_TMA))
+        return FOCSS_ERR_INVALID_ARG;
+    c->staging = mode;
+    for (auto& kv : c->plans) kv.second.staging = mode;
     return FOCSS_OK;
+}
+
+FOCSS_API focss_status focss_set_row_staging(focss_ctx* c, int mode) {
+    if (mode != FOCSS_STAGING_LOADS && mode != FOCSS_STAGING_BULK) return FOCSS_ERR_INVALID_ARG;
+    return focss_set_pass_staging(c, mode);
 }
 
 // Step-grid record / replay: device copies of the step lists live in scratch

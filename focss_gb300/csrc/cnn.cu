@@ -13,9 +13,7 @@
 // Input gradient: the same conv with W'[ci][kk][co] = W[co][8-kk][ci].
 // Weight gradient: gW[co][kk][ci] = sum_p g[p][co] in[p+kk-4][ci]
 //   GEMM per tap, K = positions (chunked, atomics).
-#include <cuda.h>  // CUtensorMap (the encoder is reached through the runtime's driver entry point)
 #include <cuda_bf16.h>
-#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
@@ -26,6 +24,7 @@
 
 #include "common.cuh"
 #include "internal.h"
+#include "tma_map.h"
 
 namespace fg {
 namespace {
@@ -692,23 +691,6 @@ __global__ void cnn_adam_kernel(float* __restrict__ p, const float* __restrict__
 
 inline int gridn(size_t n) {
     return (int)std::max<size_t>(1, std::min<size_t>((n + 255) / 256, (size_t)sm_count() * 16));
-}
-
-// cuTensorMapEncodeTiled, found once through the runtime's driver entry point.
-cudaError_t tensor_map_encoder(PFN_cuTensorMapEncodeTiled_v12000* out) {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static std::mutex mu;
-    std::lock_guard<std::mutex> lock(mu);
-    if (!fn) {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
-        if (e != cudaSuccess) return e;
-        if (q != cudaDriverEntryPointSuccess || !p) return cudaErrorNotSupported;
-        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }
-    *out = fn;
-    return cudaSuccess;
 }
 
 template <int CIN, int COUT, bool F32>

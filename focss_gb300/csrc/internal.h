@@ -95,7 +95,7 @@ struct PassArgs {
 struct Plan {
     int N = 0, N1 = 0, N2 = 0, log2N1 = 0, log2N2 = 0;
     float4* tw = nullptr;   // device tables (layout above)
-    int row_staging = 0;    // FOCSS_STAGING_*: how the row pass moves its rows
+    int staging = 0;        // FOCSS_STAGING_*: how the passes move their data
 };
 
 struct LoopGraph;  // span_loop.cu
@@ -123,7 +123,7 @@ struct Ctx {
     // split-step FFT split (log2 N1) per length picked by the autotuner or
     // pinned by the caller; lengths absent here use the balanced split
     std::map<int, int> ssfm_split;
-    int row_staging = 0;             // FOCSS_STAGING_* for new plans (focss_set_row_staging)
+    int staging = 0;                 // FOCSS_STAGING_* for new plans (focss_set_pass_staging)
     // instantiated span-loop graphs keyed by shape and parameters, and the
     // streams/events their capture uses (span_loop.cu)
     std::map<std::string, LoopGraph*> loops;

@@ -25,6 +25,7 @@
 #include <mutex>
 
 #include "ssfm_kernels.cuh"
+#include "tma_map.h"
 
 namespace fg {
 
@@ -90,11 +91,11 @@ constexpr int kMaxDevices = 64;
 std::mutex g_launch_mutex;
 
 // The cached launch of pass kind `kind` (0 column, 1 row, 2 row with
-// bulk-copy staging, 3 row in 64-thread CTAs, 4 column in 64-thread CTAs) for
-// log2 length lg on the current device, opted in to `smem` bytes of dynamic
-// shared memory.
+// bulk-copy staging, 3 row in 64-thread CTAs, 4 column in 64-thread CTAs, 5
+// column with TMA tensor staging) for log2 length lg on the current device,
+// opted in to `smem` bytes of dynamic shared memory.
 cudaError_t cached_launch(int kind, int lg, size_t smem, Launch* out) {
-    static Launch cache[kMaxDevices][5][16];
+    static Launch cache[kMaxDevices][6][16];
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
@@ -102,7 +103,7 @@ cudaError_t cached_launch(int kind, int lg, size_t smem, Launch* out) {
     std::lock_guard<std::mutex> lock(g_launch_mutex);
     Launch& l = cache[dev][kind][lg];
     if (!l.fn) {
-        l = kind == 0 || kind == 4 ? col_launch_for(lg) : row_launch_for(lg);
+        l = kind == 0 || kind == 4 || kind == 5 ? col_launch_for(lg) : row_launch_for(lg);
         if (kind == 2) l.fn = l.fn_bulk;
         if (kind == 3 || kind == 4) {
             l.fn = l.fn_narrow;
@@ -112,7 +113,8 @@ cudaError_t cached_launch(int kind, int lg, size_t smem, Launch* out) {
     }
     if (!l.fn) return cudaErrorInvalidValue;
     if (!l.attr_set || smem > l.smem) {
-        e = cudaFuncSetAttribute((const void*)l.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        const void* fn = kind == 5 ? (const void*)l.fn_tma : (const void*)l.fn;
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         l.attr_set = true;
         l.smem = smem;
@@ -150,26 +152,64 @@ cudaError_t launch_pass(const Launch& l, dim3 grid, int threads, size_t smem, cu
     return e != cudaSuccess ? e : last;
 }
 
+// The column pass with TMA tensor staging (FOCSS_STAGING_TMA): a tensor map
+// over the launch's fields (batch x modes x N1 rows of N2 8-byte elements,
+// boxes of C columns x min(N1, 256) rows) passed as a kernel parameter.
+cudaError_t launch_col_tma(const Plan& p, const PassArgs& a, int batch, int modes, size_t smem, cudaStream_t s) {
+    Launch l;
+    cudaError_t e = cached_launch(5, p.log2N1, smem, &l);
+    if (e != cudaSuccess) return e;
+    PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    e = tensor_map_encoder(&encode);
+    if (e != cudaSuccess) return e;
+    CUtensorMap map;
+    const cuuint64_t dims[2] = {(cuuint64_t)p.N2, (cuuint64_t)batch * modes * p.N1};
+    const cuuint64_t strides[1] = {(cuuint64_t)p.N2 * sizeof(float2)};
+    const cuuint32_t box[2] = {(cuuint32_t)l.per_block, (cuuint32_t)(p.N1 < 256 ? p.N1 : 256)}, estr[2] = {1, 1};
+    if (encode(&map, CU_TENSOR_MAP_DATA_TYPE_INT64, 2, a.data, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(p.N2 / l.per_block, batch);
+    cfg.blockDim = dim3(l.threads * modes);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(s, &cs);
+    if (e != cudaSuccess) return e;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = cs == cudaStreamCaptureStatusNone ? 1 : 0;
+    e = cudaLaunchKernelEx(&cfg, l.fn_tma, map, a);
+    count_launch();
+    const cudaError_t last = cudaGetLastError();
+    return e != cudaSuccess ? e : last;
+}
+
 cudaError_t launch_col(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
     Launch l = col_launch_for(p.log2N1);
     if (!l.fn) return cudaErrorInvalidValue;
     const int modes = a.modes > 1 ? a.modes : 1;
     // few column blocks in the whole launch: 64-thread CTAs spread them over more SMs
-    const bool narrow = l.per_block_narrow < l.per_block &&
+    const bool narrow = p.staging != FOCSS_STAGING_TMA && l.per_block_narrow < l.per_block &&
                         (long long)(p.N2 / l.per_block) * batch < sm_count() && p.N2 % l.per_block_narrow == 0;
     const int C = narrow ? l.per_block_narrow : l.per_block;
     // s_fc (N1) + six-step table (Q x C, Q = N1/P) + exchange (N1 x C per mode)
     const int P = l.threads / l.per_block;
     const size_t smem = sizeof(float4) * ((size_t)p.N1 + (size_t)(p.N1 / P) * C) +
                         sizeof(float2) * (size_t)p.N1 * C * modes;
-    cudaError_t e = cached_launch(narrow ? 4 : 0, p.log2N1, smem, &l);
-    if (e != cudaSuccess) return e;
     a.N = p.N;
     a.N1 = p.N1;
     a.N2 = p.N2;
     a.log2N2 = p.log2N2;
     a.tw = p.tw;
     a.batch = batch;
+    if (p.staging == FOCSS_STAGING_TMA) return launch_col_tma(p, a, batch, modes, smem + 128, s);
+    cudaError_t e = cached_launch(narrow ? 4 : 0, p.log2N1, smem, &l);
+    if (e != cudaSuccess) return e;
     return launch_pass(l, dim3(p.N2 / l.per_block, batch), l.threads * modes, smem, s, a);
 }
 
@@ -180,9 +220,9 @@ cudaError_t launch_row(const Plan& p, PassArgs a, int batch, cudaStream_t s) {
     const int Q = p.N2 / P;
     const int rows = batch * (a.modes > 1 ? a.modes : 1);
     // few row blocks in the whole launch: 64-thread CTAs spread them over more SMs
-    const bool narrow = p.row_staging != FOCSS_STAGING_BULK && (long long)(p.N1 / l.per_block) * rows < sm_count() &&
+    const bool narrow = p.staging == FOCSS_STAGING_LOADS && (long long)(p.N1 / l.per_block) * rows < sm_count() &&
                         p.N1 % l.per_block_narrow == 0;
-    const int kind = p.row_staging == FOCSS_STAGING_BULK ? 2 : narrow ? 3 : 1;
+    const int kind = p.staging != FOCSS_STAGING_LOADS ? 2 : narrow ? 3 : 1;
     int R = narrow ? l.per_block_narrow : l.per_block;
     const size_t smem = sizeof(float4) * ((size_t)p.N2 + 512) + sizeof(float2) * (size_t)R * Q * (P + 1);
     cudaError_t e = cached_launch(kind, p.log2N2, smem, &l);

@@ -4,6 +4,8 @@
 #pragma once
 #include <cmath>
 
+#include <cuda.h>  // CUtensorMap
+
 #include "fft.cuh"
 #include "internal.h"
 
@@ -194,7 +196,8 @@ __device__ __noinline__ static void ssfm_advance(SsfmState& s, const SsfmParams&
 template <int N1, int C>
 __device__ __forceinline__ void col_work(const PassArgs& a, int op, const SsfmState* st, float2* data, int n2_0,
                                          const float4* s_fc, const float4* sB, int sB_stride, float2* sx,
-                                         float2* s_x0, int mo, int modes, int gt, int ld, float& pk, float& sm) {
+                                         float2* s_x0, int mo, int modes, int gt, int ld, float& pk, float& sm,
+                                         const float2* src = nullptr, int src_ld = 0) {
     constexpr int P = ColFFT<N1>::P, Q = ColFFT<N1>::Q;
     constexpr bool PAIR = ColFFT<N1>::PAIR;
     // Element j of a thread is time-domain row t + P j; in the spectral
@@ -212,9 +215,13 @@ __device__ __forceinline__ void col_work(const PassArgs& a, int op, const SsfmSt
     const float2 tsA = make_float2(fa.x, fa.y);
     const int qA = __float_as_int(fa.z);
     float2* base = data + n2;
+    // the columns come from `src` (a tile of C columns, rows src_ld apart,
+    // staged in shared memory) when given, else from data
+    const float2* lb = src ? src + c : base;
+    const size_t lld = src ? (size_t)src_ld : (size_t)ld;
     float2 v[Q];
 #pragma unroll
-    for (int j = 0; j < Q; ++j) v[j] = base[(size_t)(op == COL_FWD ? t + P * j : a0 + a1 * j) * ld];
+    for (int j = 0; j < Q; ++j) v[j] = lb[(size_t)(op == COL_FWD ? t + P * j : a0 + a1 * j) * lld];
     __syncthreads();
 
     const ColLayout<P, C> lay{c};
@@ -299,6 +306,31 @@ __device__ __forceinline__ void col_work(const PassArgs& a, int op, const SsfmSt
     for (int j = 0; j < Q; ++j) base[(size_t)(op == COL_INV ? t + P * j : a0 + a1 * j) * ld] = v[j];
 }
 
+// The column-pass CTAs of realization b add their peak and energy to its
+// state; the last one to finish advances the step state (ssfm_advance).
+__device__ __forceinline__ void col_advance(const PassArgs& a, SsfmState* st, int b, int op, float pk, float sm,
+                                            float* red) {
+    block_max_sum(pk, sm, red);
+    if (threadIdx.x == 0) {
+        if (op != COL_INV) {
+            atomicMax(&st->peak_bits, __float_as_uint(pk));
+            atomicAdd(&st->sum, (double)sm);
+        }
+        __threadfence();
+        const unsigned prev = atomicAdd(&st->blocks_done, 1u);
+        if (prev == gridDim.x - 1) {
+            __threadfence();
+            const float peak = __uint_as_float(atomicOr(&st->peak_bits, 0u));
+            const double sum = atomicAdd(&st->sum, 0.0);
+            ssfm_advance(*st, a.prm, b, op, peak, sum);
+            st->peak_bits = 0u;
+            st->sum = 0.0;
+            st->blocks_done = 0u;
+            __threadfence();
+        }
+    }
+}
+
 // A CTA holds the same C columns of every mode of one realization (a.modes
 // groups of C*P threads; 1 or 2 modes), so the Kerr phase can use the power
 // summed over modes (Field::power, src/focss/field.cpp:164-171).  The launch
@@ -339,28 +371,7 @@ __global__ void __launch_bounds__(2 * C * ColFFT<N1>::P, 1) col_kernel(const Pas
     float pk = 0.0f, sm = 0.0f;
     col_work<N1, C>(a, op, st, a.data + ((size_t)b * modes + mo) * a.N, blockIdx.x * C, s_fc, s_B, C, sx, s_x0, mo,
                     modes, threadIdx.x % (C * P), a.N2, pk, sm);
-
-    if (st) {
-        block_max_sum(pk, sm, red);
-        if (threadIdx.x == 0) {
-            if (op != COL_INV) {
-                atomicMax(&st->peak_bits, __float_as_uint(pk));
-                atomicAdd(&st->sum, (double)sm);
-            }
-            __threadfence();
-            const unsigned prev = atomicAdd(&st->blocks_done, 1u);
-            if (prev == gridDim.x - 1) {
-                __threadfence();
-                const float peak = __uint_as_float(atomicOr(&st->peak_bits, 0u));
-                const double sum = atomicAdd(&st->sum, 0.0);
-                ssfm_advance(*st, a.prm, b, op, peak, sum);
-                st->peak_bits = 0u;
-                st->sum = 0.0;
-                st->blocks_done = 0u;
-                __threadfence();
-            }
-        }
-    }
+    if (st) col_advance(a, st, b, op, pk, sm, red);
 }
 
 // ---------------------------------------------------------------- row pass
@@ -562,7 +573,8 @@ __global__ void __launch_bounds__(R* PQ<N2>::P, 2) row_kernel_bulk(const PassArg
     if (st)
         for (int i = threadIdx.x; i < 512; i += blockDim.x) s_T[i] = a.tw[2 * a.N1 + 2 * N2 + i];
     __syncthreads();  // barrier initialised, tables in place
-    if (!mbar_wait_bounded(ub, 0)) {
+    // every thread polls; the CTA leaves together if any of them gave up
+    if (__syncthreads_or(!mbar_wait_bounded(ub, 0))) {
         if (a.fault) atomicExch(a.fault, 1);
         if (threadIdx.x == 0) mbar_wait_bounded(ub, 0);  // the copies must land before the CTA exits
         return;
@@ -585,6 +597,78 @@ __global__ void __launch_bounds__(R* PQ<N2>::P, 2) row_kernel_bulk(const PassArg
         asm volatile("cp.async.bulk.commit_group;" ::: "memory");
         asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // shared memory read before exit
     }
+}
+
+// ---------------------------------------------------------------- column pass, TMA tensor staging
+// The same column pass with the CTA's tile (C columns x N1 rows of each mode,
+// a strided block of the field) moved by the TMA engine as 2-D tensor boxes
+// (cp.async.bulk.tensor.2d, at most 256 rows per box) into the modes'
+// exchange buffers, behind one mbarrier whose wait is bounded; the threads
+// read their elements from there and the results go back with ordinary
+// stores.  `fmap` views the launch's fields as one row-major matrix of
+// batch x modes x N1 rows of N2 8-byte elements, boxes of C x min(N1, 256).
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+template <int N1, int C>
+__global__ void __launch_bounds__(2 * C * ColFFT<N1>::P, 1)
+    col_kernel_tma(const __grid_constant__ CUtensorMap fmap, const PassArgs a) {
+    constexpr int P = ColFFT<N1>::P, Q = ColFFT<N1>::Q;
+    constexpr int a1 = ColFFT<N1>::PAIR ? Q : P;
+    constexpr int BOX = N1 < 256 ? N1 : 256;
+    extern __shared__ float4 smem4[];
+    float4* s_fc = smem4;                                  // column sub-FFT twiddles, (u,t) order
+    float4* s_B = s_fc + N1;                               // six-step factors W_N^{n2 a1 j}, [j][c]
+    // exchange buffers (the TMA landing tiles), N1*C per mode, from a
+    // 128-byte boundary (the launch adds 128 bytes for it)
+    const uint32_t xb = smem_addr(s_B + Q * C), xpad = (128u - (xb & 127u)) & 127u;
+    float2* s_x0 = reinterpret_cast<float2*>(reinterpret_cast<char*>(s_B + Q * C) + xpad);
+    const int mo = threadIdx.x / (C * P);
+    float2* sx = s_x0 + (size_t)mo * N1 * C;
+    __shared__ float red[64];
+    __shared__ __align__(8) unsigned long long bar;
+
+    pdl_trigger();
+    const int log2N = a.log2N2 + ilog2c(N1);
+    for (int i = threadIdx.x; i < Q * C; i += blockDim.x)
+        s_B[i] = sixstep_factor((blockIdx.x * C + i % C) * a1 * (i / C), log2N);
+    pdl_wait();
+    const int b = blockIdx.y;
+    SsfmState* st = a.state ? a.state + b : nullptr;
+    int op = a.op;
+    if (st) {
+        op = *(volatile int*)&st->action;
+        if (op == COL_IDLE) return;  // before any copy is queued
+    }
+    const int modes = a.modes > 1 ? a.modes : 1;
+    const uint32_t ub = smem_addr(&bar);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(ub) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ub),
+                     "r"((uint32_t)(modes * N1 * C * sizeof(float2)))
+                     : "memory");
+        for (int m = 0; m < modes; ++m)
+            for (int h = 0; h < N1 / BOX; ++h)
+                tma_load_2d(smem_addr(s_x0 + (size_t)m * N1 * C + (size_t)h * BOX * C), &fmap, blockIdx.x * C,
+                            (b * modes + m) * N1 + h * BOX, ub);
+    }
+    for (int i = threadIdx.x; i < N1; i += blockDim.x) s_fc[i] = a.tw[i];
+    __syncthreads();  // barrier initialised, tables in place
+    if (__syncthreads_or(!mbar_wait_bounded(ub, 0))) {
+        if (a.fault) atomicExch(a.fault, 1);
+        if (threadIdx.x == 0) mbar_wait_bounded(ub, 0);  // the copies must land before the CTA exits
+        return;
+    }
+    float pk = 0.0f, sm = 0.0f;
+    col_work<N1, C>(a, op, st, a.data + ((size_t)b * modes + mo) * a.N, blockIdx.x * C, s_fc, s_B, C, sx, s_x0, mo,
+                    modes, threadIdx.x % (C * P), a.N2, pk, sm, sx, C);
+    if (st) col_advance(a, st, b, op, pk, sm, red);
 }
 
 // ---------------------------------------------------------------- single CTA
@@ -671,10 +755,12 @@ __global__ void __launch_bounds__(kBlockThreads, BlockShape<N1, N2>::SMEM <= 113
 }
 
 typedef void (*PassFn)(PassArgs);
+typedef void (*ColTmaFn)(CUtensorMap, PassArgs);
 struct Launch {
     PassFn fn = nullptr;
     PassFn fn_bulk = nullptr;  // row pass with bulk-copy staging
     PassFn fn_narrow = nullptr;  // the pass in 64-thread CTAs (few blocks in the whole launch)
+    ColTmaFn fn_tma = nullptr;   // column pass with TMA tensor staging
     int per_block_narrow = 0;
     int threads = 0, per_block = 0;
     size_t smem = 0;
@@ -716,6 +802,7 @@ Launch row_launch_for(int log2N2);
         Launch l;                                                              \
         l.fn = col_kernel<L, ColShape<L>::C>;                                  \
         l.fn_narrow = col_kernel<L, ColShape<L>::CN>;                          \
+        l.fn_tma = col_kernel_tma<L, ColShape<L>::C>;                          \
         l.per_block_narrow = ColShape<L>::CN;                                  \
         l.threads = ColShape<L>::C * ColFFT<L>::P;                             \
         l.per_block = ColShape<L>::C;                                          \

@@ -149,15 +149,20 @@ FOCSS_API focss_status focss_field_ifft(focss_field* field);
 FOCSS_API focss_status focss_ssfm_run(focss_ctx* ctx, focss_field* field, const focss_fiber* fiber,
                                       const focss_ssfm_opts* opts, double direction, int* steps_out);
 
-/* How the split-step row pass moves its rows between HBM and shared memory
+/* How the split-step passes move their data between HBM and shared memory
  * (no reference counterpart): FOCSS_STAGING_LOADS (default) with coalesced
- * 8-byte loads and stores by every thread, FOCSS_STAGING_BULK with the TMA
- * bulk-copy engine (cp.async.bulk, one copy per row behind an mbarrier).
- * The arithmetic is the same, so the results are the same bit for bit.
- * Applies to this context's split-step and transform passes from the next
- * launch on. */
+ * 8-byte loads and stores by every thread; FOCSS_STAGING_BULK with the row
+ * pass's rows moved by the TMA bulk-copy engine (cp.async.bulk, one copy per
+ * row behind an mbarrier); FOCSS_STAGING_TMA as BULK, and the column pass's
+ * tiles (C columns x N1 rows) loaded as 2-D TMA tensor boxes
+ * (cp.async.bulk.tensor.2d).  The arithmetic is the same, so the results are
+ * the same bit for bit.  Applies to this context's split-step and transform
+ * passes from the next launch on.  focss_set_row_staging is the same call
+ * restricted to LOADS and BULK. */
 #define FOCSS_STAGING_LOADS 0
 #define FOCSS_STAGING_BULK 1
+#define FOCSS_STAGING_TMA 2
+FOCSS_API focss_status focss_set_pass_staging(focss_ctx* ctx, int mode);
 FOCSS_API focss_status focss_set_row_staging(focss_ctx* ctx, int mode);
 
 /* Step-grid record and replay.  The reference has no counterpart: SSFM::run
