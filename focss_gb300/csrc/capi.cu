@@ -231,6 +231,17 @@ FOCSS_API focss_status focss_ctx_create(int device, focss_ctx** out) {
     if (!c) return FOCSS_ERR_OOM;
     c->device = device;
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        e = cudaMemPoolCreate(&c->pool, &props);
+    }
+    if (e == cudaSuccess) {
+        unsigned long long keep = ~0ull;  // released blocks stay in the pool
+        e = cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     if (e == cudaSuccess) e = cudaMalloc(&c->d_counters, sizeof(int) * 16);
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_pinned, sizeof(int) * 16);
     if (e != cudaSuccess) {
@@ -255,6 +266,8 @@ FOCSS_API focss_status focss_ctx_destroy(focss_ctx* c) {
     cudaFree(c->d_red);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
     if (c->stream) cudaStreamDestroy(c->stream);
+    // fields still alive keep their blocks; the pool goes when they are freed
+    if (c->pool) cudaMemPoolDestroy(c->pool);
     delete c;
     return FOCSS_OK;
 }
@@ -285,10 +298,12 @@ FOCSS_API focss_status focss_field_create(focss_ctx* c, const focss_domain* d, i
     f->dt = d->time_step;
     f->f0 = d->center_frequency;
     f->batch = batch;
-    cudaError_t e = cudaMalloc(&f->d, sizeof(float2) * f->n());
+    // stream-ordered: the block is usable by work queued on the context's
+    // stream after this call (every library call on the field)
+    cudaError_t e = cudaMallocFromPoolAsync((void**)&f->d, sizeof(float2) * f->n(), c->pool, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(f->d, 0, sizeof(float2) * f->n(), c->stream);
     if (e != cudaSuccess) {
-        cudaFree(f->d);
+        if (f->d) cudaFreeAsync(f->d, c->stream);
         delete f;
         return fg::cuda_check(c, e, "field alloc");
     }
@@ -298,8 +313,8 @@ FOCSS_API focss_status focss_field_create(focss_ctx* c, const focss_domain* d, i
 
 FOCSS_API focss_status focss_field_destroy(focss_field* f) {
     if (!f) return FOCSS_OK;
-    if (f->ctx) cudaStreamSynchronize(f->ctx->stream);
-    cudaFree(f->d);
+    // released after the work already queued on the context's stream
+    if (f->d) cudaFreeAsync(f->d, f->ctx->stream);
     delete f;
     return FOCSS_OK;
 }

@@ -103,6 +103,9 @@ struct LoopGraph;  // span_loop.cu
 struct Ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    // field storage: a stream-ordered pool that keeps released blocks for
+    // reuse, so creating and destroying fields costs no device-wide sync
+    cudaMemPool_t pool = nullptr;
     std::map<long long, Plan> plans;  // key (log2 N1 << 32) | N
     std::string last_error;
     SsfmState* d_state = nullptr;

@@ -101,7 +101,10 @@ FOCSS_API int focss_abi_version(void);
 
 /* ------------------------------------------------------------------ field */
 /* focss::Field(const Domain&) (src/focss/field.cpp:24-38): zero-filled;      */
-/* batch x modes <= 65535 (FOCSS_ERR_INVALID_ARG otherwise).                  */
+/* batch x modes <= 65535 (FOCSS_ERR_INVALID_ARG otherwise).  The storage     */
+/* comes from the context's stream-ordered memory pool (allocated and, on     */
+/* destroy, released in order on the context's stream, with no device-wide   */
+/* synchronization); destroy a context's fields before the context.          */
 FOCSS_API focss_status focss_field_create(focss_ctx* ctx, const focss_domain* domain, int batch,
                                           focss_field** out);
 /* ~Field (src/focss/field.cpp:130, 543-547) */
@@ -128,7 +131,9 @@ FOCSS_API focss_status focss_field_copy_realizations(focss_field* dst, int dst_f
  * src/tasks/wdm_run.cpp:55-77) and back. */
 FOCSS_API focss_status focss_field_copy_modes(focss_field* dst, int dst_first, const focss_field* src, int src_first,
                                               int count);
-/* Device pointer to the complex64 data (for interop); valid until destroy. */
+/* Device pointer to the complex64 data (for interop); valid until destroy,  */
+/* ordered on the context's stream (synchronize the context before using it */
+/* from another stream).                                                    */
 FOCSS_API void* focss_field_device_ptr(focss_field* field);
 /* Field::operator*=(const complex_t&) (src/focss/field.cpp:387-391). */
 FOCSS_API focss_status focss_field_scale(focss_field* field, double re, double im);
