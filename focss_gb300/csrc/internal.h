@@ -20,6 +20,7 @@ struct SsfmState {
     double hl;                     // signed linear step of the next row pass
     double sum;                    // sum |A|^2 accumulator (LOGARITHMIC estimate)
     double gain_ratio;             // prod(exact gains) / prod(applied FP32 gains) (error feedback)
+    double g_exact;                // exp(-alpha*hl/2)/N of the current hl (reused while hl repeats)
     unsigned long long disp_hi;    // beta2/2*hl*dw^2/(2pi) turns per k'^2 as a 96-bit
     unsigned long long disp_lo;    //   fraction: disp_hi * 2^-64 + disp_lo * 2^-96
     float lin_gain;                // exp(-alpha*hl/2)/N for the next row pass (FP32, fed back)

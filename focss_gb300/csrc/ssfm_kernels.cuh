@@ -170,13 +170,22 @@ __device__ __noinline__ static void ssfm_advance(SsfmState& s, const SsfmParams&
         if (s.recorded < p.h_cap) p.h_record[(size_t)b * p.h_cap + s.recorded] = fabs(s.h);
         s.recorded++;
     }
+    // A linear step equal to the previous one (UNIFORM grids, ADAPTIVE steps
+    // at the maximum step size) keeps its dispersion phase and loss factor:
+    // the same values a recomputation would give, without its FP64 chain.
+    double g;
+    if (op_done == COL_KERR && hl == s.hl) {
+        g = s.g_exact;
+    } else {
+        turns_fix96(p.disp_c * hl, s.disp_hi, s.disp_lo);  // beta2/2 hl dw^2 in turns
+        g = exp_short(p.loss_c * hl) * p.inv_samples;
+        s.g_exact = g;
+    }
     s.hl = hl;
-    turns_fix96(p.disp_c * hl, s.disp_hi, s.disp_lo);  // beta2/2 hl dw^2 in turns
     // FP32 gain with error feedback: the running product of applied gains
     // tracks the exact FP64 product to one rounding instead of drifting.
     // ratio' = t / g32 = 1 + (t - g32) / g32 with t - g32 exact (Sterbenz) and
     // ~2^-24 relative, so the FP32 reciprocal of g32 carries it to ~2^-48.
-    const double g = exp_short(p.loss_c * hl) * p.inv_samples;
     const double t = g * s.gain_ratio;
     const float g32 = (float)t;
     s.gain_ratio = fma(t - (double)g32, (double)__frcp_rn(g32), 1.0);
@@ -312,16 +321,14 @@ __device__ __forceinline__ void col_advance(const PassArgs& a, SsfmState* st, in
                                             float* red) {
     block_max_sum(pk, sm, red);
     if (threadIdx.x == 0) {
-        if (op != COL_INV) {
-            atomicMax(&st->peak_bits, __float_as_uint(pk));
-            atomicAdd(&st->sum, (double)sm);
-        }
+        if (op != COL_INV) atomicMax(&st->peak_bits, __float_as_uint(pk));
+        if (op == COL_FWD) atomicAdd(&st->sum, (double)sm);  // the energy is read at the first step only
         __threadfence();
         const unsigned prev = atomicAdd(&st->blocks_done, 1u);
         if (prev == gridDim.x - 1) {
             __threadfence();
             const float peak = __uint_as_float(atomicOr(&st->peak_bits, 0u));
-            const double sum = atomicAdd(&st->sum, 0.0);
+            const double sum = op == COL_FWD ? atomicAdd(&st->sum, 0.0) : 0.0;
             ssfm_advance(*st, a.prm, b, op, peak, sum);
             st->peak_bits = 0u;
             st->sum = 0.0;
