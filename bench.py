@@ -910,6 +910,8 @@ def run_ncu_case(args):
           samples/symbol (2^20 samples): map, RRC shaping, channel selection,
           decimation, matched filter, phase search, decisions, certainty,
           error counts, Q;
+    single one realization of N = 2^17 (the plain single-channel shape),
+          UNIFORM 20 steps: the latency-bound small launches (narrow CTAs);
     block single-CTA split-step kernel, 304 realizations of N = 2^14 (2 CTAs
           per SM of work, 40 MB), UNIFORM 10 steps in one launch;
     fit   SINO normal equations (features, z-scores, FP64-accumulated Gram),
@@ -928,6 +930,8 @@ def run_ncu_case(args):
     fib = fg.Fiber(alpha, beta2, gamma, W["span_m"])
     rng = np.random.default_rng(5)
     kind = args.ncu_case
+    fg.set_pass_staging({"loads": fg.STAGING_LOADS, "bulk": fg.STAGING_BULK, "tma": fg.STAGING_TMA}[args.staging],
+                        ctx=ctx)
     if kind == "ssfm":
         x = (synth_wdm() * np.sqrt(1e-3)).astype(np.complex64)
         B = args.ncu_batch
@@ -936,6 +940,13 @@ def run_ncu_case(args):
         f = fg.Field(fg.Domain(1, N, DT, F0), data=np.broadcast_to(x, (B, 1, N)), batch=B, ctx=ctx)
         fg.SSFM(fib, 4).run(f)
         fg.Amplifier(10 ** 1.6, 10 ** 0.5, seed=1).amplify(f)
+    elif kind == "single":
+        n1 = 1 << 17
+        if args.split:
+            fg.set_fft_split(n1, args.split, ctx=ctx)
+        x = ((rng.standard_normal(n1) + 1j * rng.standard_normal(n1)) * np.sqrt(0.8e-3)).astype(np.complex64)
+        f = fg.Field(fg.Domain(1, n1, 1 / 256e9, F0), data=x[None, None], ctx=ctx)
+        fg.SSFM(fib, 20).run(f)
     elif kind == "ppe":
         from focss_gb300 import sino
         R, ns, B = 32, 2 ** 18, 4
@@ -1067,9 +1078,11 @@ def run_ncu_case(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ncu-case", nargs="?", const="ssfm", default=None,
-                    help="small fixed case for ncu captures: ssfm (default), ppe, ldbp, cnn, dsp, block, fit, wdmppe")
+                    help="small fixed case for ncu captures: ssfm (default), single, ppe, ldbp, cnn, dsp, block, fit, wdmppe, aux")
     ap.add_argument("--ncu-batch", type=int, default=40)
     ap.add_argument("--split", type=int, default=0, help="ncu case: log2 N1 of the FFT split (0: balanced)")
+    ap.add_argument("--staging", default="loads", choices=["loads", "bulk", "tma"],
+                    help="ncu case: how the split-step passes move their data (focss_set_pass_staging)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
