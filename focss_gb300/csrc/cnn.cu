@@ -194,20 +194,23 @@ __device__ __forceinline__ void ld_x16(uint32_t taddr, float (&r)[16]) {
 // out [B][L][COUT] (bf16, or f32 when OUT_F32); mask (optional, [B][L][COUT]
 // bf16): multiply the result by (mask > 0).
 //
-// Persistent and warp-specialized: the grid covers the SMs, each CTA stages
-// the weights once and takes position tiles i = blockIdx.x + k gridDim.x of
-// all B x ceil(L/128) tiles.  Warp 0 (one thread) loads each tile's
-// activations with TMA tensor copies (cp.async.bulk.tensor: one box of 8
-// channels x 136 rows per 8-channel group, zero-filled outside [0, L)) into a
-// ring of STAGES buffers (mbarriers full / empty); warp 1 (one thread) issues
-// the tile's 9 CIN/16 MMAs into one of two tensor-memory accumulators and
-// commits them to the stage's `empty` barrier and the accumulator's `full`
-// barrier; warps 2-5 (the four lane quarters of tensor memory) run the
-// epilogue of tile k while the MMAs of tile k + 1 and the loads of the tiles
-// after it are in flight, and release the accumulator through `acc_empty`.
-// Every wait is bounded: past kWaitCap polls a role sets `abort`, the others
-// leave their loops, the CTA waits (bounded) for its copies and MMAs in
-// flight, frees its tensor memory and writes its tiles as NaN.
+// Persistent and warp-specialized: the grid covers the SMs, each CTA takes
+// position tiles i = blockIdx.x + k gridDim.x of all B x ceil(L/128) tiles.
+// Warp 0 (one thread) loads each tile's activations with TMA tensor copies
+// (cp.async.bulk.tensor: one 128-byte-swizzled box of 64 channels x 136 rows,
+// or one box of 8 channels per 8-channel group, zero-filled outside [0, L))
+// into a ring of STAGES buffers (mbarriers full / empty); warp 1 (one thread)
+// waits for the weights, then issues each tile's 9 CIN/16 MMAs into one of
+// two tensor-memory accumulators and commits them to the stage's `empty`
+// barrier and the accumulator's `full` barrier; warps 2-9 stage the weights
+// once (barrier `wready`) and then run the epilogue in two groups of four
+// (group g takes accumulator g, i.e. every other tile; a warp's lane quarter
+// of tensor memory is warp & 3), so the epilogues of two tiles overlap the
+// MMAs and loads of the tiles after them; each group releases its
+// accumulator through `acc_empty`.  Every wait is bounded: past kWaitCap
+// polls a role sets `abort`, the others leave their loops, the CTA waits
+// (bounded) for its copies and MMAs in flight, frees its tensor memory and
+// writes its tiles as NaN.
 template <int CIN, int COUT, bool OUT_F32>
 __global__ void __launch_bounds__(tc::FWD_THREADS, 1)
     conv_fwd_tc_kernel(const __grid_constant__ CUtensorMap amap, const bf16* __restrict__ W,
