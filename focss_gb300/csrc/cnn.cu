@@ -425,46 +425,54 @@ __global__ void __launch_bounds__(tc::FWD_THREADS, 1)
 // channel groups SBO apart.  The input operand of tap kk is the same buffer
 // starting kk rows further (kk x 16 B), so the tap shift along K is an
 // address offset.  A CTA accumulates three taps in tensor memory over its
-// chunk of positions in tiles of 128, the next tile copied asynchronously
-// while the current tile's MMAs run; each buffer has its own mbarrier so a
-// wait never sees two completed phases.  With M = 64 the accumulator row m
-// sits in tensor-memory lane 32 (m / 16) + m % 16.
+// chunk of positions (a whole number of 128-position tiles).  One thread
+// loads the tiles with TMA tensor copies (one box of 8 channels x 128 or 136
+// rows per channel group, zero-filled outside [0, L)) into a ring of
+// WSTAGES buffers (mbarriers full / empty); one thread issues each tile's
+// MMAs and commits them to the tile's `empty` barrier, and after the last
+// tile to `done`; then all warps add the accumulators to gW.  With M = 64
+// the accumulator row m sits in tensor-memory lane 32 (m / 16) + m % 16.
+// Every wait is bounded (kWaitCap polls); a CTA that gives up drains its
+// copies and MMAs (bounded) and adds NaN, so the failure shows in gW.
 namespace tcw {
 constexpr int P = 128;                // positions per tile
 constexpr int PR = P + 2 * HALF;      // input rows per tile (halo)
 constexpr int TAPS = 3;               // taps per CTA
+constexpr int WSTAGES = 3;            // tiles in flight per CTA
 constexpr uint32_t LBO = 128;
 template <int COUT, int CIN>
 struct Shape {
     static constexpr bool G_IS_A = COUT == 64;           // M side = output-gradient channels
     static constexpr int NC = G_IS_A ? CIN : COUT;        // N
-    static constexpr size_t SMEM_G = (size_t)(COUT / 8) * P * 16;
-    static constexpr size_t SMEM_I = (size_t)(CIN / 8) * PR * 16;
-    static constexpr size_t STAGE = (SMEM_G + SMEM_I + 127) / 128 * 128;
-    static constexpr size_t SMEM = 2 * STAGE + 32 * 1024;  // the tail caps residency at 2 CTAs per SM
+    static constexpr uint32_t SMEM_G = (uint32_t)(COUT / 8) * P * 16;
+    static constexpr uint32_t SMEM_I = (uint32_t)(CIN / 8) * PR * 16;
+    static constexpr uint32_t STAGE = SMEM_G + SMEM_I;   // multiples of 128 bytes (TMA destinations)
+    static constexpr size_t SMEM = (size_t)WSTAGES * STAGE + 128;  // + alignment slack
     static constexpr uint32_t TMEM_COLS = TAPS * NC <= 64 ? 64 : 256;
     // kind::f16: FP32 D, BF16 A/B, both MN-major (bits 15, 16), N = NC, M = 64.
     static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) |
                                       ((uint32_t)(NC >> 3) << 17) | ((uint32_t)(64 >> 4) << 24);
     static_assert((COUT == 64 && (CIN == 64 || CIN == 16)) || (COUT == 16 && CIN == 64), "wgrad shapes");
+    static_assert(SMEM_G % 128 == 0 && SMEM_I % 128 == 0, "TMA destinations on 128-byte boundaries");
 };
 }  // namespace tcw
 
 template <int CIN, int COUT>
-__global__ void __launch_bounds__(128) conv_wgrad_tc_kernel(const bf16* __restrict__ gout, const bf16* __restrict__ in,
+__global__ void __launch_bounds__(128) conv_wgrad_tc_kernel(const __grid_constant__ CUtensorMap gmap,
+                                                            const __grid_constant__ CUtensorMap imap,
                                                             float* __restrict__ gW, int L, int chunk) {
     using S = tcw::Shape<COUT, CIN>;
-    constexpr int GG = COUT / 8, IG = CIN / 8;  // 16-byte channel groups
+    constexpr int GG = COUT / 8, IG = CIN / 8, ST = tcw::WSTAGES;  // 16-byte channel groups
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    __shared__ __align__(8) unsigned long long bar[2];
+    __shared__ __align__(8) unsigned long long full[ST], empty[ST], done, drain;
     __shared__ uint32_t tmem_base;
+    __shared__ volatile int abort_flag;
     const int tap0 = blockIdx.x * tcw::TAPS;
     const int b = blockIdx.z;
     const int c0 = blockIdx.y * chunk;
     const int c1 = min(L, c0 + chunk);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint4* g4 = reinterpret_cast<const uint4*>(gout + (size_t)b * L * COUT);
-    const uint4* i4 = reinterpret_cast<const uint4*>(in + (size_t)b * L * CIN);
+    const uint32_t raw = tc::smem_addr(smem_raw), base = (raw + 127u) & ~127u;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(tc::smem_addr(&tmem_base)),
@@ -472,78 +480,73 @@ __global__ void __launch_bounds__(128) conv_wgrad_tc_kernel(const bf16* __restri
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
     }
     if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(tc::smem_addr(&bar[0])), "r"(1));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(tc::smem_addr(&bar[1])), "r"(1));
-        asm volatile("fence.mbarrier_init.release.cluster;\n");
+        abort_flag = 0;
+        for (int i = 0; i < ST; ++i) {
+            tc::mbar_init(&full[i], 1);
+            tc::mbar_init(&empty[i], 1);
+        }
+        tc::mbar_init(&done, 1);
+        tc::mbar_init(&drain, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
-    // tile t -> stage t & 1: G[cg][r] = g[p0 + r][8cg ..], I[cg][r] = in[p0 - 4 + r][8cg ..]
-    // (zero outside [c0, c1) / [0, L))
-    auto stage = [&](int t) {
-        const int p0 = c0 + t * tcw::P;
-        const uint32_t base = tc::smem_addr(smem_raw) + (uint32_t)((t & 1) * S::STAGE);
-        for (int i = threadIdx.x; i < GG * tcw::P; i += 128) {
-            const int cg = i / tcw::P, r = i % tcw::P;
-            const int p = p0 + r;
-            const bool ok = p < c1;
-            tc::cp16(base + 16u * i, ok ? (const void*)(g4 + (size_t)p * GG + cg) : (const void*)g4, ok ? 16u : 0u);
-        }
-        for (int i = threadIdx.x; i < IG * tcw::PR; i += 128) {
-            const int cg = i / tcw::PR, r = i % tcw::PR;
-            const int p = p0 - HALF + r;
-            const bool ok = p >= 0 && p < L;
-            tc::cp16(base + (uint32_t)S::SMEM_G + 16u * i, ok ? (const void*)(i4 + (size_t)p * IG + cg) : (const void*)i4,
-                     ok ? 16u : 0u);
-        }
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-    };
-    auto wait_bar = [&](int t) {  // MMAs of tile t (buffer t & 1, its (t / 2)-th phase)
-        uint32_t done = 0;
-        for (long long it = 0; it < tc::kWaitCap && !done; ++it)
-            asm volatile(
-                "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.b32 %0, 1, 0, p;\n}\n"
-                : "=r"(done)
-                : "r"(tc::smem_addr(&bar[t & 1])), "r"((uint32_t)((t >> 1) & 1)));
-        return done != 0;
-    };
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = tmem_base;
     const int n = c1 > c0 ? (c1 - c0 + tcw::P - 1) / tcw::P : 0;
-    if (n > 0) stage(0);
-    bool ok = true;
-    uint32_t tmem = 0;
-    for (int t = 0; t < n; ++t) {
-        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        tmem = tmem_base;
-        if (threadIdx.x == 0) {
-            const uint32_t gb = tc::smem_addr(smem_raw) + (uint32_t)((t & 1) * S::STAGE);
-            const uint32_t ib = gb + (uint32_t)S::SMEM_G;
+    int issued = 0;
+    if (warp == 0 && lane == 0) {
+        // tile t -> stage t % ST: G[cg][r] = g[p0 + r][8cg ..], I[cg][r] = in[p0 - 4 + r][8cg ..]
+        for (int t = 0; t < n; ++t) {
+            const int s = t % ST;
+            if (t >= ST && !tc::mbar_wait(&empty[s], ((t / ST) & 1) ^ 1, &abort_flag)) break;
+            const int p0 = c0 + t * tcw::P;
+            const uint32_t gb = base + (uint32_t)s * S::STAGE, ib = gb + S::SMEM_G;
+            tc::mbar_expect_tx(&full[s], S::STAGE);
+#pragma unroll
+            for (int cg = 0; cg < GG; ++cg) tc::tma_load_3d(gb + (uint32_t)cg * (tcw::P * 16), &gmap, 8 * cg, p0, b, &full[s]);
+#pragma unroll
+            for (int cg = 0; cg < IG; ++cg)
+                tc::tma_load_3d(ib + (uint32_t)cg * (tcw::PR * 16), &imap, 8 * cg, p0 - HALF, b, &full[s]);
+            issued = t + 1;
+        }
+    } else if (warp == 1 && lane == 0) {
+        for (int t = 0; t < n; ++t) {
+            const int s = t % ST;
+            if (!tc::mbar_wait(&full[s], (t / ST) & 1, &abort_flag)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t gb = base + (uint32_t)s * S::STAGE, ib = gb + S::SMEM_G;
+#pragma unroll
             for (int j = 0; j < tcw::TAPS; ++j) {
                 const int kk = tap0 + j;
 #pragma unroll
                 for (int ks = 0; ks < tcw::P / 16; ++ks) {  // 16 positions = 2 K core matrices per MMA
                     const uint64_t gd = tc::smem_desc(gb + ks * 2 * tcw::LBO, tcw::LBO, tcw::P * 16);
                     const uint64_t id = tc::smem_desc(ib + kk * 16 + ks * 2 * tcw::LBO, tcw::LBO, tcw::PR * 16);
-                    const uint32_t acc = (t | ks) ? 1u : 0u;
-                    asm volatile(
-                        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem + (uint32_t)(S::NC * j)),
-                        "l"(S::G_IS_A ? gd : id), "l"(S::G_IS_A ? id : gd), "r"(S::IDESC), "r"(acc));
+                    tc::mma_bf16(tmem + (uint32_t)(S::NC * j), S::G_IS_A ? gd : id, S::G_IS_A ? id : gd, S::IDESC,
+                                 (t | ks) != 0);
                 }
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                tc::smem_addr(&bar[t & 1])));
+            tc::mma_commit(&empty[s]);  // the stage is free once these MMAs have read it
+            if (t == n - 1) tc::mma_commit(&done);
         }
-        // buffer (t + 1) & 1 was read by the MMAs of tile t - 1
-        if (t >= 1) ok = wait_bar(t - 1) && ok;
-        if (t + 1 < n) stage(t + 1);
     }
-    if (n > 0) ok = wait_bar(n - 1) && ok;
+    __syncthreads();
+    bool ok = !abort_flag && (n == 0 || tc::mbar_wait(&done, 0, &abort_flag));
+    ok = !__syncthreads_or(!ok);
+    if (!ok) {
+        // drain: the queued copies and the issued MMAs complete (bounded) before the CTA leaves
+        if (warp == 0 && lane == 0)
+            for (int t = issued > ST ? issued - ST : 0; t < issued; ++t) tc::mbar_wait(&full[t % ST], (t / ST) & 1, nullptr);
+        if (warp == 1 && lane == 0) {
+            tc::mma_commit(&drain);
+            tc::mbar_wait(&drain, 0, nullptr);
+        }
+        __syncthreads();
+    }
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     // epilogue: lanes 0-15 of warp w hold M-side channel m = 16 w + lane
     if (n > 0) {
-        tmem = tmem_base;
         const int m = 16 * warp + lane;
         for (int j = 0; j < tcw::TAPS; ++j)
 #pragma unroll
@@ -552,21 +555,27 @@ __global__ void __launch_bounds__(128) conv_wgrad_tc_kernel(const bf16* __restri
                 tc::ld_x16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(S::NC * j + q), v);
                 asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
                 if (lane < 16) {
+                    if (!ok)
 #pragma unroll
-                    for (int e = 0; e < 16; ++e) {
-                        const int nn = q + e;
-                        const int co = S::G_IS_A ? m : nn, ci = S::G_IS_A ? nn : m;
-                        atomicAdd(gW + ((size_t)co * KW + tap0 + j) * CIN + ci, ok ? v[e] : __int_as_float(0x7fc00000));
+                        for (int e = 0; e < 16; ++e) v[e] = __int_as_float(0x7fc00000);
+                    if constexpr (S::G_IS_A) {
+                        // 16 consecutive input channels of output channel m: 4 vector reductions
+                        float* dst = gW + ((size_t)m * KW + tap0 + j) * CIN + q;
+#pragma unroll
+                        for (int e = 0; e < 16; e += 4)
+                            asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst + e), "f"(v[e]),
+                                         "f"(v[e + 1]), "f"(v[e + 2]), "f"(v[e + 3])
+                                         : "memory");
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < 16; ++e) atomicAdd(gW + ((size_t)(q + e) * KW + tap0 + j) * CIN + m, v[e]);
                     }
                 }
             }
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
-    if (warp == 0) {
-        tmem = tmem_base;
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(S::TMEM_COLS));
-    }
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(S::TMEM_COLS));
 }
 
 // bias gradient: gb[co] += sum_p g[p][co].  Each lane sums one channel pair
@@ -730,16 +739,36 @@ cudaError_t conv_fwd(const bf16* in, const bf16* W, const float* bias, void* out
     return cudaGetLastError();
 }
 
+// [B][L][C] bf16 as a 3-D tensor {C, L, B}; one box = 8 channels (16 bytes)
+// x `rows` positions of one realization, zero-filled outside the tensor.
+cudaError_t channel_group_map(CUtensorMap* map, const bf16* p, int C, int L, int B, int rows) {
+    PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    const cudaError_t e = tensor_map_encoder(&encode);
+    if (e != cudaSuccess) return e;
+    const cuuint64_t dims[3] = {(cuuint64_t)C, (cuuint64_t)L, (cuuint64_t)B};
+    const cuuint64_t strides[2] = {(cuuint64_t)C * sizeof(bf16), (cuuint64_t)L * C * sizeof(bf16)};
+    const cuuint32_t box[3] = {8, (cuuint32_t)rows, 1}, estr[3] = {1, 1, 1};
+    if (encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<bf16*>(p), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    return cudaSuccess;
+}
+
 template <int CIN, int COUT>
 cudaError_t conv_wgrad(const bf16* g, const bf16* in, float* gW, int L, int B, cudaStream_t s) {
     using S = tcw::Shape<COUT, CIN>;
     static_assert(KW % tcw::TAPS == 0, "taps per CTA");
-    const int chunk = 2048;
+    const int chunk = 2048;  // a whole number of 128-position tiles: no tile crosses a chunk
     cudaError_t e = cudaFuncSetAttribute(conv_wgrad_tc_kernel<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)S::SMEM);
     if (e != cudaSuccess) return e;
-    conv_wgrad_tc_kernel<CIN, COUT><<<dim3(KW / tcw::TAPS, (L + chunk - 1) / chunk, B), 128, S::SMEM, s>>>(g, in, gW, L,
-                                                                                                          chunk);
+    CUtensorMap gmap, imap;
+    e = channel_group_map(&gmap, g, COUT, L, B, tcw::P);
+    if (e == cudaSuccess) e = channel_group_map(&imap, in, CIN, L, B, tcw::PR);
+    if (e != cudaSuccess) return e;
+    conv_wgrad_tc_kernel<CIN, COUT><<<dim3(KW / tcw::TAPS, (L + chunk - 1) / chunk, B), 128, S::SMEM, s>>>(
+        gmap, imap, gW, L, chunk);
     count_launch();
     return cudaGetLastError();
 }
