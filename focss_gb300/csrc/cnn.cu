@@ -632,14 +632,15 @@ __device__ __forceinline__ float2 triplet_at(const float2* __restrict__ row, int
 // x0 = [Re y / s, Im y / s, Re f_0 / s^3, Im f_0 / s^3, ..., 0 ...] (16 channels)
 __global__ void cnn_input_kernel(const float2* __restrict__ y, size_t n, int L, float inv_s, Triplets tr,
                                  bf16* __restrict__ x0) {
+    static_assert(CIN0 == 2 + 2 * kMaxTriplets, "x0 channels: y and the triplets");
     const float inv_s3 = inv_s * inv_s * inv_s;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    // positions < 2^31 (the field's batch x length), so 32-bit index arithmetic
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (int)n; i += gridDim.x * blockDim.x) {
         const float2 v = y[i];
-        bf16* o = x0 + i * CIN0;
-        o[0] = __float2bfloat16(v.x * inv_s);
-        o[1] = __float2bfloat16(v.y * inv_s);
-        const float2* row = y + (i / L) * L;
-        const int k = (int)(i % L);
+        const int r = i / L, k = i - r * L;
+        const float2* row = y + (size_t)r * L;
+        uint32_t w[CIN0 / 2];
+        w[0] = pack2(__float2bfloat16(v.x * inv_s), __float2bfloat16(v.y * inv_s));
 #pragma unroll
         for (int j = 0; j < kMaxTriplets; ++j) {
             float2 f = make_float2(0.f, 0.f);
@@ -647,9 +648,11 @@ __global__ void cnn_input_kernel(const float2* __restrict__ y, size_t n, int L, 
                 f = triplet_at(row, L, k, tr.m[j], tr.n[j]);
                 if (tr.m[j] != 0 || tr.n[j] != 0) f = cadd(f, triplet_at(row, L, k, -tr.m[j], -tr.n[j]));
             }
-            o[2 + 2 * j] = __float2bfloat16(f.x * inv_s3);
-            o[3 + 2 * j] = __float2bfloat16(f.y * inv_s3);
+            w[1 + j] = pack2(__float2bfloat16(f.x * inv_s3), __float2bfloat16(f.y * inv_s3));
         }
+        uint4* o = reinterpret_cast<uint4*>(x0 + (size_t)i * CIN0);  // 32 bytes per position
+        o[0] = make_uint4(w[0], w[1], w[2], w[3]);
+        o[1] = make_uint4(w[4], w[5], w[6], w[7]);
     }
 }
 
@@ -664,11 +667,11 @@ __global__ void cnn_output_kernel(const float2* __restrict__ y, const float* __r
         if (tx) {
             const float2 d = csub(v, tx[i]);
             acc += (double)cnorm(d);
-            bf16* o = g4 + i * COUT4;
-            o[0] = __float2bfloat16(2.f * s * d.x * inv_m);
-            o[1] = __float2bfloat16(2.f * s * d.y * inv_m);
-#pragma unroll
-            for (int c = 2; c < COUT4; ++c) o[c] = __float2bfloat16(0.f);
+            static_assert(COUT4 == 16, "g4: 2 live channels and 14 zeros, 32 bytes per position");
+            uint4* o = reinterpret_cast<uint4*>(g4 + i * COUT4);
+            o[0] = make_uint4(pack2(__float2bfloat16(2.f * s * d.x * inv_m), __float2bfloat16(2.f * s * d.y * inv_m)), 0u,
+                              0u, 0u);
+            o[1] = make_uint4(0u, 0u, 0u, 0u);
         }
     }
     __shared__ double sd[32];
