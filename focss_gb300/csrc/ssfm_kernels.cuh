@@ -194,6 +194,23 @@ __device__ __noinline__ static void ssfm_advance(SsfmState& s, const SsfmParams&
     s.kerr_coef = (float)(p.kg * s.h);
 }
 
+// Column-pass tile width: 16 columns (128-byte rows) below N1 = 512, 8 from
+// there (N1 = 1024: keeps 256 threads and its per-thread register budget;
+// N1 = 512: 256-thread CTAs, four per SM instead of two of 512 at the same
+// 64 registers, so one CTA's barriers stall fewer warps -- 126 x 2^19
+// column pass 0.414 -> 0.400 ms).  MINB is the CTAs per SM of (up to) two
+// mode groups the launch bound sizes the register budget for.
+template <int N1>
+struct ColShape {
+    static constexpr int C = N1 >= 512 ? 8 : 16;
+    static constexpr int MINB = N1 == 512 ? 2 : 1;
+    // 64-thread CTAs (2 columns at N1 = 512, 4 at 256) when a launch has fewer
+    // column blocks than the GPU has SMs: a single 2^17 field at a 512 x 256
+    // split has 16 blocks of 16 columns, which leaves 136 SMs idle while each
+    // of the 16 runs 16 warps through the whole transform pair.
+    static constexpr int CN = 64 / ColFFT<N1>::P < C ? 64 / ColFFT<N1>::P : C;
+};
+
 // ---------------------------------------------------------------- column pass
 // The work of one thread group (C columns x P threads, `gt` its thread index)
 // on columns [n2_0, n2_0 + C) of one mode of one realization; `data` points
@@ -341,14 +358,14 @@ __device__ __forceinline__ void col_advance(const PassArgs& a, SsfmState* st, in
 // A CTA holds the same C columns of every mode of one realization (a.modes
 // groups of C*P threads; 1 or 2 modes), so the Kerr phase can use the power
 // summed over modes (Field::power, src/focss/field.cpp:164-171).  The launch
-// bound of 2 groups x 1 CTA fixes the register budget at 65536 / (2 C P)
-// per thread (64 for N1 = 512: 2 x 512 threads), exactly what two
-// single-mode CTAs (1 group each) need to share an SM, so the two-CTA
-// residency of the single-mode launches cannot be lost to a register
-// heuristic; a bound of (C P, 2) would express the same budget but reject
-// the two-mode launches of 2 C P threads.
+// bound of 2 groups x MINB CTAs fixes the register budget at
+// 65536 / (2 C P MINB) per thread (64 for N1 = 512: 2 x 2 x 256 threads),
+// exactly what 2 MINB single-mode CTAs (1 group each) need to share an SM, so
+// that residency cannot be lost to a register heuristic; a bound of
+// (C P, 2 MINB) would express the same budget but reject the two-mode
+// launches of 2 C P threads.
 template <int N1, int C>
-__global__ void __launch_bounds__(2 * C * ColFFT<N1>::P, 1) col_kernel(const PassArgs a) {
+__global__ void __launch_bounds__(2 * C * ColFFT<N1>::P, ColShape<N1>::MINB) col_kernel(const PassArgs a) {
     constexpr int P = ColFFT<N1>::P, Q = ColFFT<N1>::Q;
     constexpr int a1 = ColFFT<N1>::PAIR ? Q : P;
     extern __shared__ float4 smem4[];
@@ -623,7 +640,7 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
 }
 
 template <int N1, int C>
-__global__ void __launch_bounds__(2 * C * ColFFT<N1>::P, 1)
+__global__ void __launch_bounds__(2 * C * ColFFT<N1>::P, ColShape<N1>::MINB)
     col_kernel_tma(const __grid_constant__ CUtensorMap fmap, const PassArgs a) {
     constexpr int P = ColFFT<N1>::P, Q = ColFFT<N1>::Q;
     constexpr int a1 = ColFFT<N1>::PAIR ? Q : P;
@@ -774,17 +791,6 @@ struct Launch {
     bool attr_set = false;
 };
 
-// Column-pass tile width: 16 columns (128-byte rows) up to N1 = 512, 8 above
-// (keeps 256 threads and the per-thread register budget at N1 = 1024).
-template <int N1>
-struct ColShape {
-    static constexpr int C = N1 >= 1024 ? 8 : 16;
-    // 64-thread CTAs (2 columns at N1 = 512, 4 at 256) when a launch has fewer
-    // column blocks than the GPU has SMs: a single 2^17 field at a 512 x 256
-    // split has 16 blocks of 16 columns, which leaves 136 SMs idle while each
-    // of the 16 runs 16 warps through the whole transform pair.
-    static constexpr int CN = 64 / ColFFT<N1>::P < C ? 64 / ColFFT<N1>::P : C;
-};
 // Row-pass rows per block: must divide N1 (N1 >= max(16, N2/2) for every plan).
 template <int N2>
 struct RowShape {
