@@ -198,7 +198,8 @@ __device__ __noinline__ static void ssfm_advance(SsfmState& s, const SsfmParams&
 // there (N1 = 1024: keeps 256 threads and its per-thread register budget;
 // N1 = 512: 256-thread CTAs, four per SM instead of two of 512 at the same
 // 64 registers, so one CTA's barriers stall fewer warps -- 126 x 2^19
-// column pass 0.414 -> 0.400 ms).  MINB is the CTAs per SM of (up to) two
+// column pass 0.414 -> 0.400 ms; 4 columns, with 32-byte row segments,
+// measured 0.525 ms).  MINB is the CTAs per SM of (up to) two
 // mode groups the launch bound sizes the register budget for.
 template <int N1>
 struct ColShape {
