@@ -256,6 +256,7 @@ FOCSS_API focss_status focss_ctx_destroy(focss_ctx* c) {
     if (!c) return FOCSS_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    for (fg::Field* f : c->fields) f->ctx = nullptr;  // still valid until destroyed; see focss_field_destroy
     for (auto& kv : c->plans) cudaFree(kv.second.tw);
     for (void* p : c->scratch) cudaFree(p);
     for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
@@ -307,14 +308,20 @@ FOCSS_API focss_status focss_field_create(focss_ctx* c, const focss_domain* d, i
         delete f;
         return fg::cuda_check(c, e, "field alloc");
     }
+    c->fields.insert(f);
     *out = f;
     return FOCSS_OK;
 }
 
 FOCSS_API focss_status focss_field_destroy(focss_field* f) {
     if (!f) return FOCSS_OK;
-    // released after the work already queued on the context's stream
-    if (f->d) cudaFreeAsync(f->d, f->ctx->stream);
+    if (f->ctx) {
+        f->ctx->fields.erase(f);
+        // released after the work already queued on the context's stream
+        if (f->d) cudaFreeAsync(f->d, f->ctx->stream);
+    } else if (f->d) {
+        cudaFree(f->d);  // the context went first: a plain (synchronizing) release
+    }
     delete f;
     return FOCSS_OK;
 }

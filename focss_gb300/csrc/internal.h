@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <map>
+#include <set>
 #include <memory>
 #include <string>
 #include <vector>
@@ -133,6 +134,9 @@ struct Ctx {
     std::map<std::string, LoopGraph*> loops;
     std::vector<cudaStream_t> side_streams;
     std::vector<cudaEvent_t> side_events;
+    // live fields of this context: detached (ctx = null) when the context is
+    // destroyed first, so that their later destroy does not touch it
+    std::set<struct Field*> fields;
 };
 
 // Process-wide launch counter (focss_launch_count).  While a graph is being

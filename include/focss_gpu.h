@@ -104,7 +104,8 @@ FOCSS_API int focss_abi_version(void);
 /* batch x modes <= 65535 (FOCSS_ERR_INVALID_ARG otherwise).  The storage     */
 /* comes from the context's stream-ordered memory pool (allocated and, on     */
 /* destroy, released in order on the context's stream, with no device-wide   */
-/* synchronization); destroy a context's fields before the context.          */
+/* synchronization).  A field destroyed after its context is released with  */
+/* a synchronizing free; no other call may use it once the context is gone. */
 FOCSS_API focss_status focss_field_create(focss_ctx* ctx, const focss_domain* domain, int batch,
                                           focss_field** out);
 /* ~Field (src/focss/field.cpp:130, 543-547) */
